@@ -1,0 +1,90 @@
+"""Generate the golden parity fixtures from the G+Smo reference itself.
+
+Builds the reference's own FP64 assembler/solver from its sources (oracle/ref/Makefile, output in
+oracle/_ref/), runs it on seeded problems from gismo_gb300.problems and stores what it returns
+(dof map, CSC matrix, rhs, eliminated-dof values, solution, iterations, L2 error) as compressed
+.npz files next to this script. Run from the repository root, in a container that has the G+Smo
+source tree:
+
+    python tests/golden/make_golden.py --ref /path/to/gismo
+
+The fixtures are committed; nothing on the GPU host runs this script.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from gismo_gb300 import problems as P  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def cases():
+    """name -> Problem. Kept small so the fixtures stay a few MB in total."""
+    out = {}
+    out["square_p2_n4"] = P.square_poisson(4, 2)
+    out["square_p2_n64"] = P.square_poisson(64, 2)  # the reference's CPU-runnable config, full size
+    pr = P.displaced_single_patch(2, (7, 9), (3, 2), 5, 0.05, ufreq=2)
+    out["disp2d_p3x2_7x9"] = pr
+    pr = P.displaced_single_patch(2, (12, 10), (4, 4), 17, 0.05, ufreq=3)
+    out["disp2d_p4_12x10"] = pr
+    out["disp3d_p232_4x5x6"] = P.displaced_single_patch(3, (4, 5, 6), (2, 3, 2), 5, 0.04)
+    out["disp3d_p3_8"] = P.volume_poisson(8, 3, seed=1)
+    pr = P.cube_grid(n=2, n_elem=4, p=2, seed=3, kappa_modes=8)
+    pr.mg_levels = 3
+    pr.tol = 1e-8
+    out["cubegrid2_p2_n4_mg"] = pr
+    pr = P.cube_grid(n=2, n_elem=4, p=2, seed=3, kappa_modes=8)
+    pr.solver = "cg"
+    pr.tol = 1e-8
+    out["cubegrid2_p2_n4_cg"] = pr
+    return out
+
+
+def run_reference(exe: str, prob, workdir: str) -> dict:
+    spec = os.path.join(workdir, "spec.txt")
+    P.write_spec(prob, spec)
+    subprocess.check_call([exe, spec, workdir])
+    ld = lambda n, t: np.fromfile(os.path.join(workdir, n), dtype=t)
+    info = dict(line.split() for line in open(os.path.join(workdir, "info.txt")))
+    with open(spec) as fh:
+        spec_text = fh.read()
+    return dict(
+        dofmap=ld("dofmap.i32", np.int32), csc_ptr=ld("csc_ptr.i32", np.int32), csc_idx=ld("csc_idx.i32", np.int32),
+        csc_val=ld("csc_val.f64", np.float64), rhs=ld("rhs.f64", np.float64), ddof=ld("ddof.f64", np.float64),
+        x=ld("x.f64", np.float64), free=np.int64(info["free"]), nnz=np.int64(info["nnz"]),
+        iters=np.int64(info["iters"]), relres=np.float64(info["error"]), l2=np.float64(info["l2"]),
+        spec=np.array(spec_text),
+    )
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default=os.environ.get("GISMO_REF", ""))
+    ap.add_argument("--only", default="")
+    args = ap.parse_args()
+    mk = ["make", "-C", os.path.join(ROOT, "oracle", "ref"), "-j8"]
+    if args.ref:
+        mk.append(f"REF={args.ref}")
+    subprocess.check_call(mk)
+    exe = os.path.join(ROOT, "oracle", "_ref", "gsref")
+    for name, prob in cases().items():
+        if args.only and name != args.only:
+            continue
+        with tempfile.TemporaryDirectory() as td:
+            res = run_reference(exe, prob, td)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
+        print(name, "free", int(res["free"]), "nnz", int(res["nnz"]), "iters", int(res["iters"]), "l2", float(res["l2"]))
+
+
+if __name__ == "__main__":
+    main()
