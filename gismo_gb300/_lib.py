@@ -1,0 +1,91 @@
+"""ctypes binding of libgsgpu.so (include/gsgpu.h). Loading fails loudly when the library is
+missing: there is no CPU fallback."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgsgpu.so")
+
+# the exported entry points declared in include/gsgpu.h
+EXPORTS = [
+    "gsgpu_create", "gsgpu_destroy", "gsgpu_last_error", "gsgpu_set_problem", "gsgpu_refresh", "gsgpu_set_coefs",
+    "gsgpu_assemble", "gsgpu_sizes", "gsgpu_matrix_csr", "gsgpu_rhs", "gsgpu_fixed_dofs", "gsgpu_dof_map",
+    "gsgpu_solve", "gsgpu_l2_error", "gsgpu_min_jacobian", "gsgpu_assemble_times", "gsgpu_stream",
+    "gsgpu_set_profiling", "gsgpu_spmv_stats",
+]
+
+OK, ERR_INVALID, ERR_CUDA, ERR_BUDGET, ERR_NOT_CONVERGED, ERR_JACOBIAN, ERR_STATE, ERR_TIMEOUT = range(8)
+SOLVER_CG_JACOBI, SOLVER_CG_MG = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+
+
+class Problem(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int), ("npatches", C.c_int),
+        ("degree", C.POINTER(C.c_int)), ("nknots", C.POINTER(C.c_int)), ("knots", C.POINTER(C.c_double)),
+        ("gdegree", C.POINTER(C.c_int)), ("gnknots", C.POINTER(C.c_int)), ("gknots", C.POINTER(C.c_double)),
+        ("coefs", C.POINTER(C.c_double)),
+        ("ninterfaces", C.c_int), ("interfaces", C.POINTER(C.c_int)),
+        ("ndirichlet", C.c_int), ("dirichlet", C.POINTER(C.c_int)),
+        ("kappa_fourier", C.c_int), ("kappa_const", C.c_double), ("kappa_alpha", C.c_double),
+        ("kappa_scale", C.c_double), ("kappa_nmodes", C.c_int), ("kappa_amp", C.POINTER(C.c_double)),
+        ("kappa_k", C.POINTER(C.c_int)), ("kappa_phase", C.POINTER(C.c_double)),
+        ("ufreq", C.c_int), ("quA", C.c_double), ("quB", C.c_int),
+    ]
+
+
+class SolverOpts(C.Structure):
+    _fields_ = [
+        ("method", C.c_int), ("precision", C.c_int), ("tol", C.c_double), ("max_iters", C.c_int),
+        ("mg_levels", C.c_int), ("mg_npre", C.c_int), ("mg_npost", C.c_int), ("mg_damping", C.c_double),
+        ("inner_tol", C.c_double),
+    ]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("relres", C.c_double), ("refinements", C.c_int), ("t_solve_ms", C.c_double)]
+
+
+class GsGpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"gsgpu error {code}: {msg}")
+        self.code = code
+
+
+_LIB = None
+
+
+def lib() -> C.CDLL:
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with __graft_entry__.build() (no CPU fallback exists)")
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        L.gsgpu_create.argtypes = [C.POINTER(vp), C.c_int]
+        L.gsgpu_destroy.argtypes = [vp]
+        L.gsgpu_last_error.argtypes = [vp]
+        L.gsgpu_last_error.restype = C.c_char_p
+        L.gsgpu_set_problem.argtypes = [vp, C.POINTER(Problem)]
+        L.gsgpu_refresh.argtypes = [vp]
+        L.gsgpu_set_coefs.argtypes = [vp, vp]
+        L.gsgpu_assemble.argtypes = [vp, C.c_int]
+        L.gsgpu_sizes.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_longlong), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.gsgpu_matrix_csr.argtypes = [vp, vp, vp, vp]
+        L.gsgpu_rhs.argtypes = [vp, vp]
+        L.gsgpu_fixed_dofs.argtypes = [vp, vp]
+        L.gsgpu_dof_map.argtypes = [vp, vp]
+        L.gsgpu_solve.argtypes = [vp, C.POINTER(SolverOpts), vp, C.POINTER(SolveInfo)]
+        L.gsgpu_l2_error.argtypes = [vp, C.POINTER(C.c_double)]
+        L.gsgpu_min_jacobian.argtypes = [vp, C.POINTER(C.c_double)]
+        L.gsgpu_assemble_times.argtypes = [vp, vp]
+        L.gsgpu_stream.argtypes = [vp, C.POINTER(vp)]
+        L.gsgpu_set_profiling.argtypes = [vp, C.c_int]
+        L.gsgpu_spmv_stats.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        for name in EXPORTS:
+            if name != "gsgpu_last_error":
+                getattr(L, name).restype = C.c_int
+        _LIB = L
+    return _LIB

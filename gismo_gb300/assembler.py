@@ -1,0 +1,188 @@
+"""Python mirror of G+Smo's gsPoissonAssembler / gsConjugateGradient interface over libgsgpu.
+
+    A = GpuPoissonAssembler(problem)          # gsPoissonAssembler(mp, mb, bc, f) + refresh()
+    A.assemble()                              # gsPoissonAssembler::assemble()
+    K, b = A.matrix(), A.rhs()                # gsAssembler::matrix() / rhs()
+    x, info = A.solve(tol=1e-10)              # gsConjugateGradient(K, gsJacobiOp(K)).solve(b, x)
+
+(src/gsAssembler/gsPoissonAssembler.h:35-142, src/gsAssembler/gsAssembler.h:538-639,
+src/gsSolver/gsConjugateGradient.hpp). Errors raise GsGpuError (G+Smo raises std::runtime_error
+from GISMO_ENSURE); non-convergence is reported in the info like gsIterativeSolver::error().
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import GsGpuError, Problem as _CProblem, SolverOpts, SolveInfo
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class PackedProblem:
+    """The C-ABI problem struct (include/gsgpu.h gsgpu_problem) plus the arrays it points to."""
+
+    def __init__(self, prob):
+        d = prob.dim
+        deg, nk, kn, gdeg, gnk, gkn, co = [], [], [], [], [], [], []
+        for pt in prob.patches:
+            for k in range(3):
+                if k < d:
+                    deg.append(pt.degree[k]); nk.append(len(pt.knots[k])); kn.extend(pt.knots[k])
+                    gdeg.append(pt.gdegree[k]); gnk.append(len(pt.gknots[k])); gkn.extend(pt.gknots[k])
+                else:
+                    deg.append(0); nk.append(0); gdeg.append(0); gnk.append(0)
+            co.append(np.ascontiguousarray(pt.coefs, dtype=np.float64).ravel())
+        self.arrays = dict(
+            degree=np.array(deg, np.int32), nknots=np.array(nk, np.int32), knots=np.array(kn, np.float64),
+            gdegree=np.array(gdeg, np.int32), gnknots=np.array(gnk, np.int32), gknots=np.array(gkn, np.float64),
+            coefs=np.concatenate(co), ifaces=np.array(prob.interfaces, np.int32).reshape(-1),
+            dirichlet=np.array(prob.dirichlet, np.int32).reshape(-1),
+            amp=np.ascontiguousarray(prob.kappa_amp, np.float64),
+            kk=np.ascontiguousarray(prob.kappa_k, np.int32).reshape(-1),
+            phase=np.ascontiguousarray(prob.kappa_phase, np.float64),
+        )
+        a = self.arrays
+        s = _CProblem()
+        s.dim = d
+        s.npatches = len(prob.patches)
+        s.degree = _ptr(a["degree"], C.c_int); s.nknots = _ptr(a["nknots"], C.c_int); s.knots = _ptr(a["knots"], C.c_double)
+        s.gdegree = _ptr(a["gdegree"], C.c_int); s.gnknots = _ptr(a["gnknots"], C.c_int)
+        s.gknots = _ptr(a["gknots"], C.c_double)
+        s.coefs = _ptr(a["coefs"], C.c_double)
+        s.ninterfaces = len(prob.interfaces); s.interfaces = _ptr(a["ifaces"], C.c_int)
+        s.ndirichlet = len(prob.dirichlet); s.dirichlet = _ptr(a["dirichlet"], C.c_int)
+        s.kappa_fourier = int(prob.kappa_fourier); s.kappa_const = prob.kappa_const
+        s.kappa_alpha = prob.kappa_alpha; s.kappa_scale = prob.kappa_scale
+        s.kappa_nmodes = len(prob.kappa_amp) if prob.kappa_fourier else 0
+        s.kappa_amp = _ptr(a["amp"], C.c_double); s.kappa_k = _ptr(a["kk"], C.c_int)
+        s.kappa_phase = _ptr(a["phase"], C.c_double)
+        s.ufreq = prob.ufreq; s.quA = prob.quA; s.quB = prob.quB
+        self.struct = s
+
+
+class GpuPoissonAssembler:
+    """gsPoissonAssembler on the GPU: one context per problem (device memory is owned here)."""
+
+    def __init__(self, prob, device: int = 0, refresh: bool = True):
+        self.L = _lib.lib()
+        self.prob = prob
+        self.h = C.c_void_p()
+        rc = self.L.gsgpu_create(C.byref(self.h), device)
+        if rc != _lib.OK:
+            raise GsGpuError(rc, "could not create a context on CUDA device %d" % device)
+        self._packed = PackedProblem(prob)
+        self._check(self.L.gsgpu_set_problem(self.h, C.byref(self._packed.struct)))
+        if refresh:
+            self.refresh()
+
+    def _check(self, rc: int) -> int:
+        if rc != _lib.OK:
+            raise GsGpuError(rc, self.L.gsgpu_last_error(self.h).decode())
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.gsgpu_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- gsAssembler interface ----
+    def refresh(self):
+        self._check(self.L.gsgpu_refresh(self.h))
+
+    def set_coefs(self, coefs: np.ndarray):
+        c = np.ascontiguousarray(coefs, np.float64)
+        self._check(self.L.gsgpu_set_coefs(self.h, c.ctypes.data))
+
+    def assemble(self, precision: str = "fp64"):
+        prec = _lib.PREC_FP64 if precision == "fp64" else _lib.PREC_MIXED
+        self._check(self.L.gsgpu_assemble(self.h, prec))
+
+    def sizes(self):
+        nf, nnz, nb, nl = C.c_int(), C.c_longlong(), C.c_int(), C.c_int()
+        self._check(self.L.gsgpu_sizes(self.h, C.byref(nf), C.byref(nnz), C.byref(nb), C.byref(nl)))
+        return nf.value, nnz.value, nb.value, nl.value
+
+    def numDofs(self) -> int:
+        return self.sizes()[0]
+
+    def csr(self):
+        nf, nnz, _, _ = self.sizes()
+        ptr = np.empty(nf + 1, np.int32)
+        col = np.empty(nnz, np.int32)
+        val = np.empty(nnz, np.float64)
+        self._check(self.L.gsgpu_matrix_csr(self.h, ptr.ctypes.data, col.ctypes.data, val.ctypes.data))
+        return ptr, col, val
+
+    def matrix(self):
+        import scipy.sparse as sp
+        ptr, col, val = self.csr()
+        n = len(ptr) - 1
+        return sp.csr_matrix((val, col, ptr), shape=(n, n))
+
+    def rhs(self) -> np.ndarray:
+        out = np.empty(self.sizes()[0], np.float64)
+        self._check(self.L.gsgpu_rhs(self.h, out.ctypes.data))
+        return out
+
+    def fixedDofs(self) -> np.ndarray:
+        out = np.empty(self.sizes()[2], np.float64)
+        self._check(self.L.gsgpu_fixed_dofs(self.h, out.ctypes.data))
+        return out
+
+    def dofMapper(self) -> np.ndarray:
+        out = np.empty(self.sizes()[3], np.int32)
+        self._check(self.L.gsgpu_dof_map(self.h, out.ctypes.data))
+        return out
+
+    def min_jacobian(self) -> float:
+        v = C.c_double()
+        self._check(self.L.gsgpu_min_jacobian(self.h, C.byref(v)))
+        return v.value
+
+    def assemble_times(self) -> np.ndarray:
+        out = np.zeros(7)
+        self._check(self.L.gsgpu_assemble_times(self.h, out.ctypes.data))
+        return out
+
+    def stream_handle(self) -> int:
+        v = C.c_void_p()
+        self._check(self.L.gsgpu_stream(self.h, C.byref(v)))
+        return v.value or 0
+
+    def set_profiling(self, on: bool):
+        self._check(self.L.gsgpu_set_profiling(self.h, int(on)))
+
+    def spmv_stats(self):
+        n, ms, b = C.c_longlong(), C.c_double(), C.c_double()
+        self._check(self.L.gsgpu_spmv_stats(self.h, C.byref(n), C.byref(ms), C.byref(b)))
+        return n.value, ms.value, b.value
+
+    # ---- gsConjugateGradient ----
+    def solve(self, tol: float = 1e-10, max_iters: int = 1000, method: str = "jacobi", precision: str = "fp64",
+              mg_levels: int = 4, mg_npre: int = 2, mg_npost: int = 2, mg_damping: float = 0.6,
+              inner_tol: float = 1e-4, download: bool = True):
+        o = SolverOpts()
+        o.method = _lib.SOLVER_CG_JACOBI if method == "jacobi" else _lib.SOLVER_CG_MG
+        o.precision = _lib.PREC_FP64 if precision == "fp64" else _lib.PREC_MIXED
+        o.tol, o.max_iters = tol, max_iters
+        o.mg_levels, o.mg_npre, o.mg_npost, o.mg_damping = mg_levels, mg_npre, mg_npost, mg_damping
+        o.inner_tol = inner_tol
+        info = SolveInfo()
+        x = np.empty(self.sizes()[0], np.float64) if download else None
+        rc = self.L.gsgpu_solve(self.h, C.byref(o), x.ctypes.data if download else None, C.byref(info))
+        if rc not in (_lib.OK, _lib.ERR_NOT_CONVERGED):
+            self._check(rc)
+        return x, dict(iterations=info.iterations, relres=info.relres, refinements=info.refinements,
+                       t_solve_ms=info.t_solve_ms, converged=(rc == _lib.OK))

@@ -1,0 +1,612 @@
+// libgsgpu C ABI (include/gsgpu.h): context, refresh (host set-up + upload), assemble (K1-K4 on
+// the device) and the CG solvers.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/gsgpu.h"
+#include "context.h"
+#include "device_funcs.cuh"
+#include "kernels.h"
+#include "kernels_solve.h"
+#include "plan.h"
+
+namespace gsgpu {
+
+CudaError::CudaError(cudaError_t e, const char* expr, const char* file, int line)
+    : std::runtime_error(std::string("CUDA error ") + cudaGetErrorString(e) + " in " + expr + " (" + file + ":" +
+                         std::to_string(line) + ")"),
+      code(e) {}
+
+void* DeviceArena::alloc(size_t bytes) {
+    if (bytes == 0) return nullptr;
+    if (budget > 0 && used + bytes > budget) throw BudgetError("device-memory budget exceeded");
+    void* p = nullptr;
+    GSGPU_CUDA_TRY(cudaMalloc(&p, bytes));
+    used += bytes;
+    sizes.push_back({p, bytes});
+    return p;
+}
+void DeviceArena::release(void* p) {
+    if (!p) return;
+    for (size_t i = 0; i < sizes.size(); ++i)
+        if (sizes[i].first == p) {
+            used -= sizes[i].second;
+            sizes.erase(sizes.begin() + long(i));
+            cudaFree(p);
+            return;
+        }
+}
+void DeviceArena::releaseAll() {
+    for (auto& s : sizes) cudaFree(s.first);
+    sizes.clear();
+    used = 0;
+}
+
+template <typename T>
+static void upload(DeviceArena& A, T*& dptr, const std::vector<T>& h, cudaStream_t s) {
+    A.release(dptr);
+    dptr = static_cast<T*>(A.alloc(h.size() * sizeof(T)));
+    if (!h.empty()) GSGPU_CUDA_TRY(cudaMemcpyAsync(dptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+template <typename T>
+static void allocN(DeviceArena& A, T*& dptr, long long n) {
+    A.release(dptr);
+    dptr = static_cast<T*>(A.alloc(size_t(std::max(0LL, n)) * sizeof(T)));
+}
+
+}  // namespace gsgpu
+
+using namespace gsgpu;
+
+// ---------------------------------------------------------------------------------------------
+// assembly-time helpers
+
+namespace gsgpu {
+
+void Context::buildTables() {
+    auto mk = [&](Tab& T, auto workfn) {
+        std::vector<long long> w;
+        for (const DevPatch& D : L.dev) w.push_back(workfn(D));
+        blockTable(w, launch::kBlock, T.h);
+        upload(arena, T.d, T.h, stream);
+    };
+    {
+        std::vector<long long> w;
+        for (const PfJob& j : L.pfjobs) w.push_back(j.count);
+        blockTable(w, launch::kBlock, tabPf.h);
+        upload(arena, tabPf.d, tabPf.h, stream);
+    }
+    mk(tabCoef, [](const DevPatch& D) { return D.ngeo * D.dim; });
+    mk(tabGeo1, [](const DevPatch& D) {
+        return D.dim == 3 ? (long long)D.dim * 2 * D.gn[2] * D.gn[1] * D.Q[0] : (long long)D.dim * 2 * D.gn[1] * D.Q[0];
+    });
+    mk(tabGeo2, [](const DevPatch& D) { return D.dim == 3 ? (long long)D.dim * 3 * D.gn[2] * D.Q[1] * D.Q[0] : 0LL; });
+    mk(tabPoint, [](const DevPatch& D) { return D.nq; });
+    if (pd.dim == 3) {
+        mk(tabSt[0], [](const DevPatch& D) { return dev::stageWork<31>(D); });
+        mk(tabSt[1], [](const DevPatch& D) { return dev::stageWork<32>(D); });
+        mk(tabSt[2], [](const DevPatch& D) { return dev::stageWork<33>(D); });
+        mk(tabLd[0], [](const DevPatch& D) { return dev::loadWork<31>(D); });
+        mk(tabLd[1], [](const DevPatch& D) { return dev::loadWork<32>(D); });
+        mk(tabLd[2], [](const DevPatch& D) { return dev::loadWork<33>(D); });
+    } else {
+        mk(tabSt[0], [](const DevPatch& D) { return dev::stageWork<21>(D); });
+        mk(tabSt[1], [](const DevPatch& D) { return dev::stageWork<22>(D); });
+        mk(tabLd[0], [](const DevPatch& D) { return dev::loadWork<21>(D); });
+        mk(tabLd[1], [](const DevPatch& D) { return dev::loadWork<22>(D); });
+    }
+}
+
+void Context::refresh() {
+    if (!hasProblem) throw StateError("refresh() before set_problem()");
+    if (device >= 0) freeAssembly();
+    buildDofMap(pd, map);
+    buildLayout(pd, L);
+    buildPattern(pd, map, L, pat, 0);
+    if (device < 0) {  // host-only context: the plan, no device buffers
+        refreshed = true;
+        return;
+    }
+    // diagonal slot of every row (Jacobi)
+    diag.assign(pat.n, -1);
+    for (int r = 0; r < pat.n; ++r) {
+        const int* b = pat.col.data() + pat.ptr[r];
+        const int* e = pat.col.data() + pat.ptr[r + 1];
+        const int* f = std::lower_bound(b, e, r);
+        if (f == e || *f != r) throw std::runtime_error("pattern has no diagonal entry");
+        diag[r] = pat.ptr[r] + int(f - b);
+    }
+    upload(arena, dPatches, L.dev, stream);
+    std::vector<FieldParams> fp(1, pd.fields);
+    upload(arena, dFields, fp, stream);
+    upload(arena, dKnots, L.knots, stream);
+    upload(arena, dGknots, L.gknots, stream);
+    upload(arena, dTabJobs, L.tabjobs, stream);
+    upload(arena, dGtabJobs, L.gtabjobs, stream);
+    upload(arena, dPfJobs, L.pfjobs, stream);
+    upload(arena, dIbuf, L.ibuf, stream);
+    upload(arena, dWq, L.wq, stream);
+    allocN(arena, dTab, L.ntab);
+    allocN(arena, dGtab, L.ngtab);
+    allocN(arena, dPf, L.npf);
+    allocN(arena, dCoefRaw, L.coefs);
+    allocN(arena, dCoefs, L.coefs);
+    allocN(arena, dFieldC, L.fields);
+    allocN(arena, dFieldL, L.lfield);
+    allocN(arena, dY1, L.y1);
+    allocN(arena, dY2, std::max(1LL, L.y2));
+    allocN(arena, dS, L.s);
+    allocN(arena, dU, std::max(1LL, L.u));
+    allocN(arena, dBand, L.band);
+    allocN(arena, dLv1, L.lv1);
+    allocN(arena, dLv2, std::max(1LL, L.lv2));
+    allocN(arena, dLvec, L.lvec);
+    upload(arena, dPtr, pat.ptr, stream);
+    upload(arena, dCol, pat.col, stream);
+    upload(arena, dSrc, pat.src, stream);
+    upload(arena, dOvfPtr, pat.ovf_ptr.empty() ? std::vector<uint32_t>(1, 0) : pat.ovf_ptr, stream);
+    upload(arena, dOvfIdx, pat.ovf_idx.empty() ? std::vector<uint32_t>(1, 0) : pat.ovf_idx, stream);
+    upload(arena, dLptr, pat.lptr, stream);
+    upload(arena, dLidx, pat.lidx, stream);
+    upload(arena, dFptr, pat.fptr, stream);
+    upload(arena, dFband, pat.fband.empty() ? std::vector<uint32_t>(1, 0) : pat.fband, stream);
+    upload(arena, dFbidx, pat.fbidx.empty() ? std::vector<uint32_t>(1, 0) : pat.fbidx, stream);
+    upload(arena, dDiag, diag, stream);
+    allocN(arena, dVal, (long long)pat.col.size());
+    allocN(arena, dRhs, pat.n);
+    allocN(arena, dDdof, std::max(1, map.boundarySize));
+    allocN(arena, dDetKey, 1);
+    buildTables();
+    // the control points of the problem
+    std::vector<double> raw;
+    for (const HostPatch& P : pd.patches) raw.insert(raw.end(), P.coefs.begin(), P.coefs.end());
+    GSGPU_CUDA_TRY(cudaMemcpyAsync(dCoefRaw, raw.data(), raw.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
+    launch::coefsToSoa(dPatches, tabCoef.d, (long long)tabCoef.h.size(), dCoefRaw, dCoefs, stream);
+    GSGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+    refreshed = true;
+    assembled = false;
+    solved = false;
+}
+
+void Context::setCoefs(const double* coefs) {
+    if (!refreshed) throw StateError("set_coefs() before refresh()");
+    if (device < 0) throw StateError("set_coefs() needs a CUDA device (host-only context)");
+    // keep the host copy (Dirichlet values are computed on the host)
+    const double* c = coefs;
+    for (HostPatch& P : pd.patches) {
+        std::copy(c, c + P.coefs.size(), P.coefs.begin());
+        c += P.coefs.size();
+    }
+    GSGPU_CUDA_TRY(cudaMemcpyAsync(dCoefRaw, coefs, size_t(L.coefs) * sizeof(double), cudaMemcpyHostToDevice, stream));
+    launch::coefsToSoa(dPatches, tabCoef.d, (long long)tabCoef.h.size(), dCoefRaw, dCoefs, stream);
+    assembled = false;
+}
+
+void Context::assemble(int precision) {
+    if (!refreshed) throw StateError("assemble() before refresh()");
+    if (device < 0) throw StateError("assemble() needs a CUDA device (host-only context)");
+    cudaStream_t s = stream;
+    for (int i = 0; i < 8; ++i)
+        if (!ev[i]) GSGPU_CUDA_TRY(cudaEventCreate(&ev[i]));
+    GSGPU_CUDA_TRY(cudaEventRecord(ev[0], s));
+    // Dirichlet values (host, gsAssembler::computeDirichletDofsIntpl) -> device
+    auto t0 = std::chrono::steady_clock::now();
+    dirichletValues(pd, map, ddof);
+    hostDirichletMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (!ddof.empty())
+        GSGPU_CUDA_TRY(cudaMemcpyAsync(dDdof, ddof.data(), ddof.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    GSGPU_CUDA_TRY(cudaEventRecord(ev[1], s));
+    // K1: basis tables and pair factors
+    launch::basisTables(dTabJobs, (long long)L.tabjobs.size(), dKnots, dTab, s);
+    launch::basisTables(dGtabJobs, (long long)L.gtabjobs.size(), dGknots, dGtab, s);
+    launch::pairFactors<double>(dPfJobs, tabPf.d, (long long)tabPf.h.size(), dTab, dPf, s);
+    GSGPU_CUDA_TRY(cudaEventRecord(ev[2], s));
+    // K2: geometry map, Jacobians, coefficient and load fields
+    const unsigned long long init = launch::detKeyInit();
+    GSGPU_CUDA_TRY(cudaMemcpyAsync(dDetKey, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+    launch::geoStage1(dPatches, tabGeo1.d, (long long)tabGeo1.h.size(), dCoefs, dGtab, dIbuf, dY1, s);
+    if (pd.dim == 3) launch::geoStage2(dPatches, tabGeo2.d, (long long)tabGeo2.h.size(), dY1, dGtab, dIbuf, dY2, s);
+    launch::pointStep(dPatches, tabPoint.d, (long long)tabPoint.h.size(), dFields, dY1, dY2, dGtab, dIbuf, dWq,
+                      dFieldC, dFieldL, dDetKey, s);
+    GSGPU_CUDA_TRY(cudaEventRecord(ev[3], s));
+    // K3: sum-factorised stiffness contraction into the band
+    if (pd.dim == 3) {
+        launch::contract<double, 31>(dPatches, tabSt[0].d, (long long)tabSt[0].h.size(), dFieldC, dS, dIbuf, dPf, s);
+        launch::contract<double, 32>(dPatches, tabSt[1].d, (long long)tabSt[1].h.size(), dS, dU, dIbuf, dPf, s);
+        launch::contract<double, 33>(dPatches, tabSt[2].d, (long long)tabSt[2].h.size(), dU, dBand, dIbuf, dPf, s);
+    } else {
+        launch::contract<double, 21>(dPatches, tabSt[0].d, (long long)tabSt[0].h.size(), dFieldC, dS, dIbuf, dPf, s);
+        launch::contract<double, 22>(dPatches, tabSt[1].d, (long long)tabSt[1].h.size(), dS, dBand, dIbuf, dPf, s);
+    }
+    GSGPU_CUDA_TRY(cudaEventRecord(ev[4], s));
+    // load vector
+    if (pd.dim == 3) {
+        launch::loadContract<31>(dPatches, tabLd[0].d, (long long)tabLd[0].h.size(), dFieldL, dLv1, dTab, dIbuf, s);
+        launch::loadContract<32>(dPatches, tabLd[1].d, (long long)tabLd[1].h.size(), dLv1, dLv2, dTab, dIbuf, s);
+        launch::loadContract<33>(dPatches, tabLd[2].d, (long long)tabLd[2].h.size(), dLv2, dLvec, dTab, dIbuf, s);
+    } else {
+        launch::loadContract<21>(dPatches, tabLd[0].d, (long long)tabLd[0].h.size(), dFieldL, dLv1, dTab, dIbuf, s);
+        launch::loadContract<22>(dPatches, tabLd[1].d, (long long)tabLd[1].h.size(), dLv1, dLvec, dTab, dIbuf, s);
+    }
+    GSGPU_CUDA_TRY(cudaEventRecord(ev[5], s));
+    // K4: CSR values (segmented gather) and rhs with the Dirichlet lift
+    launch::gatherCsr<double>((long long)pat.col.size(), dSrc, dBand, dOvfPtr, dOvfIdx, dVal, s);
+    launch::rhsRows(pat.n, dLvec, dLptr, dLidx, dBand, dFptr, dFband, dFbidx, dDdof, dRhs, s);
+    GSGPU_CUDA_TRY(cudaEventRecord(ev[6], s));
+    GSGPU_CUDA_TRY(cudaGetLastError());
+    GSGPU_CUDA_TRY(cudaEventSynchronize(ev[6]));
+    unsigned long long key = 0;
+    GSGPU_CUDA_TRY(cudaMemcpyAsync(&key, dDetKey, sizeof(key), cudaMemcpyDeviceToHost, s));
+    GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    detMin = launch::detKeyDecode(key);
+    assembled = true;
+    solved = false;
+    assembledPrecision = precision;
+    if (!(detMin > 0.0)) throw JacobianError("geometry map has det J <= 0 at a quadrature point");
+}
+
+void Context::times(double* ms) {
+    float t[6];
+    for (int i = 0; i < 6; ++i) GSGPU_CUDA_TRY(cudaEventElapsedTime(&t[i], ev[i], ev[i + 1]));
+    ms[0] = hostDirichletMs;
+    for (int i = 1; i < 6; ++i) ms[i] = t[i];
+    float tot;
+    GSGPU_CUDA_TRY(cudaEventElapsedTime(&tot, ev[0], ev[6]));
+    ms[6] = tot;
+}
+
+void Context::freeAssembly() {
+    arena.releaseAll();
+    *this = Context::reset(std::move(*this));
+}
+
+Context Context::reset(Context&& c) {
+    Context n;
+    n.device = c.device;
+    n.stream = c.stream;
+    for (int i = 0; i < 8; ++i) n.ev[i] = c.ev[i];
+    n.pd = std::move(c.pd);
+    n.hasProblem = c.hasProblem;
+    n.arena.budget = c.arena.budget;
+    c.stream = nullptr;
+    for (int i = 0; i < 8; ++i) c.ev[i] = nullptr;
+    return n;
+}
+
+// ---------------------------------------------------------------------------------------------
+void Context::ensureSolveBuffers() {
+    const int n = pat.n;
+    if (solveN == n && dX) return;
+    for (double** b : {&dX, &dR, &dZ, &dP, &dT, &dDinv, &dPart0, &dPart1, &dPart2}) arena.release(*b), *b = nullptr;
+    arena.release(dCg);
+    dCg = nullptr;
+    allocN(arena, dX, n);
+    allocN(arena, dR, n);
+    allocN(arena, dZ, n);
+    allocN(arena, dP, n);
+    allocN(arena, dT, n);
+    allocN(arena, dDinv, n);
+    allocN(arena, dPart0, launch::cgPartials(n));
+    allocN(arena, dPart1, launch::cgPartials(n));
+    // SpMV partials: one per SpMV block; the most blocks are launched with 32 lanes per row
+    allocN(arena, dPart2, std::max(launch::cgPartials(n), launch::spmvPartials(n, 32)));
+    dCg = static_cast<CgState*>(arena.alloc(sizeof(CgState)));
+    solveN = n;
+}
+
+int Context::lanesPerRow() const {
+    const double avg = pat.n ? double(pat.col.size()) / pat.n : 1.0;
+    if (avg > 48) return 32;
+    if (avg > 20) return 16;
+    if (avg > 10) return 8;
+    return 4;
+}
+
+void Context::solve(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
+    if (!assembled) throw StateError("solve() before assemble()");
+    if (o.method != GSGPU_SOLVER_CG_JACOBI) throw std::invalid_argument("solver method not available in this build");
+    if (o.precision != GSGPU_PREC_FP64) throw std::invalid_argument("precision mode not available in this build");
+    ensureSolveBuffers();
+    cudaStream_t s = stream;
+    cudaEvent_t e0, e1;
+    GSGPU_CUDA_TRY(cudaEventCreate(&e0));
+    GSGPU_CUDA_TRY(cudaEventCreate(&e1));
+    GSGPU_CUDA_TRY(cudaEventRecord(e0, s));
+    launch::jacobiDiag(pat.n, dDiag, dVal, 1.0, dDinv, s);
+    CgBuffers B;
+    B.n = pat.n;
+    B.lanes_per_row = lanesPerRow();
+    B.ptr = dPtr;
+    B.col = dCol;
+    B.val = dVal;
+    B.b = dRhs;
+    B.dinv = dDinv;
+    B.x = dX; B.r = dR; B.z = dZ; B.p = dP; B.t = dT;
+    B.part0 = dPart0; B.part1 = dPart1; B.part2 = dPart2;
+    B.st = dCg;
+    const double tol = o.tol > 0 ? o.tol : 1e-10;
+    const int maxit = o.max_iters > 0 ? o.max_iters : 1000;
+    launch::cgInit(B, tol, maxit, s);
+    CgState hs{};
+    spmvBytes = double(pat.col.size()) * (8 + 4) + double(pat.n + 1) * 4 + 2.0 * pat.n * 8;
+    if (profiling) {
+        // one iteration at a time, every SpMV bracketed by events (no graph)
+        cudaEvent_t a, b;
+        GSGPU_CUDA_TRY(cudaEventCreate(&a));
+        GSGPU_CUDA_TRY(cudaEventCreate(&b));
+        GSGPU_CUDA_TRY(cudaMemcpyAsync(&hs, dCg, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+        GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
+        for (int it = 0; it < maxit && !hs.done; ++it) {
+            GSGPU_CUDA_TRY(cudaEventRecord(a, s));
+            launch::cgSpmv(B, s);
+            GSGPU_CUDA_TRY(cudaEventRecord(b, s));
+            launch::cgRest(B, s);
+            GSGPU_CUDA_TRY(cudaMemcpyAsync(&hs, dCg, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+            GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
+            float m = 0;
+            GSGPU_CUDA_TRY(cudaEventElapsedTime(&m, a, b));
+            spmvMs += m;
+            ++spmvLaunches;
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    } else {
+        // iterations in chunks captured as a CUDA graph; kernels become no-ops once converged
+        const int chunk = 16;
+        cudaGraphExec_t exec = nullptr;
+        {
+            cudaGraph_t g;
+            GSGPU_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            for (int k = 0; k < chunk; ++k) launch::cgIteration(B, s);
+            GSGPU_CUDA_TRY(cudaStreamEndCapture(s, &g));
+            GSGPU_CUDA_TRY(cudaGraphInstantiate(&exec, g, 0));
+            cudaGraphDestroy(g);
+        }
+        for (int done_it = 0; done_it < maxit + chunk; done_it += chunk) {
+            GSGPU_CUDA_TRY(cudaGraphLaunch(exec, s));
+            GSGPU_CUDA_TRY(cudaMemcpyAsync(&hs, dCg, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+            GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
+            if (hs.done) break;
+        }
+        cudaGraphExecDestroy(exec);
+    }
+    GSGPU_CUDA_TRY(cudaEventRecord(e1, s));
+    GSGPU_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    info.iterations = hs.iters;
+    info.relres = hs.relres;
+    info.refinements = 0;
+    info.t_solve_ms = ms;
+    solved = true;
+    lastConverged = hs.done == 1;
+}
+
+}  // namespace gsgpu
+
+// ---------------------------------------------------------------------------------------------
+// C ABI
+
+struct gsgpu_context {
+    gsgpu::Context c;
+    std::string err;
+};
+
+namespace {
+template <class F>
+int guarded(gsgpu_context* ctx, F&& f) {
+    if (!ctx) return GSGPU_ERR_INVALID;
+    try {
+        if (ctx->c.device >= 0) GSGPU_CUDA_TRY(cudaSetDevice(ctx->c.device));
+        f();
+        ctx->err.clear();
+        return GSGPU_OK;
+    } catch (const gsgpu::CudaError& e) {
+        ctx->err = e.what();
+        return GSGPU_ERR_CUDA;
+    } catch (const gsgpu::BudgetError& e) {
+        ctx->err = e.what();
+        return GSGPU_ERR_BUDGET;
+    } catch (const gsgpu::StateError& e) {
+        ctx->err = e.what();
+        return GSGPU_ERR_STATE;
+    } catch (const gsgpu::JacobianError& e) {
+        ctx->err = e.what();
+        return GSGPU_ERR_JACOBIAN;
+    } catch (const std::invalid_argument& e) {
+        ctx->err = e.what();
+        return GSGPU_ERR_INVALID;
+    } catch (const std::exception& e) {
+        ctx->err = e.what();
+        return GSGPU_ERR_INVALID;
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int gsgpu_create(gsgpu_context** out, int device) {
+    if (!out) return GSGPU_ERR_INVALID;
+    *out = nullptr;
+    if (device == -1) {  // host-only context: dof map and sparsity pattern, no device work
+        gsgpu_context* c = new gsgpu_context();
+        c->c.device = -1;
+        *out = c;
+        return GSGPU_OK;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return GSGPU_ERR_CUDA;
+    if (cudaSetDevice(device) != cudaSuccess) return GSGPU_ERR_CUDA;
+    gsgpu_context* c = new gsgpu_context();
+    c->c.device = device;
+    if (cudaStreamCreateWithFlags(&c->c.stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return GSGPU_ERR_CUDA;
+    }
+    *out = c;
+    return GSGPU_OK;
+}
+
+int gsgpu_destroy(gsgpu_context* ctx) {
+    if (!ctx) return GSGPU_ERR_INVALID;
+    if (ctx->c.device < 0) {
+        delete ctx;
+        return GSGPU_OK;
+    }
+    cudaSetDevice(ctx->c.device);
+    if (ctx->c.stream) cudaStreamSynchronize(ctx->c.stream);
+    ctx->c.arena.releaseAll();
+    for (int i = 0; i < 8; ++i)
+        if (ctx->c.ev[i]) cudaEventDestroy(ctx->c.ev[i]);
+    if (ctx->c.stream) cudaStreamDestroy(ctx->c.stream);
+    delete ctx;
+    return GSGPU_OK;
+}
+
+const char* gsgpu_last_error(const gsgpu_context* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int gsgpu_set_problem(gsgpu_context* ctx, const gsgpu_problem* prob) {
+    return guarded(ctx, [&] {
+        gsgpu::ProblemDesc pd;
+        gsgpu::problemFromC(prob, pd);
+        if (ctx->c.device >= 0) ctx->c.arena.releaseAll();
+        ctx->c = gsgpu::Context::reset(std::move(ctx->c));
+        ctx->c.pd = std::move(pd);
+        ctx->c.hasProblem = true;
+    });
+}
+
+int gsgpu_refresh(gsgpu_context* ctx) { return guarded(ctx, [&] { ctx->c.refresh(); }); }
+
+int gsgpu_set_coefs(gsgpu_context* ctx, const double* coefs) {
+    return guarded(ctx, [&] {
+        if (!coefs) throw std::invalid_argument("null coefs");
+        ctx->c.setCoefs(coefs);
+    });
+}
+
+int gsgpu_assemble(gsgpu_context* ctx, int precision) {
+    return guarded(ctx, [&] { ctx->c.assemble(precision); });
+}
+
+int gsgpu_sizes(gsgpu_context* ctx, int* nfree, long long* nnz, int* nfixed, int* nlocal) {
+    return guarded(ctx, [&] {
+        if (!ctx->c.refreshed) throw gsgpu::StateError("sizes() before refresh()");
+        if (nfree) *nfree = ctx->c.pat.n;
+        if (nnz) *nnz = (long long)ctx->c.pat.col.size();
+        if (nfixed) *nfixed = ctx->c.map.boundarySize;
+        if (nlocal) *nlocal = ctx->c.map.nlocal;
+    });
+}
+
+int gsgpu_matrix_csr(gsgpu_context* ctx, int* ptr, int* col, double* val) {
+    return guarded(ctx, [&] {
+        auto& c = ctx->c;
+        if (!c.refreshed) throw gsgpu::StateError("matrix() before refresh()");
+        if (val && !c.assembled) throw gsgpu::StateError("matrix() values before assemble()");
+        if (ptr) std::copy(c.pat.ptr.begin(), c.pat.ptr.end(), ptr);
+        if (col) std::copy(c.pat.col.begin(), c.pat.col.end(), col);
+        if (val) {
+            GSGPU_CUDA_TRY(cudaMemcpyAsync(val, c.dVal, c.pat.col.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            GSGPU_CUDA_TRY(cudaStreamSynchronize(c.stream));
+        }
+    });
+}
+
+int gsgpu_rhs(gsgpu_context* ctx, double* rhs) {
+    return guarded(ctx, [&] {
+        auto& c = ctx->c;
+        if (!c.assembled) throw gsgpu::StateError("rhs() before assemble()");
+        GSGPU_CUDA_TRY(cudaMemcpyAsync(rhs, c.dRhs, size_t(c.pat.n) * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        GSGPU_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int gsgpu_fixed_dofs(gsgpu_context* ctx, double* ddof) {
+    return guarded(ctx, [&] {
+        auto& c = ctx->c;
+        if (!c.assembled) throw gsgpu::StateError("fixedDofs() before assemble()");
+        std::copy(c.ddof.begin(), c.ddof.end(), ddof);
+    });
+}
+
+int gsgpu_dof_map(gsgpu_context* ctx, int* index) {
+    return guarded(ctx, [&] {
+        auto& c = ctx->c;
+        if (!c.refreshed) throw gsgpu::StateError("dof map before refresh()");
+        std::copy(c.map.index.begin(), c.map.index.end(), index);
+    });
+}
+
+int gsgpu_solve(gsgpu_context* ctx, const gsgpu_solver_opts* opts, double* x, gsgpu_solve_info* info) {
+    if (!opts) return GSGPU_ERR_INVALID;
+    gsgpu_solve_info tmp{};
+    const int rc = guarded(ctx, [&] {
+        ctx->c.solve(*opts, tmp);
+        if (x) {  // on the context's stream, so that caller-side events on it bracket the copy
+            GSGPU_CUDA_TRY(cudaMemcpyAsync(x, ctx->c.dX, size_t(ctx->c.pat.n) * sizeof(double), cudaMemcpyDeviceToHost,
+                                           ctx->c.stream));
+            GSGPU_CUDA_TRY(cudaStreamSynchronize(ctx->c.stream));
+        }
+    });
+    if (info) *info = tmp;
+    if (rc == GSGPU_OK && !ctx->c.lastConverged) {
+        ctx->err = "maximum number of iterations reached";
+        return GSGPU_ERR_NOT_CONVERGED;
+    }
+    return rc;
+}
+
+int gsgpu_l2_error(gsgpu_context* ctx, double* err) {
+    return guarded(ctx, [&] {
+        (void)err;
+        throw std::invalid_argument("l2_error is not available in this build");
+    });
+}
+
+int gsgpu_stream(gsgpu_context* ctx, void** stream) {
+    return guarded(ctx, [&] { *stream = (void*)ctx->c.stream; });
+}
+
+int gsgpu_set_profiling(gsgpu_context* ctx, int on) {
+    return guarded(ctx, [&] {
+        ctx->c.profiling = on != 0;
+        ctx->c.spmvLaunches = 0;
+        ctx->c.spmvMs = 0.0;
+    });
+}
+
+int gsgpu_spmv_stats(gsgpu_context* ctx, long long* launches, double* total_ms, double* bytes_per_launch) {
+    return guarded(ctx, [&] {
+        if (launches) *launches = ctx->c.spmvLaunches;
+        if (total_ms) *total_ms = ctx->c.spmvMs;
+        if (bytes_per_launch) *bytes_per_launch = ctx->c.spmvBytes;
+    });
+}
+
+int gsgpu_min_jacobian(gsgpu_context* ctx, double* detmin) {
+    return guarded(ctx, [&] {
+        if (!ctx->c.assembled) throw gsgpu::StateError("min_jacobian() before assemble()");
+        *detmin = ctx->c.detMin;
+    });
+}
+
+int gsgpu_assemble_times(gsgpu_context* ctx, double* ms7) {
+    return guarded(ctx, [&] {
+        if (!ctx->c.assembled) throw gsgpu::StateError("assemble_times() before assemble()");
+        ctx->c.times(ms7);
+    });
+}
+
+}  // extern "C"

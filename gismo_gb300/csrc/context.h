@@ -1,0 +1,106 @@
+// The state behind one gsgpu_context: host plan, device buffers, streams and events.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/gsgpu.h"
+#include "gsgpu_internal.h"
+#include "kernels_solve.h"
+#include "plan.h"
+
+namespace gsgpu {
+
+struct CudaError : std::runtime_error {
+    cudaError_t code;
+    CudaError(cudaError_t e, const char* expr, const char* file, int line);
+};
+struct BudgetError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+struct StateError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+struct JacobianError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+// every device allocation of a context goes through here (accounting against a budget)
+struct DeviceArena {
+    size_t used = 0;
+    size_t budget = 0;  // 0 = unlimited
+    std::vector<std::pair<void*, size_t>> sizes;
+    void* alloc(size_t bytes);
+    void release(void* p);
+    void releaseAll();
+};
+
+struct Tab {
+    std::vector<BlkEnt> h;
+    BlkEnt* d = nullptr;
+};
+
+namespace launch {
+void coefsToSoa(const DevPatch* P, const BlkEnt* tab, long long nblk, const double* raw, double* soa, cudaStream_t s);
+}
+
+struct Context {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[8] = {};
+    DeviceArena arena;
+
+    ProblemDesc pd;
+    bool hasProblem = false, refreshed = false, assembled = false, solved = false, lastConverged = false;
+    int assembledPrecision = 0;
+    DofMap map;
+    Layout L;
+    Pattern pat;
+    std::vector<int> diag;
+    std::vector<double> ddof;
+    double detMin = 0.0, hostDirichletMs = 0.0;
+
+    // device buffers (assembly)
+    DevPatch* dPatches = nullptr;
+    FieldParams* dFields = nullptr;
+    double *dKnots = nullptr, *dGknots = nullptr, *dTab = nullptr, *dGtab = nullptr, *dPf = nullptr, *dWq = nullptr;
+    TabJob *dTabJobs = nullptr, *dGtabJobs = nullptr;
+    PfJob* dPfJobs = nullptr;
+    int* dIbuf = nullptr;
+    double *dCoefRaw = nullptr, *dCoefs = nullptr, *dFieldC = nullptr, *dFieldL = nullptr, *dY1 = nullptr,
+           *dY2 = nullptr, *dS = nullptr, *dU = nullptr, *dBand = nullptr, *dLv1 = nullptr, *dLv2 = nullptr,
+           *dLvec = nullptr;
+    int *dPtr = nullptr, *dCol = nullptr, *dDiag = nullptr;
+    uint32_t *dSrc = nullptr, *dOvfPtr = nullptr, *dOvfIdx = nullptr, *dLptr = nullptr, *dLidx = nullptr,
+             *dFptr = nullptr, *dFband = nullptr, *dFbidx = nullptr;
+    double *dVal = nullptr, *dRhs = nullptr, *dDdof = nullptr;
+    unsigned long long* dDetKey = nullptr;
+    Tab tabPf, tabCoef, tabGeo1, tabGeo2, tabPoint, tabSt[3], tabLd[3];
+
+    // device buffers (solve)
+    int solveN = -1;
+    double *dX = nullptr, *dR = nullptr, *dZ = nullptr, *dP = nullptr, *dT = nullptr, *dDinv = nullptr;
+    double *dPart0 = nullptr, *dPart1 = nullptr, *dPart2 = nullptr;
+    CgState* dCg = nullptr;
+    // profiling of the solver's SpMV launches
+    bool profiling = false;
+    long long spmvLaunches = 0;
+    double spmvMs = 0.0, spmvBytes = 0.0;
+
+    void refresh();
+    void setCoefs(const double* coefs);
+    void assemble(int precision);
+    void solve(const gsgpu_solver_opts& o, gsgpu_solve_info& info);
+    void times(double* ms);
+    void freeAssembly();
+    void buildTables();
+    void ensureSolveBuffers();
+    int lanesPerRow() const;
+    static Context reset(Context&& c);
+};
+
+}  // namespace gsgpu

@@ -1,0 +1,500 @@
+// Per-work-item bodies of the assembly kernels. Each function computes one output element from
+// the packed patch data; the __global__ wrappers in kernels_assemble.cu map threads to items.
+#pragma once
+
+#include <cmath>
+
+#include "gsgpu_internal.h"
+
+#ifdef __CUDACC__
+#define GS_HD __host__ __device__ __forceinline__
+#define GS_LDG(p) __ldg(p)
+#else
+#define GS_HD inline
+#define GS_LDG(p) (*(p))
+#endif
+
+namespace gsgpu {
+namespace dev {
+
+constexpr int kMaxKappaWave = 8;  // largest |k_m,i| of a Fourier mode supported on the device
+
+// -------------------------------------------------------------------------------------------
+// K1: values and first derivatives of the p+1 B-splines of span s at u (Cox-de Boor triangle;
+// derivatives from the degree p-1 values). out[0..p] values, out[p+1..2p+1] derivatives.
+GS_HD void basis1d(const double* __restrict__ t, int p, int s, double u, double* __restrict__ out) {
+    double N[16], Nm1[16];
+    N[0] = 1.0;
+    if (p == 0) { out[0] = 1.0; out[1] = 0.0; return; }
+    for (int k = 1; k <= p; ++k) {
+        if (k == p)
+            for (int r = 0; r < p; ++r) Nm1[r] = N[r];
+        double saved = 0.0;
+        for (int r = 0; r < k; ++r) {
+            const double tr = t[s + 1 + r], tl = t[s + 1 + r - k];
+            const double tmp = N[r] / (tr - tl);
+            N[r] = saved + (tr - u) * tmp;
+            saved = (u - tl) * tmp;
+        }
+        N[k] = saved;
+    }
+    const int a = s - p;
+    for (int r = 0; r <= p; ++r) {
+        out[r] = N[r];
+        double d = 0.0;
+        if (r >= 1) d += p * Nm1[r - 1] / (t[a + r + p] - t[a + r]);
+        if (r <= p - 1) d -= p * Nm1[r] / (t[a + r + p + 1] - t[a + r + 1]);
+        out[p + 1 + r] = d;
+    }
+}
+
+// pair factor PF[tau][e][r][s][t] = B^(alpha)_s(g) B^(beta)_t(g), tau = 2 alpha + beta,
+// g = e*q + r; tab holds [V_0..V_p, D_0..D_p] per abscissa
+template <typename T>
+GS_HD T pairFactor(const double* __restrict__ tab, int p, int q, int E, long long item) {
+    const int P1 = p + 1;
+    const int t = int(item % P1);
+    long long r0 = item / P1;
+    const int s = int(r0 % P1);
+    r0 /= P1;
+    const int r = int(r0 % q);
+    r0 /= q;
+    const int e = int(r0 % E);
+    const int tau = int(r0 / E);
+    const double* row = tab + (long long)(e * q + r) * 2 * P1;
+    const double a = (tau & 2) ? row[P1 + s] : row[s];
+    const double b = (tau & 1) ? row[P1 + t] : row[t];
+    return T(a * b);
+}
+
+// -------------------------------------------------------------------------------------------
+// geometry map, sum-factorised over the control net: stage 1 (direction 0)
+// 3D: Y1[m][tau][i2][i1][g0] ; 2D: Y1[m][tau][i1][g0]  (tau: 0 value, 1 derivative)
+GS_HD double geoStage1(const DevPatch& D, long long item, const double* __restrict__ coefs,
+                       const double* __restrict__ gtab, const int* __restrict__ ibuf) {
+    const int Q0 = D.Q[0];
+    const int g0 = int(item % Q0);
+    long long r = item / Q0;
+    long long rest;  // (i2*gn1 + i1) or i1
+    int tau, m;
+    if (D.dim == 3) {
+        const long long plane = (long long)D.gn[2] * D.gn[1];
+        rest = r % plane;
+        r /= plane;
+    } else {
+        rest = r % D.gn[1];
+        r /= D.gn[1];
+    }
+    tau = int(r % 2);
+    m = int(r / 2);
+    const int gp = D.gp[0];
+    const int f0 = ibuf[D.gqoff[0] + g0];
+    const double* tb = gtab + D.gtoff[0] + (long long)g0 * 2 * (gp + 1) + tau * (gp + 1);
+    const double* c = coefs + D.coef_off + m * D.ngeo + rest * D.gn[0] + f0;
+    double acc = 0.0;
+    for (int s = 0; s <= gp; ++s) acc += tb[s] * c[s];
+    return acc;
+}
+
+// 3D stage 2 (direction 1): Y2[m][tau][i2][g1][g0], tau: 0 vv, 1 dv (d/dxi0), 2 vd (d/dxi1)
+GS_HD double geoStage2(const DevPatch& D, long long item, const double* __restrict__ Y1,
+                       const double* __restrict__ gtab, const int* __restrict__ ibuf) {
+    const int Q0 = D.Q[0], Q1 = D.Q[1];
+    const int g0 = int(item % Q0);
+    long long r = item / Q0;
+    const int g1 = int(r % Q1);
+    r /= Q1;
+    const int i2 = int(r % D.gn[2]);
+    r /= D.gn[2];
+    const int tau = int(r % 3);
+    const int m = int(r / 3);
+    const int t1 = (tau == 1) ? 1 : 0;  // derivative in direction 0 (from stage 1)
+    const int t2 = (tau == 2) ? 1 : 0;  // derivative in direction 1
+    const int gp = D.gp[1];
+    const int f1 = ibuf[D.gqoff[1] + g1];
+    const double* tb = gtab + D.gtoff[1] + (long long)g1 * 2 * (gp + 1) + t2 * (gp + 1);
+    const double* y = Y1 + D.y1_off + ((((long long)m * 2 + t1) * D.gn[2] + i2) * D.gn[1] + f1) * Q0 + g0;
+    double acc = 0.0;
+    for (int s = 0; s <= gp; ++s) acc += tb[s] * y[(long long)s * Q0];
+    return acc;
+}
+
+// closed-form fields at a physical point: kappa and f = -div(kappa grad u)
+// (g = scale sum_m amp_m cos(pi k_m.x + phase_m), kappa = exp(alpha g), u = prod sin(freq pi x_i)).
+// cos/sin of the mode phases use e^{i theta} = e^{i phase} prod_i (e^{i pi x_i})^{k_i}.
+struct Complex {
+    double re, im;
+};
+GS_HD Complex cmul(Complex a, Complex b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+
+GS_HD void sincospiD(double x, double* s, double* c) {
+#ifdef __CUDA_ARCH__
+    sincospi(x, s, c);
+#else
+    *s = std::sin(M_PI * x);
+    *c = std::cos(M_PI * x);
+#endif
+}
+
+GS_HD void fields(const FieldParams& F, const double* x, double& kappa, double& f) {
+    const int d = F.dim;
+    const double w = F.ufreq * M_PI;
+    double sn[3], cs[3];
+    for (int i = 0; i < d; ++i) sincospiD(F.ufreq * x[i], &sn[i], &cs[i]);
+    double u = 1.0;
+    for (int i = 0; i < d; ++i) u *= sn[i];
+    double gu[3];
+    for (int j = 0; j < d; ++j) {
+        double t = w * cs[j];
+        for (int i = 0; i < d; ++i)
+            if (i != j) t *= sn[i];
+        gu[j] = t;
+    }
+    if (!F.fourier) {
+        kappa = F.kconst;
+        f = kappa * (d * w * w * u);
+        return;
+    }
+    Complex zp[3][kMaxKappaWave + 1];
+    for (int i = 0; i < d; ++i) {
+        double s, c;
+        sincospiD(x[i], &s, &c);
+        zp[i][0] = {1.0, 0.0};
+        const Complex z{c, s};
+        for (int k = 1; k <= F.kmax; ++k) zp[i][k] = cmul(zp[i][k - 1], z);
+    }
+    double g = 0.0, gg[3] = {0.0, 0.0, 0.0};
+    for (int m = 0; m < F.nmodes; ++m) {
+        Complex e{F.cph[m], F.sph[m]};
+        for (int i = 0; i < d; ++i) e = cmul(e, zp[i][F.kk[m][i]]);
+        g += F.amp[m] * e.re;
+        const double as = F.amp[m] * e.im * M_PI;
+        for (int i = 0; i < d; ++i) gg[i] -= as * F.kk[m][i];
+    }
+    g *= F.scale;
+    double dot = 0.0;
+    for (int i = 0; i < d; ++i) dot += gg[i] * gu[i];
+    dot *= F.scale;
+#ifdef __CUDA_ARCH__
+    kappa = exp(F.alpha * g);
+#else
+    kappa = std::exp(F.alpha * g);
+#endif
+    f = kappa * (d * w * w * u - F.alpha * dot);
+}
+
+// point-wise step: last geometry stage, metric and coefficient fields.
+// C^{ab} = w kappa |det J| (J^-1 J^-T)_{ab} = w kappa / |det J| sum_m cof_{ma} cof_{mb},
+// L = w |det J| f.  Component order 3D: 00 01 02 11 12 22 ; 2D: 00 01 11.
+// Returns det J.
+GS_HD double pointStep(const DevPatch& D, const FieldParams& F, long long item, const double* __restrict__ Y1,
+                       const double* __restrict__ Y2, const double* __restrict__ gtab, const int* __restrict__ ibuf,
+                       const double* __restrict__ wq, double* __restrict__ C, double* __restrict__ Lf) {
+    const int d = D.dim;
+    const int Q0 = D.Q[0], Q1 = D.Q[1];
+    const int g0 = int(item % Q0);
+    long long r = item / Q0;
+    const int g1 = int(r % Q1);
+    const int g2 = int(r / Q1);
+    double x[3], J[3][3];
+    if (d == 3) {
+        const int gp = D.gp[2];
+        const int f2 = ibuf[D.gqoff[2] + g2];
+        const double* tb = gtab + D.gtoff[2] + (long long)g2 * 2 * (gp + 1);
+        const long long plane = (long long)Q1 * Q0;
+        for (int m = 0; m < 3; ++m) {
+            const double* yvv = Y2 + D.y2_off + (((long long)m * 3 + 0) * D.gn[2] + f2) * plane + (long long)g1 * Q0 + g0;
+            const double* ydv = yvv + (long long)D.gn[2] * plane;
+            const double* yvd = ydv + (long long)D.gn[2] * plane;
+            double a = 0, b = 0, c = 0, e = 0;
+            for (int s = 0; s <= gp; ++s) {
+                const double v = tb[s], dv = tb[gp + 1 + s];
+                const long long o = (long long)s * plane;
+                a += v * yvv[o];
+                b += v * ydv[o];
+                c += v * yvd[o];
+                e += dv * yvv[o];
+            }
+            x[m] = a;
+            J[m][0] = b;
+            J[m][1] = c;
+            J[m][2] = e;
+        }
+    } else {
+        const int gp = D.gp[1];
+        const int f1 = ibuf[D.gqoff[1] + g1];
+        const double* tb = gtab + D.gtoff[1] + (long long)g1 * 2 * (gp + 1);
+        for (int m = 0; m < 2; ++m) {
+            const double* yv = Y1 + D.y1_off + (((long long)m * 2 + 0) * D.gn[1] + f1) * Q0 + g0;
+            const double* yd = yv + (long long)D.gn[1] * Q0;
+            double a = 0, b = 0, c = 0;
+            for (int s = 0; s <= gp; ++s) {
+                const double v = tb[s], dv = tb[gp + 1 + s];
+                const long long o = (long long)s * Q0;
+                a += v * yv[o];
+                b += v * yd[o];
+                c += dv * yv[o];
+            }
+            x[m] = a;
+            J[m][0] = b;
+            J[m][1] = c;
+        }
+    }
+    double w = wq[D.qoff[0] + g0] * wq[D.qoff[1] + g1];
+    if (d == 3) w *= wq[D.qoff[2] + g2];
+    double kappa, f;
+    fields(F, x, kappa, f);
+    const long long nq = D.nq;
+    double det;
+    if (d == 3) {
+        double cof[3][3];
+        cof[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        cof[0][1] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        cof[0][2] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        cof[1][0] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+        cof[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+        cof[1][2] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+        cof[2][0] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+        cof[2][1] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+        cof[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        det = J[0][0] * cof[0][0] + J[0][1] * cof[0][1] + J[0][2] * cof[0][2];
+        const double sc = w * kappa / fabs(det);
+        double* c = C + D.field_off + item;
+        int k = 0;
+        for (int a = 0; a < 3; ++a)
+            for (int b = a; b < 3; ++b, ++k)
+                c[k * nq] = sc * (cof[0][a] * cof[0][b] + cof[1][a] * cof[1][b] + cof[2][a] * cof[2][b]);
+    } else {
+        det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        // cof = [[J11, -J10], [-J01, J00]]
+        const double c00 = J[1][1], c01 = -J[1][0], c10 = -J[0][1], c11 = J[0][0];
+        const double sc = w * kappa / fabs(det);
+        double* c = C + D.field_off + item;
+        c[0] = sc * (c00 * c00 + c10 * c10);
+        c[nq] = sc * (c00 * c01 + c10 * c11);
+        c[2 * nq] = sc * (c01 * c01 + c11 * c11);
+    }
+    Lf[D.lfield_off + item] = w * fabs(det) * f;
+    return det;
+}
+
+// -------------------------------------------------------------------------------------------
+// sum-factorised stiffness contraction along one axis.
+//   out_h[o][i][oi][c] = sum_terms sum_{g in supp(i) & supp(j)} PF_tau(g; i, j) in_f[o][g][c],
+//   j = i + oi - p. The term lists below group the d^2 products C^{ab} d_a(phi_i) d_b(phi_j) by
+//   the derivative pattern of the remaining directions.
+struct Term {
+    int h, f, tau;
+};
+
+template <int KIND>
+struct Stage;
+// 3D stage 1 (axis 0): C(00,01,02,11,12,22) -> S0..S7
+template <>
+struct Stage<31> {
+    static constexpr int AX = 0, NIN = 6, NOUT = 8, NT = 8;
+    GS_HD static Term term(int k) {
+        const Term t[8] = {{0, 0, 3}, {1, 1, 2}, {2, 1, 1}, {3, 2, 2}, {4, 2, 1}, {5, 3, 0}, {6, 4, 0}, {7, 5, 0}};
+        return t[k];
+    }
+};
+// 3D stage 2 (axis 1): S -> U_vv, U_vd, U_dv, U_dd (grouped by the direction-2 factor)
+template <>
+struct Stage<32> {
+    static constexpr int AX = 1, NIN = 8, NOUT = 4, NT = 9;
+    GS_HD static Term term(int k) {
+        const Term t[9] = {{0, 0, 0}, {0, 1, 1}, {0, 2, 2}, {0, 5, 3}, {1, 3, 0},
+                           {1, 6, 2}, {2, 4, 0}, {2, 6, 1}, {3, 7, 0}};
+        return t[k];
+    }
+};
+// 3D stage 3 (axis 2): U -> band
+template <>
+struct Stage<33> {
+    static constexpr int AX = 2, NIN = 4, NOUT = 1, NT = 4;
+    GS_HD static Term term(int k) {
+        const Term t[4] = {{0, 0, 0}, {0, 1, 1}, {0, 2, 2}, {0, 3, 3}};
+        return t[k];
+    }
+};
+// 2D stage 1 (axis 0): C(00,01,11) -> S0..S3
+template <>
+struct Stage<21> {
+    static constexpr int AX = 0, NIN = 3, NOUT = 4, NT = 4;
+    GS_HD static Term term(int k) {
+        const Term t[4] = {{0, 0, 3}, {1, 1, 2}, {2, 1, 1}, {3, 2, 0}};
+        return t[k];
+    }
+};
+// 2D stage 2 (axis 1): S -> band
+template <>
+struct Stage<22> {
+    static constexpr int AX = 1, NIN = 4, NOUT = 1, NT = 4;
+    GS_HD static Term term(int k) {
+        const Term t[4] = {{0, 0, 0}, {0, 1, 1}, {0, 2, 2}, {0, 3, 3}};
+        return t[k];
+    }
+};
+
+// geometry of a stage for one patch: outer / inner extents, field strides and base offsets
+struct StageGeom {
+    long long outer, inner, in_fs, out_fs, in_base, out_base;
+};
+template <int KIND>
+GS_HD StageGeom stageGeom(const DevPatch& D) {
+    StageGeom g{};
+    const long long n0W = (long long)D.n[0] * D.W[0], n1W = (long long)D.n[1] * D.W[1];
+    if (KIND == 31) {
+        g.outer = (long long)D.Q[2] * D.Q[1]; g.inner = 1;
+        g.in_fs = D.nq; g.in_base = D.field_off;
+        g.out_fs = g.outer * n0W; g.out_base = D.s_off;
+    } else if (KIND == 32) {
+        g.outer = D.Q[2]; g.inner = n0W;
+        g.in_fs = (long long)D.Q[2] * D.Q[1] * n0W; g.in_base = D.s_off;
+        g.out_fs = (long long)D.Q[2] * n1W * n0W; g.out_base = D.u_off;
+    } else if (KIND == 33) {
+        g.outer = 1; g.inner = n1W * n0W;
+        g.in_fs = (long long)D.Q[2] * n1W * n0W; g.in_base = D.u_off;
+        g.out_fs = D.bandsize; g.out_base = D.band_off;
+    } else if (KIND == 21) {
+        g.outer = D.Q[1]; g.inner = 1;
+        g.in_fs = D.nq; g.in_base = D.field_off;
+        g.out_fs = (long long)D.Q[1] * n0W; g.out_base = D.s_off;
+    } else {  // 22
+        g.outer = 1; g.inner = n0W;
+        g.in_fs = (long long)D.Q[1] * n0W; g.in_base = D.s_off;
+        g.out_fs = D.bandsize; g.out_base = D.band_off;
+    }
+    return g;
+}
+
+template <int KIND>
+GS_HD long long stageWork(const DevPatch& D) {
+    const StageGeom g = stageGeom<KIND>(D);
+    const int ax = Stage<KIND>::AX;
+    return g.outer * D.n[ax] * D.W[ax] * g.inner;
+}
+
+template <typename T, int KIND>
+GS_HD void contractItem(const DevPatch& D, long long item, const T* __restrict__ in, T* __restrict__ out,
+                        const int* __restrict__ ibuf, const T* __restrict__ pf) {
+    using S = Stage<KIND>;
+    const int ax = S::AX;
+    const StageGeom G = stageGeom<KIND>(D);
+    const int n = D.n[ax], W = D.W[ax], q = D.q[ax], p = D.p[ax], Qa = D.Q[ax], E = D.E[ax];
+    const long long c = item % G.inner;
+    long long r = item / G.inner;
+    const int oi = int(r % W);
+    r /= W;
+    const int i = int(r % n);
+    const long long o = r / n;
+    const int j = i + oi - p;
+    T acc[S::NOUT];
+    for (int h = 0; h < S::NOUT; ++h) acc[h] = T(0);
+    if (j >= 0 && j < n) {
+        const int* first = ibuf + D.eoff[ax];
+        const int* elo = ibuf + D.doff[ax];
+        const int* ehi = elo + n;
+        const int e0 = elo[i] > elo[j] ? elo[i] : elo[j];
+        const int e1 = ehi[i] < ehi[j] ? ehi[i] : ehi[j];
+        const int P1 = p + 1;
+        const long long tstride = (long long)E * q * P1 * P1;  // per pair type
+        const T* pfa = pf + D.pfoff[ax];
+        for (int e = e0; e <= e1; ++e) {
+            const int fe = first[e];
+            const int s = i - fe, t = j - fe;
+            for (int rr = 0; rr < q; ++rr) {
+                const int g = e * q + rr;
+                const long long pidx = ((long long)(e * q + rr) * P1 + s) * P1 + t;
+                T x[S::NIN];
+                const T* ip = in + G.in_base + (o * Qa + g) * G.inner + c;
+                for (int f = 0; f < S::NIN; ++f) x[f] = ip[f * G.in_fs];
+                T pv[4];
+                for (int tau = 0; tau < 4; ++tau) pv[tau] = GS_LDG(pfa + tau * tstride + pidx);
+                for (int k = 0; k < S::NT; ++k) {
+                    const Term tm = S::term(k);
+                    acc[tm.h] += pv[tm.tau] * x[tm.f];
+                }
+            }
+        }
+    }
+    T* op = out + G.out_base + ((o * n + i) * W + oi) * G.inner + c;
+    for (int h = 0; h < S::NOUT; ++h) op[h * G.out_fs] = acc[h];
+}
+
+// -------------------------------------------------------------------------------------------
+// load vector: single-index contraction of L with the basis values along one axis
+//   3D: 31: L[g2][g1][g0] -> lv1[g2][g1][i0]; 32: lv1 -> lv2[g2][i1][i0]; 33: lv2 -> F[i2][i1][i0]
+//   2D: 21: L[g1][g0] -> lv1[g1][i0]; 22: lv1 -> F[i1][i0]
+struct LoadGeom {
+    long long outer, inner, in_base, out_base;
+};
+template <int KIND>
+GS_HD LoadGeom loadGeom(const DevPatch& D) {
+    LoadGeom g{};
+    if (KIND == 31) { g.outer = (long long)D.Q[2] * D.Q[1]; g.inner = 1; g.in_base = D.lfield_off; g.out_base = D.lv1_off; }
+    else if (KIND == 32) { g.outer = D.Q[2]; g.inner = D.n[0]; g.in_base = D.lv1_off; g.out_base = D.lv2_off; }
+    else if (KIND == 33) { g.outer = 1; g.inner = (long long)D.n[1] * D.n[0]; g.in_base = D.lv2_off; g.out_base = D.lvec_off; }
+    else if (KIND == 21) { g.outer = D.Q[1]; g.inner = 1; g.in_base = D.lfield_off; g.out_base = D.lv1_off; }
+    else { g.outer = 1; g.inner = D.n[0]; g.in_base = D.lv1_off; g.out_base = D.lvec_off; }
+    return g;
+}
+template <int KIND>
+GS_HD long long loadWork(const DevPatch& D) {
+    const LoadGeom g = loadGeom<KIND>(D);
+    const int ax = Stage<KIND>::AX;
+    return g.outer * D.n[ax] * g.inner;
+}
+// the input of stage 31/21 is the L field, of later stages the previous intermediate; the
+// caller passes the right base pointers (L field buffer or intermediate buffer)
+template <int KIND>
+GS_HD double loadItem(const DevPatch& D, long long item, const double* __restrict__ in, const double* __restrict__ tab,
+                      const int* __restrict__ ibuf) {
+    const int ax = Stage<KIND>::AX;
+    const LoadGeom G = loadGeom<KIND>(D);
+    const int n = D.n[ax], q = D.q[ax], p = D.p[ax], Qa = D.Q[ax];
+    const long long c = item % G.inner;
+    long long r = item / G.inner;
+    const int i = int(r % n);
+    const long long o = r / n;
+    const int* first = ibuf + D.eoff[ax];
+    const int* elo = ibuf + D.doff[ax];
+    const int* ehi = elo + n;
+    const double* tb = tab + D.toff[ax];
+    double acc = 0.0;
+    for (int e = elo[i]; e <= ehi[i]; ++e) {
+        const int s = i - first[e];
+        for (int rr = 0; rr < q; ++rr) {
+            const int g = e * q + rr;
+            acc += tb[(long long)g * 2 * (p + 1) + s] * in[G.in_base + (o * Qa + g) * G.inner + c];
+        }
+    }
+    return acc;
+}
+
+// -------------------------------------------------------------------------------------------
+// CSR values: segmented reduction of band entries over the precomputed slot map
+template <typename T>
+GS_HD T gatherSlot(uint32_t src, const T* __restrict__ band, const uint32_t* __restrict__ ovf_ptr,
+                   const uint32_t* __restrict__ ovf_idx) {
+    if (!(src & 0x80000000u)) return band[src];
+    const uint32_t o = src & 0x7fffffffu;
+    T acc = T(0);
+    for (uint32_t k = ovf_ptr[o]; k < ovf_ptr[o + 1]; ++k) acc += band[ovf_idx[k]];
+    return acc;
+}
+
+// rhs row: load-vector sources minus the Dirichlet lift sum_j K_ij g_j over eliminated j
+// (gsSparseSystem::push, src/gsAssembler/gsSparseSystem.h:972-1010)
+GS_HD double rhsRow(int I, const double* __restrict__ lvec, const uint32_t* __restrict__ lptr,
+                    const uint32_t* __restrict__ lidx, const double* __restrict__ band,
+                    const uint32_t* __restrict__ fptr, const uint32_t* __restrict__ fband,
+                    const uint32_t* __restrict__ fbidx, const double* __restrict__ ddof) {
+    double acc = 0.0;
+    for (uint32_t k = lptr[I]; k < lptr[I + 1]; ++k) acc += lvec[lidx[k]];
+    for (uint32_t k = fptr[I]; k < fptr[I + 1]; ++k) acc -= band[fband[k]] * ddof[fbidx[k]];
+    return acc;
+}
+
+}  // namespace dev
+}  // namespace gsgpu

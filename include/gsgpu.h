@@ -1,0 +1,153 @@
+/* gsgpu: GB300 (sm_103a) isogeometric Poisson / diffusion assembly and solve.
+ *
+ * C ABI of libgsgpu.so. Plain pointers and sizes only; every entry point returns a status code
+ * (GSGPU_OK on success) and the message of the last failure is available from
+ * gsgpu_last_error(). Each entry point names the G+Smo interface it replaces (paths relative to
+ * the G+Smo source tree). A context owns all device memory of one problem; contexts are
+ * independent and may be used from different host threads, one thread per context at a time
+ * (G+Smo: one assembler object is not safe for concurrent assemble() calls either).
+ */
+#ifndef GSGPU_H
+#define GSGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (G+Smo reports failures as exceptions from GISMO_ENSURE / GISMO_ERROR,
+ * src/gsCore/gsDebug.h:88-120; non-convergence is not an exception there either) */
+#define GSGPU_OK 0
+#define GSGPU_ERR_INVALID 1       /* invalid argument / unsupported input */
+#define GSGPU_ERR_CUDA 2          /* CUDA runtime error */
+#define GSGPU_ERR_BUDGET 3        /* device-memory budget exceeded */
+#define GSGPU_ERR_NOT_CONVERGED 4 /* solver reached MaxIterations (solution still returned) */
+#define GSGPU_ERR_JACOBIAN 5      /* geometry map has det J <= 0 at a quadrature point */
+#define GSGPU_ERR_STATE 6         /* call out of order (e.g. matrix() before assemble()) */
+#define GSGPU_ERR_TIMEOUT 7       /* a bounded device wait gave up */
+
+typedef struct gsgpu_context gsgpu_context;
+
+/* Problem description: what G+Smo receives as gsMultiPatch + gsMultiBasis +
+ * gsBoundaryConditions + the PDE functions in the gsPoissonAssembler / gsCDRAssembler
+ * constructors (src/gsAssembler/gsPoissonAssembler.h:93-106, gsCDRAssembler.h:113-125).
+ * Patches are tensor-product B-spline maps (gsTensorBSpline, dim 2 or 3); the discretisation
+ * basis of patch k is given by degree/knots, the geometry basis by gdegree/gknots.
+ * Interfaces are conforming with identity orientation (the gsBoxTopology interfaces of
+ * gsNurbsCreator::BSplineSquareGrid / BSplineCubeGrid), eliminated by gluing (iFace::glue).
+ * Dirichlet sides are eliminated (dirichlet::elimination) with values by interpolation
+ * (dirichlet::interpolation, gsAssembler.hpp:314-390) of the exact solution u.
+ * Coefficient, source and exact solution are closed forms evaluated on the device:
+ *   g(x) = kappa_scale * sum_m kappa_amp[m] cos(pi kappa_k[m].x + kappa_phase[m])
+ *   kappa = exp(kappa_alpha * g) if kappa_fourier else kappa_const
+ *   u = prod_i sin(ufreq pi x_i),  f = -div(kappa grad u). */
+typedef struct {
+    int dim;
+    int npatches;
+    const int* degree;     /* npatches*3 (unused directions: 0) */
+    const int* nknots;     /* npatches*3 */
+    const double* knots;   /* all knot vectors, patch-major then direction */
+    const int* gdegree;
+    const int* gnknots;
+    const double* gknots;
+    const double* coefs;   /* control points, patch-major, (ncoef x dim) row-major,
+                              first parametric direction fastest (gsTensorBasis numbering) */
+    int ninterfaces;
+    const int* interfaces; /* 4 ints per interface: patch1 side1 patch2 side2 (boxSide numbers) */
+    int ndirichlet;
+    const int* dirichlet;  /* 2 ints per side: patch side */
+    int kappa_fourier;
+    double kappa_const, kappa_alpha, kappa_scale;
+    int kappa_nmodes;
+    const double* kappa_amp;
+    const int* kappa_k;    /* 3 ints per mode, each in [0, 8] */
+    const double* kappa_phase;
+    int ufreq;
+    double quA;            /* Gauss points per direction: quA * degree + quB (gsQuadrature.h:151-171) */
+    int quB;
+} gsgpu_problem;
+
+/* solver options (gsIterativeSolver::defaultOptions gsIterativeSolver.h:92-99,
+ * gsMultiGridOp options gsMultiGrid.hpp:299-328, gsJacobiOp "Damping") */
+#define GSGPU_SOLVER_CG_JACOBI 0
+#define GSGPU_SOLVER_CG_MG 1
+#define GSGPU_PREC_FP64 0   /* plain FP64 */
+#define GSGPU_PREC_MIXED 1  /* FP32 inner iteration, FP64 residual / refinement */
+typedef struct {
+    int method;
+    int precision;
+    double tol;            /* relative residual ||r||/||b|| ("Tolerance", default 1e-10) */
+    int max_iters;         /* "MaxIterations", default 1000 */
+    int mg_levels;         /* "Levels" of gsGridHierarchy::buildByCoarsening */
+    int mg_npre, mg_npost; /* "NumPreSmooth", "NumPostSmooth" */
+    double mg_damping;     /* damping of the Jacobi smoother */
+    double inner_tol;      /* mixed precision: FP32 inner reduction per refinement step */
+} gsgpu_solver_opts;
+
+typedef struct {
+    int iterations;        /* gsIterativeSolver::iterations() */
+    double relres;         /* gsIterativeSolver::error(): final ||b - A x|| / ||b|| */
+    int refinements;       /* mixed precision: outer FP64 residual evaluations */
+    double t_solve_ms;     /* device time of the solve */
+} gsgpu_solve_info;
+
+/* lifetime. device >= 0: a CUDA device. device == -1: a host-only context that computes the
+ * dof map and the sparsity pattern (set_problem, refresh, sizes, dof_map, matrix_csr with
+ * val == NULL) and refuses every numerical call with GSGPU_ERR_STATE. */
+int gsgpu_create(gsgpu_context** ctx, int device);
+int gsgpu_destroy(gsgpu_context* ctx);
+const char* gsgpu_last_error(const gsgpu_context* ctx);
+
+/* gsPoissonAssembler(patches, bases, bc, rhs) / gsCDRAssembler(..., coeff_A = kappa I, b = 0,
+ * c = 0) constructors: copy the problem into the context (nothing is retained) */
+int gsgpu_set_problem(gsgpu_context* ctx, const gsgpu_problem* prob);
+/* gsAssembler::refresh() (gsPoissonAssembler.hpp:33-38, gsAssembler.hpp:101-122): dof mapper,
+ * symbolic sparsity pattern, gather maps, device buffers */
+int gsgpu_refresh(gsgpu_context* ctx);
+/* replace the control points of all patches (same count and layout as in the problem) without
+ * redoing refresh(); the next assemble() uses them (G+Smo: mutating gsMultiPatch::patch(k).coefs()) */
+int gsgpu_set_coefs(gsgpu_context* ctx, const double* coefs);
+/* gsPoissonAssembler::assemble() (gsPoissonAssembler.hpp:41-78): Dirichlet values, element
+ * integrals, scatter into the CSR system. precision: GSGPU_PREC_FP64 assembles the FP64 system;
+ * GSGPU_PREC_MIXED additionally keeps the FP32 inner operator used by the mixed solver. */
+int gsgpu_assemble(gsgpu_context* ctx, int precision);
+
+/* sizes: gsAssembler::numDofs() (gsAssembler.h:633-639), matrix().nonZeros(),
+ * gsDofMapper::boundarySize(), total patch-local dofs */
+int gsgpu_sizes(gsgpu_context* ctx, int* nfree, long long* nnz, int* nfixed, int* nlocal);
+/* gsAssembler::matrix() (gsAssembler.h:614) as CSR (the matrix is symmetric, so these are also
+ * the compressed ColMajor arrays outerIndexPtr / innerIndexPtr / valuePtr). Any of the three
+ * pointers may be NULL; ptr/col are available after refresh(), val after assemble(). */
+int gsgpu_matrix_csr(gsgpu_context* ctx, int* ptr, int* col, double* val);
+/* gsAssembler::rhs() (gsAssembler.h:618) */
+int gsgpu_rhs(gsgpu_context* ctx, double* rhs);
+/* gsAssembler::fixedDofs() (gsAssembler.h:538) */
+int gsgpu_fixed_dofs(gsgpu_context* ctx, double* ddof);
+/* gsDofMapper::asVector() (gsDofMapper.cpp:80-87) over all patches */
+int gsgpu_dof_map(gsgpu_context* ctx, int* index);
+
+/* gsConjugateGradient(matrix, gsJacobiOp | gsMultiGridOp).solve(rhs, x)
+ * (gsIterativeSolver.h:114-125, gsConjugateGradient.hpp:19-84). x: host array of nfree values
+ * (may be NULL to keep the solution on the device only). */
+int gsgpu_solve(gsgpu_context* ctx, const gsgpu_solver_opts* opts, double* x, gsgpu_solve_info* info);
+/* gsField::distanceL2 of the last solution against u (gsField.hpp:23-41) */
+int gsgpu_l2_error(gsgpu_context* ctx, double* err);
+
+/* Utilities with no counterpart in the reference. */
+/* the CUDA stream (cudaStream_t) all device work of the context is issued on */
+int gsgpu_stream(gsgpu_context* ctx, void** stream);
+/* profiling: when on, solve() launches its iterations one by one (no CUDA graph) and brackets
+ * every SpMV with CUDA events; gsgpu_spmv_stats returns the launches and their summed device
+ * time since profiling was switched on. */
+int gsgpu_set_profiling(gsgpu_context* ctx, int on);
+int gsgpu_spmv_stats(gsgpu_context* ctx, long long* launches, double* total_ms, double* bytes_per_launch);
+/* smallest det J over all quadrature points of the last assemble() */
+int gsgpu_min_jacobian(gsgpu_context* ctx, double* detmin);
+/* device-time breakdown of the last assemble() in milliseconds:
+ * [0] Dirichlet values, [1] basis tables, [2] geometry + coefficient fields,
+ * [3] stiffness contraction, [4] load contraction, [5] CSR + rhs scatter, [6] total */
+int gsgpu_assemble_times(gsgpu_context* ctx, double* ms7);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

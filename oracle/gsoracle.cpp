@@ -682,7 +682,8 @@ struct Oracle {
     double assemble(int nthreads, long long maxElems) {
         auto t0 = std::chrono::steady_clock::now();
         dirichletValues();
-        buildPattern();
+        if (A.ptr.empty()) buildPattern();  // symbolic set-up once per problem
+        std::fill(A.val.begin(), A.val.end(), 0.0);
         rhs.assign(map.freeSize, 0.0);
         long long ne = totalElems();
         if (maxElems >= 0) ne = std::min(ne, maxElems);

@@ -1,0 +1,82 @@
+"""The C-ABI library (CPU checks): it loads, exports every entry point include/gsgpu.h declares,
+and its host-side plan (gsDofMapper numbering, sparsity pattern) matches the reference fixtures.
+No numerical call is made here: host-only contexts refuse them."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from gismo_gb300 import _lib
+from gismo_gb300.assembler import PackedProblem
+from tests.golden_cases import golden_problem, load_golden
+from tests.test_oracle_golden import GOLDEN, _csr_from_csc
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "gsgpu.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(gsgpu_[a-z0-9_]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import __graft_entry__ as g
+    g.build()
+    return _lib.lib()
+
+
+def test_exports_every_declared_symbol(lib):
+    syms = declared_symbols()
+    assert len(syms) >= 15
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert sorted(_lib.EXPORTS) == syms
+
+
+def _host_ctx(lib, prob):
+    h = C.c_void_p()
+    assert lib.gsgpu_create(C.byref(h), -1) == _lib.OK
+    pk = PackedProblem(prob)
+    assert lib.gsgpu_set_problem(h, C.byref(pk.struct)) == _lib.OK
+    assert lib.gsgpu_refresh(h) == _lib.OK
+    return h, pk
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_host_plan_matches_reference(lib, path):
+    name = os.path.basename(path)[:-4]
+    g = load_golden(name)
+    h, pk = _host_ctx(lib, golden_problem(name))
+    try:
+        nf, nnz, nb, nl = C.c_int(), C.c_longlong(), C.c_int(), C.c_int()
+        assert lib.gsgpu_sizes(h, C.byref(nf), C.byref(nnz), C.byref(nb), C.byref(nl)) == _lib.OK
+        assert nf.value == int(g["free"]) and nnz.value == int(g["nnz"])
+        dm = np.empty(nl.value, np.int32)
+        assert lib.gsgpu_dof_map(h, dm.ctypes.data) == _lib.OK
+        assert np.array_equal(dm, g["dofmap"])
+        ptr = np.empty(nf.value + 1, np.int32)
+        col = np.empty(nnz.value, np.int32)
+        assert lib.gsgpu_matrix_csr(h, ptr.ctypes.data, col.ctypes.data, None) == _lib.OK
+        K = _csr_from_csc(g)
+        assert np.array_equal(ptr, K.indptr) and np.array_equal(col, K.indices)
+        # numerical calls are refused without a device
+        assert lib.gsgpu_assemble(h, 0) == _lib.ERR_STATE
+    finally:
+        lib.gsgpu_destroy(h)
+
+
+def test_invalid_problem_is_rejected(lib):
+    from gismo_gb300 import problems as P
+    prob = P.square_poisson(4, 2)
+    prob.dirichlet = [(0, 9)]  # no side 9 on a 2D patch
+    h = C.c_void_p()
+    assert lib.gsgpu_create(C.byref(h), -1) == _lib.OK
+    pk = PackedProblem(prob)
+    assert lib.gsgpu_set_problem(h, C.byref(pk.struct)) == _lib.ERR_INVALID
+    assert b"dirichlet" in lib.gsgpu_last_error(h)
+    assert lib.gsgpu_refresh(h) == _lib.ERR_STATE
+    lib.gsgpu_destroy(h)

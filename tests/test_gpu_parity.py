@@ -1,0 +1,147 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference fixtures and the CPU oracle.
+
+Bars (the benchmark spec): dof map and sparsity pattern bit-exact; FP64 matrix and rhs entries within
+1e-12 relative (absolute floor 1e-14 x the row's largest entry for entries that cancel to ~0);
+CG iteration counts within one of the reference's; the discrete L2 error to >= 3 significant
+digits."""
+import os
+
+import numpy as np
+import pytest
+
+from gismo_gb300 import problems as P
+from tests.golden_cases import golden_problem, load_golden
+from tests.test_oracle_golden import GOLDEN, _csr_from_csc
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-12
+FLOOR = 1e-14
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__ as g
+    g.build()
+
+
+def _assembler(prob):
+    from gismo_gb300.assembler import GpuPoissonAssembler
+    return GpuPoissonAssembler(prob, device=0)
+
+
+def _check_values(val, ref_val, ref_ptr):
+    rowmax = np.maximum.reduceat(np.abs(ref_val), ref_ptr[:-1])
+    floor = np.repeat(rowmax, np.diff(ref_ptr)) * FLOOR
+    err = np.abs(val - ref_val) - (REL * np.abs(ref_val) + floor)
+    assert np.all(err <= 0), f"max excess {err.max():.3e}"
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_fp64_matches_reference_fixture(path):
+    from oracle import oracle as O
+    name = os.path.basename(path)[:-4]
+    g = load_golden(name)
+    prob = golden_problem(name)
+    A = _assembler(prob)
+    A.assemble()
+    assert np.array_equal(A.dofMapper(), g["dofmap"])
+    ptr, col, val = A.csr()
+    K = _csr_from_csc(g)
+    assert np.array_equal(ptr, K.indptr) and np.array_equal(col, K.indices)
+    _check_values(val, K.data, K.indptr)
+    rhs = A.rhs()
+    assert np.abs(rhs - g["rhs"]).max() <= REL * np.abs(g["rhs"]).max()
+    if len(g["ddof"]):
+        assert np.abs(A.fixedDofs() - g["ddof"]).max() <= REL * max(1.0, np.abs(g["ddof"]).max())
+    if prob.solver == "cg":
+        x, info = A.solve(tol=prob.tol, max_iters=prob.maxit)
+        assert info["converged"]
+        assert abs(info["iterations"] - int(g["iters"])) <= 1
+        assert np.linalg.norm(x - g["x"]) <= 1e-8 * np.linalg.norm(g["x"])
+        o = O.OracleProblem(prob)
+        o.assemble()
+        l2 = o.l2_error(x)
+        assert abs(l2 - float(g["l2"])) <= 5e-4 * float(g["l2"])
+    A.close()
+
+
+@pytest.mark.parametrize("case", ["disp3d_p3_16", "disp2d_p4_40x33", "cubegrid3_p2_n3"])
+def test_fp64_matches_oracle(case):
+    """Sizes beyond the fixtures, against the CPU oracle on the same seeded inputs."""
+    from oracle import oracle as O
+    if case == "disp3d_p3_16":
+        prob = P.volume_poisson(16, 3, seed=2)
+    elif case == "disp2d_p4_40x33":
+        prob = P.displaced_single_patch(2, (40, 33), (4, 4), 9, 0.05, ufreq=3)
+    else:
+        prob = P.cube_grid(n=3, n_elem=3, p=2, seed=5, kappa_modes=32)
+        prob.solver = "cg"
+    o = O.OracleProblem(prob)
+    o.assemble()
+    A = _assembler(prob)
+    A.assemble()
+    assert np.array_equal(A.dofMapper(), o.dofmap())
+    ptr, col, val = A.csr()
+    optr, ocol, oval = o.csr()
+    assert np.array_equal(ptr, optr) and np.array_equal(col, ocol)
+    _check_values(val, oval, optr)
+    assert np.abs(A.rhs() - o.rhs()).max() <= REL * np.abs(o.rhs()).max()
+    x, info = A.solve(tol=1e-10)
+    xo, it, _, _ = o.solve_cg(1e-10, 1000)
+    assert info["converged"] and abs(info["iterations"] - it) <= 1
+    assert np.linalg.norm(x - xo) <= 1e-8 * np.linalg.norm(xo)
+    A.close()
+
+
+def test_full_size_volume_properties():
+    """The 3D degree-3 64^3 configuration at full size: properties that do not need the oracle."""
+    prob = P.volume_poisson(64, 3, seed=1)
+    A = _assembler(prob)
+    A.assemble()
+    nf, nnz, nb, nl = A.sizes()
+    assert (nf, nnz) == (274625, 86938307)
+    K = A.matrix()
+    d = K.diagonal()
+    assert np.all(d > 0)
+    # symmetry of the assembled operator (entries computed independently per (i,j))
+    D = (K - K.T).tocoo()
+    assert np.abs(D.data).max() <= 1e-13 * np.abs(K.data).max()
+    assert A.min_jacobian() > 0.2 * 0  # positive Jacobian everywhere
+    x, info = A.solve(tol=1e-10)
+    assert info["converged"] and info["iterations"] < 400
+    # A x = b to the stopping tolerance, checked in FP64 on the host
+    b = A.rhs()
+    assert np.linalg.norm(b - K @ x) <= 2e-10 * np.linalg.norm(b)
+    A.close()
+
+
+def test_set_coefs_reassembles_new_geometry():
+    """Changing control points without refresh() gives the same system as a fresh assembler."""
+    p1 = P.displaced_single_patch(2, (9, 8), (3, 3), 3, 0.05)
+    p2 = P.displaced_single_patch(2, (9, 8), (3, 3), 4, 0.05)
+    p2.kappa_amp, p2.kappa_k, p2.kappa_phase = p1.kappa_amp, p1.kappa_k, p1.kappa_phase
+    A = _assembler(p1)
+    A.assemble()
+    A.set_coefs(p2.patches[0].coefs)
+    A.assemble()
+    B = _assembler(p2)
+    B.assemble()
+    assert np.array_equal(A.csr()[2], B.csr()[2])
+    assert np.array_equal(A.rhs(), B.rhs())
+    A.close()
+    B.close()
+
+
+def test_inverted_geometry_is_reported():
+    """A folded map (det J <= 0) is a status code, not a fault (G+Smo: GISMO_ENSURE)."""
+    from gismo_gb300._lib import GsGpuError, ERR_JACOBIAN
+    prob = P.square_poisson(6, 2)
+    c = prob.patches[0].coefs.copy()
+    c[:, 0] = 1.0 - c[:, 0]  # mirror x: det J < 0 everywhere
+    prob.patches[0].coefs = c
+    A = _assembler(prob)
+    with pytest.raises(GsGpuError) as e:
+        A.assemble()
+    assert e.value.code == ERR_JACOBIAN
+    A.close()
