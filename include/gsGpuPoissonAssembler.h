@@ -1,0 +1,180 @@
+/** gsGpuPoissonAssembler: drop-in for gismo::gsPoissonAssembler / gsCDRAssembler that assembles
+ *  on a GB300 through libgsgpu (include/gsgpu.h).
+ *
+ *  Header-only; include it in a G+Smo build and link libgsgpu.so. It keeps the
+ *  gsPoissonAssembler interface (src/gsAssembler/gsPoissonAssembler.h:35-142): construct from
+ *  (gsMultiPatch, gsMultiBasis, gsBoundaryConditions, rhs), call assemble(), then matrix(),
+ *  rhs(), fixedDofs(), numDofs(), constructSolution() as usual. refresh() builds the dof map and
+ *  the sparsity pattern on the host and uploads the patch data; assemble() runs the device
+ *  kernels and fills m_system (an Eigen compressed ColMajor matrix with int indices, as G+Smo's).
+ *
+ *  Functions: the device evaluates closed forms, so the coefficient, the source and the
+ *  Dirichlet data are passed as gsGpuFields parameters (kappa = exp(alpha g) with a Fourier
+ *  field g, or a constant; f = -div(kappa grad u) for u = prod sin(freq pi x_i)); the gsFunction
+ *  given to the constructor is kept for G+Smo-side post-processing (e.g. distanceL2).
+ *  Supported inputs: gsTensorBSpline patches of dimension 2 or 3, tensor B-spline bases,
+ *  conforming interfaces with identity orientation (iFace::glue), Dirichlet sides eliminated
+ *  with interpolated values. Anything else throws (no CPU fallback).
+ */
+#pragma once
+
+#include <gsAssembler/gsPoissonAssembler.h>
+#include <gsNurbs/gsTensorBSpline.h>
+#include <gsNurbs/gsTensorBSplineBasis.h>
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "gsgpu.h"
+
+namespace gismo {
+
+struct gsGpuFields {
+    bool kappaFourier = false;
+    double kappaConst = 1.0, kappaAlpha = 0.0, kappaScale = 0.0;
+    std::vector<double> amp, phase;
+    std::vector<int> waves;  // 3 per mode
+    int ufreq = 1;
+};
+
+template <class T = real_t>
+class gsGpuPoissonAssembler : public gsPoissonAssembler<T> {
+public:
+    typedef gsPoissonAssembler<T> Base;
+
+    gsGpuPoissonAssembler(const gsMultiPatch<T>& patches, const gsMultiBasis<T>& basis,
+                          const gsBoundaryConditions<T>& bconditions, const gsFunction<T>& rhs,
+                          const gsGpuFields& fields, int device = 0)
+        : Base(patches, basis, bconditions, rhs, dirichlet::elimination, iFace::glue), m_fields(fields) {
+        check(gsgpu_create(&m_ctx, device));
+        upload();
+    }
+
+    ~gsGpuPoissonAssembler() {
+        if (m_ctx) gsgpu_destroy(m_ctx);
+    }
+
+    /// gsAssembler::refresh(): dof map, sparsity pattern and device buffers
+    void refresh() override {
+        Base::refresh();
+        if (m_ctx) upload();
+    }
+
+    /// gsPoissonAssembler::assemble() on the device
+    void assemble() override {
+        check(gsgpu_assemble(m_ctx, GSGPU_PREC_FP64));
+        int n = 0, nb = 0, nl = 0;
+        long long nnz = 0;
+        check(gsgpu_sizes(m_ctx, &n, &nnz, &nb, &nl));
+        std::vector<int> ptr(n + 1), col(nnz);
+        std::vector<double> val(nnz);
+        check(gsgpu_matrix_csr(m_ctx, ptr.data(), col.data(), val.data()));
+        // the system is symmetric: the CSR arrays are the compressed ColMajor arrays
+        gsSparseMatrix<T>& K = this->m_system.matrix();
+        K.resize(n, n);
+        K.reserve(gsVector<index_t>::Map(std::vector<index_t>(ptr.begin() + 1, ptr.end()).data(), n) -
+                  gsVector<index_t>::Map(std::vector<index_t>(ptr.begin(), ptr.end() - 1).data(), n));
+        for (int c = 0; c < n; ++c)
+            for (int k = ptr[c]; k < ptr[c + 1]; ++k) K.insert(col[k], c) = val[k];
+        K.makeCompressed();
+        gsMatrix<T>& b = this->m_system.rhs();
+        b.resize(n, 1);
+        check(gsgpu_rhs(m_ctx, b.data()));
+        this->m_ddof.resize(1);
+        this->m_ddof[0].resize(nb, 1);
+        if (nb) check(gsgpu_fixed_dofs(m_ctx, this->m_ddof[0].data()));
+    }
+
+    /// CG (+ Jacobi) on the device-resident system (gsConjugateGradient(matrix(), gsJacobiOp))
+    int solve(gsMatrix<T>& x, double tol = 1e-10, int maxIter = 1000) {
+        gsgpu_solver_opts o = {GSGPU_SOLVER_CG_JACOBI, GSGPU_PREC_FP64, tol, maxIter, 4, 2, 2, 0.6, 1e-4};
+        gsgpu_solve_info info;
+        x.resize(this->numDofs(), 1);
+        const int rc = gsgpu_solve(m_ctx, &o, x.data(), &info);
+        if (rc != GSGPU_OK && rc != GSGPU_ERR_NOT_CONVERGED) check(rc);
+        return info.iterations;
+    }
+
+private:
+    void check(int rc) const {
+        if (rc != GSGPU_OK)
+            throw std::runtime_error(std::string("gsgpu: ") + (m_ctx ? gsgpu_last_error(m_ctx) : "no context"));
+    }
+
+    template <short_t D>
+    void packPatch(index_t k) {
+        const gsTensorBSplineBasis<D, T>* db =
+            dynamic_cast<const gsTensorBSplineBasis<D, T>*>(&this->m_bases[0][k]);
+        const gsTensorBSpline<D, T>* geo = dynamic_cast<const gsTensorBSpline<D, T>*>(&this->patches().patch(k));
+        if (!db || !geo) throw std::invalid_argument("gsGpuPoissonAssembler: tensor B-spline patches and bases only");
+        for (short_t i = 0; i < 3; ++i) {
+            if (i < D) {
+                const gsKnotVector<T>& kv = db->knots(i);
+                m_degree.push_back(kv.degree());
+                m_nknots.push_back(index_t(kv.size()));
+                m_knots.insert(m_knots.end(), kv.begin(), kv.end());
+                const gsKnotVector<T>& gk = geo->basis().knots(i);
+                m_gdegree.push_back(gk.degree());
+                m_gnknots.push_back(index_t(gk.size()));
+                m_gknots.insert(m_gknots.end(), gk.begin(), gk.end());
+            } else {
+                m_degree.push_back(0); m_nknots.push_back(0); m_gdegree.push_back(0); m_gnknots.push_back(0);
+            }
+        }
+        const gsMatrix<T>& c = geo->coefs();
+        for (index_t r = 0; r < c.rows(); ++r)
+            for (index_t m = 0; m < c.cols(); ++m) m_coefs.push_back(c(r, m));
+    }
+
+    void upload() {
+        const gsMultiPatch<T>& mp = this->patches();
+        const short_t d = mp.parDim();
+        m_degree.clear(); m_nknots.clear(); m_knots.clear();
+        m_gdegree.clear(); m_gnknots.clear(); m_gknots.clear(); m_coefs.clear();
+        m_ifaces.clear(); m_dsides.clear();
+        for (size_t k = 0; k < mp.nPatches(); ++k) {
+            if (d == 2) packPatch<2>(index_t(k));
+            else if (d == 3) packPatch<3>(index_t(k));
+            else throw std::invalid_argument("gsGpuPoissonAssembler: dimension 2 or 3 only");
+        }
+        for (typename gsMultiPatch<T>::const_iiterator it = mp.iBegin(); it != mp.iEnd(); ++it) {
+            if (!it->dirOrientation().all()) throw std::invalid_argument("gsGpuPoissonAssembler: re-oriented interface");
+            for (index_t i = 0; i < it->dirMap().size(); ++i)
+                if (it->dirMap()(i) != i) throw std::invalid_argument("gsGpuPoissonAssembler: permuted interface");
+            m_ifaces.push_back(it->first().patch);
+            m_ifaces.push_back(it->first().side().index());
+            m_ifaces.push_back(it->second().patch);
+            m_ifaces.push_back(it->second().side().index());
+        }
+        const gsBoundaryConditions<T>& bc = this->pde().bc();
+        for (typename gsBoundaryConditions<T>::const_iterator it = bc.dirichletBegin(); it != bc.dirichletEnd(); ++it) {
+            m_dsides.push_back(it->patch());
+            m_dsides.push_back(it->side().index());
+        }
+        gsgpu_problem p;
+        p.dim = d;
+        p.npatches = int(mp.nPatches());
+        p.degree = m_degree.data(); p.nknots = m_nknots.data(); p.knots = m_knots.data();
+        p.gdegree = m_gdegree.data(); p.gnknots = m_gnknots.data(); p.gknots = m_gknots.data();
+        p.coefs = m_coefs.data();
+        p.ninterfaces = int(m_ifaces.size() / 4); p.interfaces = m_ifaces.data();
+        p.ndirichlet = int(m_dsides.size() / 2); p.dirichlet = m_dsides.data();
+        p.kappa_fourier = m_fields.kappaFourier ? 1 : 0;
+        p.kappa_const = m_fields.kappaConst; p.kappa_alpha = m_fields.kappaAlpha; p.kappa_scale = m_fields.kappaScale;
+        p.kappa_nmodes = int(m_fields.amp.size());
+        p.kappa_amp = m_fields.amp.data(); p.kappa_k = m_fields.waves.data(); p.kappa_phase = m_fields.phase.data();
+        p.ufreq = m_fields.ufreq;
+        p.quA = this->m_options.getReal("quA");
+        p.quB = this->m_options.getInt("quB");
+        check(gsgpu_set_problem(m_ctx, &p));
+        check(gsgpu_refresh(m_ctx));
+    }
+
+    gsgpu_context* m_ctx = nullptr;
+    gsGpuFields m_fields;
+    std::vector<int> m_degree, m_nknots, m_gdegree, m_gnknots, m_ifaces, m_dsides;
+    std::vector<double> m_knots, m_gknots, m_coefs;
+};
+
+}  // namespace gismo
