@@ -13,7 +13,7 @@ EXPORTS = [
     "gsgpu_create", "gsgpu_destroy", "gsgpu_last_error", "gsgpu_set_problem", "gsgpu_refresh", "gsgpu_set_coefs",
     "gsgpu_assemble", "gsgpu_sizes", "gsgpu_matrix_csr", "gsgpu_rhs", "gsgpu_fixed_dofs", "gsgpu_dof_map",
     "gsgpu_solve", "gsgpu_l2_error", "gsgpu_min_jacobian", "gsgpu_assemble_times", "gsgpu_stream",
-    "gsgpu_set_profiling", "gsgpu_spmv_stats",
+    "gsgpu_set_profiling", "gsgpu_spmv_stats", "gsgpu_cg_jacobi_noalloc",
 ]
 
 OK, ERR_INVALID, ERR_CUDA, ERR_BUDGET, ERR_NOT_CONVERGED, ERR_JACOBIAN, ERR_STATE, ERR_TIMEOUT = range(8)
@@ -84,6 +84,8 @@ def lib() -> C.CDLL:
         L.gsgpu_stream.argtypes = [vp, C.POINTER(vp)]
         L.gsgpu_set_profiling.argtypes = [vp, C.c_int]
         L.gsgpu_spmv_stats.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.gsgpu_cg_jacobi_noalloc.argtypes = [C.c_int, vp, vp, vp, vp, vp, C.c_double, C.c_int, vp,
+                                               C.POINTER(C.c_int), C.POINTER(C.c_double)]
         for name in EXPORTS:
             if name != "gsgpu_last_error":
                 getattr(L, name).restype = C.c_int
