@@ -6,10 +6,12 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/gsgpu.h"
@@ -95,12 +97,21 @@ void Context::buildTables() {
         mk(tabSt[0], [](const DevPatch& D) { return dev::stageWork<31>(D); });
         mk(tabSt[1], [](const DevPatch& D) { return dev::stageWork<32>(D); });
         mk(tabSt[2], [](const DevPatch& D) { return dev::stageWork<33>(D); });
+        for (int P = 1; P <= 4; ++P) {
+            mk(tabRow[0][P], [P](const DevPatch& D) { return D.p[0] == P ? dev::stageRowWork<31>(D) : 0LL; });
+            mk(tabRow[1][P], [P](const DevPatch& D) { return D.p[1] == P ? dev::stageRowWork<32>(D) : 0LL; });
+            mk(tabRow[2][P], [P](const DevPatch& D) { return D.p[2] == P ? dev::stageRowWork<33>(D) : 0LL; });
+        }
         mk(tabLd[0], [](const DevPatch& D) { return dev::loadWork<31>(D); });
         mk(tabLd[1], [](const DevPatch& D) { return dev::loadWork<32>(D); });
         mk(tabLd[2], [](const DevPatch& D) { return dev::loadWork<33>(D); });
     } else {
         mk(tabSt[0], [](const DevPatch& D) { return dev::stageWork<21>(D); });
         mk(tabSt[1], [](const DevPatch& D) { return dev::stageWork<22>(D); });
+        for (int P = 1; P <= 4; ++P) {
+            mk(tabRow[0][P], [P](const DevPatch& D) { return D.p[0] == P ? dev::stageRowWork<21>(D) : 0LL; });
+            mk(tabRow[1][P], [P](const DevPatch& D) { return D.p[1] == P ? dev::stageRowWork<22>(D) : 0LL; });
+        }
         mk(tabLd[0], [](const DevPatch& D) { return dev::loadWork<21>(D); });
         mk(tabLd[1], [](const DevPatch& D) { return dev::loadWork<22>(D); });
     }
@@ -126,8 +137,15 @@ void Context::refresh() {
         diag[r] = pat.ptr[r] + int(f - b);
     }
     upload(arena, dPatches, L.dev, stream);
-    std::vector<FieldParams> fp(1, pd.fields);
-    upload(arena, dFields, fp, stream);
+    std::vector<dev::FieldConst<double>> fc64(1, dev::fieldConst<double>(pd.fields));
+    upload(arena, dFields, fc64, stream);
+    std::vector<dev::FieldConst<df32>> fcdf(1, dev::fieldConst<df32>(pd.fields));
+    upload(arena, dFieldsDf, fcdf, stream);
+    {
+        std::vector<df32> w(L.wq.size());
+        for (size_t i = 0; i < w.size(); ++i) w[i] = df32(L.wq[i]);
+        upload(arena, dWqDf, w, stream);
+    }
     upload(arena, dKnots, L.knots, stream);
     upload(arena, dGknots, L.gknots, stream);
     upload(arena, dTabJobs, L.tabjobs, stream);
@@ -161,6 +179,21 @@ void Context::refresh() {
     upload(arena, dFband, pat.fband.empty() ? std::vector<uint32_t>(1, 0) : pat.fband, stream);
     upload(arena, dFbidx, pat.fbidx.empty() ? std::vector<uint32_t>(1, 0) : pat.fbidx, stream);
     upload(arena, dDiag, diag, stream);
+    {
+        // banded patterns (single patches) store columns as 16-bit offsets from the row
+        bool fits = true;
+        for (int r = 0; r < pat.n && fits; ++r)
+            for (int k = pat.ptr[r]; k < pat.ptr[r + 1]; ++k)
+                if (pat.col[k] - r > 32767 || pat.col[k] - r < -32768) { fits = false; break; }
+        arena.release(dColOff);
+        dColOff = nullptr;
+        if (fits && !pat.col.empty()) {
+            std::vector<int16_t> off(pat.col.size());
+            for (int r = 0; r < pat.n; ++r)
+                for (int k = pat.ptr[r]; k < pat.ptr[r + 1]; ++k) off[k] = int16_t(pat.col[k] - r);
+            upload(arena, dColOff, off, stream);
+        }
+    }
     allocN(arena, dVal, (long long)pat.col.size());
     allocN(arena, dRhs, pat.n);
     allocN(arena, dDdof, std::max(1, map.boundarySize));
@@ -198,28 +231,103 @@ void Context::assemble(int precision) {
     for (int i = 0; i < 8; ++i)
         if (!ev[i]) GSGPU_CUDA_TRY(cudaEventCreate(&ev[i]));
     GSGPU_CUDA_TRY(cudaEventRecord(ev[0], s));
-    // Dirichlet values (host, gsAssembler::computeDirichletDofsIntpl) -> device
-    auto t0 = std::chrono::steady_clock::now();
-    dirichletValues(pd, map, ddof);
-    hostDirichletMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    if (!ddof.empty())
-        GSGPU_CUDA_TRY(cudaMemcpyAsync(dDdof, ddof.data(), ddof.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    // Dirichlet values (gsAssembler::computeDirichletDofsIntpl) are computed on the host while the
+    // device runs K1-K3; they are only needed by the rhs lift at the end
+    struct HostTask {
+        std::thread th;
+        std::exception_ptr err;
+        ~HostTask() {
+            if (th.joinable()) th.join();
+        }
+    } dir;
+    std::vector<double> ddofNew;
+    double dirMs = 0.0;
+    dir.th = std::thread([&] {
+        try {
+            auto t0 = std::chrono::steady_clock::now();
+            dirichletValues(pd, map, ddofNew);
+            dirMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        } catch (...) {
+            dir.err = std::current_exception();
+        }
+    });
     GSGPU_CUDA_TRY(cudaEventRecord(ev[1], s));
     // K1: basis tables and pair factors
+    const bool mixed = precision == kMixed;
+    if (mixed) ensureMixedBuffers();
     launch::basisTables(dTabJobs, (long long)L.tabjobs.size(), dKnots, dTab, s);
     launch::basisTables(dGtabJobs, (long long)L.gtabjobs.size(), dGknots, dGtab, s);
-    launch::pairFactors<double>(dPfJobs, tabPf.d, (long long)tabPf.h.size(), dTab, dPf, s);
+    // the df32 path reuses the FP64 intermediate buffers (same 8-byte element size)
+    df32* gtabDf = reinterpret_cast<df32*>(dGtab);
+    df32* pfDf = reinterpret_cast<df32*>(dPf);
+    if (mixed) {
+        launch::toDF(L.ngtab, dGtab, gtabDf, s);  // element-wise in place
+        launch::pairFactors<df32>(dPfJobs, tabPf.d, (long long)tabPf.h.size(), dTab, pfDf, s);
+        launch::toDF(L.coefs, dCoefs, dCoefsDf, s);
+    } else {
+        launch::pairFactors<double>(dPfJobs, tabPf.d, (long long)tabPf.h.size(), dTab, dPf, s);
+    }
     GSGPU_CUDA_TRY(cudaEventRecord(ev[2], s));
     // K2: geometry map, Jacobians, coefficient and load fields
     const unsigned long long init = launch::detKeyInit();
     GSGPU_CUDA_TRY(cudaMemcpyAsync(dDetKey, &init, sizeof(init), cudaMemcpyHostToDevice, s));
-    launch::geoStage1(dPatches, tabGeo1.d, (long long)tabGeo1.h.size(), dCoefs, dGtab, dIbuf, dY1, s);
-    if (pd.dim == 3) launch::geoStage2(dPatches, tabGeo2.d, (long long)tabGeo2.h.size(), dY1, dGtab, dIbuf, dY2, s);
-    launch::pointStep(dPatches, tabPoint.d, (long long)tabPoint.h.size(), dFields, dY1, dY2, dGtab, dIbuf, dWq,
-                      dFieldC, dFieldL, dDetKey, s);
+    df32* y1Df = reinterpret_cast<df32*>(dY1);
+    df32* y2Df = reinterpret_cast<df32*>(dY2);
+    df32* cDf = reinterpret_cast<df32*>(dFieldC);
+    df32* lDf = reinterpret_cast<df32*>(dFieldL);
+    df32* sDf = reinterpret_cast<df32*>(dS);
+    df32* uDf = reinterpret_cast<df32*>(dU);
+    df32* bandDf = reinterpret_cast<df32*>(dBand);
+    if (mixed) {
+        launch::geoStage1<df32>(dPatches, tabGeo1.d, (long long)tabGeo1.h.size(), dCoefsDf, gtabDf, dIbuf, y1Df, s);
+        if (pd.dim == 3)
+            launch::geoStage2<df32>(dPatches, tabGeo2.d, (long long)tabGeo2.h.size(), y1Df, gtabDf, dIbuf, y2Df, s);
+        launch::pointStep<df32>(dPatches, tabPoint.d, (long long)tabPoint.h.size(), dFieldsDf, y1Df, y2Df, gtabDf,
+                                dIbuf, dWqDf, cDf, lDf, dDetKey, s);
+    } else {
+        launch::geoStage1<double>(dPatches, tabGeo1.d, (long long)tabGeo1.h.size(), dCoefs, dGtab, dIbuf, dY1, s);
+        if (pd.dim == 3)
+            launch::geoStage2<double>(dPatches, tabGeo2.d, (long long)tabGeo2.h.size(), dY1, dGtab, dIbuf, dY2, s);
+        launch::pointStep<double>(dPatches, tabPoint.d, (long long)tabPoint.h.size(), dFields, dY1, dY2, dGtab, dIbuf,
+                                  dWq, dFieldC, dFieldL, dDetKey, s);
+    }
     GSGPU_CUDA_TRY(cudaEventRecord(ev[3], s));
     // K3: sum-factorised stiffness contraction into the band
-    if (pd.dim == 3) {
+    if (mixed) {
+        // row-blocked df32 contractions (all band offsets of a row function per work item), one
+        // launch per degree class along each stage axis
+        // output fields per launch: 4 (fewer input re-reads) or 2 (fewer registers, more warps)
+        const bool nh2 = rowGroup2();
+        for (int P = 1; P <= 4; ++P) {
+            auto nb = [&](int st) { return (long long)tabRow[st][P].h.size(); };
+            if (pd.dim == 3 && nh2) {
+                launch::contractRowDF<31, 0, 2>(P, dPatches, tabRow[0][P].d, nb(0), cDf, sDf, dIbuf, pfDf, s);
+                launch::contractRowDF<31, 2, 2>(P, dPatches, tabRow[0][P].d, nb(0), cDf, sDf, dIbuf, pfDf, s);
+                launch::contractRowDF<31, 4, 2>(P, dPatches, tabRow[0][P].d, nb(0), cDf, sDf, dIbuf, pfDf, s);
+                launch::contractRowDF<31, 6, 2>(P, dPatches, tabRow[0][P].d, nb(0), cDf, sDf, dIbuf, pfDf, s);
+            } else if (pd.dim == 3) {
+                launch::contractRowDF<31, 0, 4>(P, dPatches, tabRow[0][P].d, nb(0), cDf, sDf, dIbuf, pfDf, s);
+                launch::contractRowDF<31, 4, 4>(P, dPatches, tabRow[0][P].d, nb(0), cDf, sDf, dIbuf, pfDf, s);
+            } else {
+                launch::contractRowDF<21, 0, 4>(P, dPatches, tabRow[0][P].d, nb(0), cDf, sDf, dIbuf, pfDf, s);
+            }
+        }
+        for (int P = 1; P <= 4; ++P) {
+            auto nb = [&](int st) { return (long long)tabRow[st][P].h.size(); };
+            if (pd.dim == 3 && nh2) {
+                launch::contractRowDF<32, 0, 2>(P, dPatches, tabRow[1][P].d, nb(1), sDf, uDf, dIbuf, pfDf, s);
+                launch::contractRowDF<32, 2, 2>(P, dPatches, tabRow[1][P].d, nb(1), sDf, uDf, dIbuf, pfDf, s);
+            } else if (pd.dim == 3) {
+                launch::contractRowDF<32, 0, 4>(P, dPatches, tabRow[1][P].d, nb(1), sDf, uDf, dIbuf, pfDf, s);
+            } else {
+                launch::contractRowDF<22, 0, 1>(P, dPatches, tabRow[1][P].d, nb(1), sDf, bandDf, dIbuf, pfDf, s);
+            }
+        }
+        if (pd.dim == 3)
+            for (int P = 1; P <= 4; ++P)
+                launch::contractRowDF<33, 0, 1>(P, dPatches, tabRow[2][P].d, (long long)tabRow[2][P].h.size(), uDf,
+                                                bandDf, dIbuf, pfDf, s);
+    } else if (pd.dim == 3) {
         launch::contract<double, 31>(dPatches, tabSt[0].d, (long long)tabSt[0].h.size(), dFieldC, dS, dIbuf, dPf, s);
         launch::contract<double, 32>(dPatches, tabSt[1].d, (long long)tabSt[1].h.size(), dS, dU, dIbuf, dPf, s);
         launch::contract<double, 33>(dPatches, tabSt[2].d, (long long)tabSt[2].h.size(), dU, dBand, dIbuf, dPf, s);
@@ -228,19 +336,36 @@ void Context::assemble(int precision) {
         launch::contract<double, 22>(dPatches, tabSt[1].d, (long long)tabSt[1].h.size(), dS, dBand, dIbuf, dPf, s);
     }
     GSGPU_CUDA_TRY(cudaEventRecord(ev[4], s));
-    // load vector
+    // load vector (FP64 contraction of the load field)
     if (pd.dim == 3) {
-        launch::loadContract<31>(dPatches, tabLd[0].d, (long long)tabLd[0].h.size(), dFieldL, dLv1, dTab, dIbuf, s);
-        launch::loadContract<32>(dPatches, tabLd[1].d, (long long)tabLd[1].h.size(), dLv1, dLv2, dTab, dIbuf, s);
-        launch::loadContract<33>(dPatches, tabLd[2].d, (long long)tabLd[2].h.size(), dLv2, dLvec, dTab, dIbuf, s);
+        if (mixed)
+            launch::loadContract<31, df32>(dPatches, tabLd[0].d, (long long)tabLd[0].h.size(), lDf, dLv1, dTab, dIbuf, s);
+        else
+            launch::loadContract<31, double>(dPatches, tabLd[0].d, (long long)tabLd[0].h.size(), dFieldL, dLv1, dTab, dIbuf, s);
+        launch::loadContract<32, double>(dPatches, tabLd[1].d, (long long)tabLd[1].h.size(), dLv1, dLv2, dTab, dIbuf, s);
+        launch::loadContract<33, double>(dPatches, tabLd[2].d, (long long)tabLd[2].h.size(), dLv2, dLvec, dTab, dIbuf, s);
     } else {
-        launch::loadContract<21>(dPatches, tabLd[0].d, (long long)tabLd[0].h.size(), dFieldL, dLv1, dTab, dIbuf, s);
-        launch::loadContract<22>(dPatches, tabLd[1].d, (long long)tabLd[1].h.size(), dLv1, dLvec, dTab, dIbuf, s);
+        if (mixed)
+            launch::loadContract<21, df32>(dPatches, tabLd[0].d, (long long)tabLd[0].h.size(), lDf, dLv1, dTab, dIbuf, s);
+        else
+            launch::loadContract<21, double>(dPatches, tabLd[0].d, (long long)tabLd[0].h.size(), dFieldL, dLv1, dTab, dIbuf, s);
+        launch::loadContract<22, double>(dPatches, tabLd[1].d, (long long)tabLd[1].h.size(), dLv1, dLvec, dTab, dIbuf, s);
     }
     GSGPU_CUDA_TRY(cudaEventRecord(ev[5], s));
     // K4: CSR values (segmented gather) and rhs with the Dirichlet lift
-    launch::gatherCsr<double>((long long)pat.col.size(), dSrc, dBand, dOvfPtr, dOvfIdx, dVal, s);
-    launch::rhsRows(pat.n, dLvec, dLptr, dLidx, dBand, dFptr, dFband, dFbidx, dDdof, dRhs, s);
+    dir.th.join();
+    if (dir.err) std::rethrow_exception(dir.err);
+    ddof.swap(ddofNew);
+    hostDirichletMs = dirMs;
+    if (!ddof.empty())
+        GSGPU_CUDA_TRY(cudaMemcpyAsync(dDdof, ddof.data(), ddof.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (mixed) {
+        launch::gatherCsrDF((long long)pat.col.size(), dSrc, bandDf, dOvfPtr, dOvfIdx, dValHi, dValLo, s);
+        launch::rhsRows<df32>(pat.n, dLvec, dLptr, dLidx, bandDf, dFptr, dFband, dFbidx, dDdof, dRhs, s);
+    } else {
+        launch::gatherCsr<double>((long long)pat.col.size(), dSrc, dBand, dOvfPtr, dOvfIdx, dVal, s);
+        launch::rhsRows<double>(pat.n, dLvec, dLptr, dLidx, dBand, dFptr, dFband, dFbidx, dDdof, dRhs, s);
+    }
     GSGPU_CUDA_TRY(cudaEventRecord(ev[6], s));
     GSGPU_CUDA_TRY(cudaGetLastError());
     GSGPU_CUDA_TRY(cudaEventSynchronize(ev[6]));
@@ -264,7 +389,14 @@ void Context::times(double* ms) {
     ms[6] = tot;
 }
 
+void Context::dropGraphs() {
+    if (gexecFp64) cudaGraphExecDestroy(gexecFp64);
+    if (gexecMixed) cudaGraphExecDestroy(gexecMixed);
+    gexecFp64 = gexecMixed = nullptr;
+}
+
 void Context::freeAssembly() {
+    dropGraphs();
     arena.releaseAll();
     *this = Context::reset(std::move(*this));
 }
@@ -286,6 +418,7 @@ Context Context::reset(Context&& c) {
 void Context::ensureSolveBuffers() {
     const int n = pat.n;
     if (solveN == n && dX) return;
+    dropGraphs();
     for (double** b : {&dX, &dR, &dZ, &dP, &dT, &dDinv, &dPart0, &dPart1, &dPart2}) arena.release(*b), *b = nullptr;
     arena.release(dCg);
     dCg = nullptr;
@@ -303,10 +436,22 @@ void Context::ensureSolveBuffers() {
     solveN = n;
 }
 
-int Context::lanesPerRow() const {
+// df32 contraction output-group width (tuning override GSGPU_ROW_NH=2|4; measured default below)
+bool Context::rowGroup2() const {
+    if (const char* e = std::getenv("GSGPU_ROW_NH")) return std::atoi(e) == 2;
+    return false;
+}
+
+// lanes per CSR row of the SpMV kernels: long rows use 16 lanes for FP32 values (the load rate
+// limits) and 8 for FP64 values (fewer FP64 shuffle-adds: the FP64 pipe limits); measured on GB300
+int Context::lanesPerRow(bool fp64) const {
+    if (const char* e = std::getenv("GSGPU_LANES_PER_ROW")) {  // tuning override: 4, 8, 16 or 32
+        const int v = std::atoi(e);
+        if (v == 4 || v == 8 || v == 16 || v == 32) return v;
+    }
     const double avg = pat.n ? double(pat.col.size()) / pat.n : 1.0;
-    if (avg > 48) return 32;
-    if (avg > 20) return 16;
+    if (avg > 48) return fp64 ? 8 : 16;
+    if (avg > 20) return fp64 ? 8 : 16;
     if (avg > 10) return 8;
     return 4;
 }
@@ -314,7 +459,13 @@ int Context::lanesPerRow() const {
 void Context::solve(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
     if (!assembled) throw StateError("solve() before assemble()");
     if (o.method != GSGPU_SOLVER_CG_JACOBI) throw std::invalid_argument("solver method not available in this build");
-    if (o.precision != GSGPU_PREC_FP64) throw std::invalid_argument("precision mode not available in this build");
+    if (o.precision == GSGPU_PREC_MIXED) {
+        if (assembledPrecision != kMixed) throw StateError("mixed-precision solve needs assemble(GSGPU_PREC_MIXED)");
+        solveMixed(o, info);
+        return;
+    }
+    if (o.precision != GSGPU_PREC_FP64) throw std::invalid_argument("unknown precision mode");
+    if (assembledPrecision != kFP64) throw StateError("FP64 solve needs assemble(GSGPU_PREC_FP64)");
     ensureSolveBuffers();
     cudaStream_t s = stream;
     cudaEvent_t e0, e1;
@@ -324,9 +475,10 @@ void Context::solve(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
     launch::jacobiDiag(pat.n, dDiag, dVal, 1.0, dDinv, s);
     CgBuffers B;
     B.n = pat.n;
-    B.lanes_per_row = lanesPerRow();
+    B.lanes_per_row = lanesPerRow(true);
     B.ptr = dPtr;
     B.col = dCol;
+    B.coff = dColOff;
     B.val = dVal;
     B.b = dRhs;
     B.dinv = dDinv;
@@ -337,7 +489,7 @@ void Context::solve(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
     const int maxit = o.max_iters > 0 ? o.max_iters : 1000;
     launch::cgInit(B, tol, maxit, s);
     CgState hs{};
-    spmvBytes = double(pat.col.size()) * (8 + 4) + double(pat.n + 1) * 4 + 2.0 * pat.n * 8;
+    spmvBytes = double(pat.col.size()) * (8 + (dColOff ? 2 : 4)) + double(pat.n + 1) * 4 + 2.0 * pat.n * 8;
     if (profiling) {
         // one iteration at a time, every SpMV bracketed by events (no graph)
         cudaEvent_t a, b;
@@ -360,24 +512,27 @@ void Context::solve(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
         cudaEventDestroy(a);
         cudaEventDestroy(b);
     } else {
-        // iterations in chunks captured as a CUDA graph; kernels become no-ops once converged
+        // iterations in chunks captured as a CUDA graph (once per context); kernels become no-ops
+        // once converged
         const int chunk = 16;
-        cudaGraphExec_t exec = nullptr;
-        {
+        if (!gexecFp64 || gexecLpr[0] != B.lanes_per_row) {
+            if (gexecFp64) cudaGraphExecDestroy(gexecFp64);
+            gexecFp64 = nullptr;
             cudaGraph_t g;
             GSGPU_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
             for (int k = 0; k < chunk; ++k) launch::cgIteration(B, s);
             GSGPU_CUDA_TRY(cudaStreamEndCapture(s, &g));
-            GSGPU_CUDA_TRY(cudaGraphInstantiate(&exec, g, 0));
+            GSGPU_CUDA_TRY(cudaGraphInstantiate(&gexecFp64, g, 0));
             cudaGraphDestroy(g);
+            gexecLpr[0] = B.lanes_per_row;
         }
+        cudaGraphExec_t exec = gexecFp64;
         for (int done_it = 0; done_it < maxit + chunk; done_it += chunk) {
             GSGPU_CUDA_TRY(cudaGraphLaunch(exec, s));
             GSGPU_CUDA_TRY(cudaMemcpyAsync(&hs, dCg, sizeof(CgState), cudaMemcpyDeviceToHost, s));
             GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
             if (hs.done) break;
         }
-        cudaGraphExecDestroy(exec);
     }
     GSGPU_CUDA_TRY(cudaEventRecord(e1, s));
     GSGPU_CUDA_TRY(cudaEventSynchronize(e1));
@@ -388,6 +543,115 @@ void Context::solve(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
     info.iterations = hs.iters;
     info.relres = hs.relres;
     info.refinements = 0;
+    info.t_solve_ms = ms;
+    solved = true;
+    lastConverged = hs.done == 1;
+}
+
+void Context::ensureMixedBuffers() {
+    if (dValHi) return;
+    dropGraphs();
+    const long long nnz = (long long)pat.col.size();
+    const int n = pat.n;
+    allocN(arena, dCoefsDf, L.coefs);
+    allocN(arena, dValHi, nnz);
+    allocN(arena, dValLo, nnz);
+    allocN(arena, dDinv32, n);
+    allocN(arena, dR32, n);
+    allocN(arena, dZ32, n);
+    allocN(arena, dP32, n);
+    allocN(arena, dT32, n);
+    allocN(arena, dDx32, n);
+    allocN(arena, dXhi, n);
+    allocN(arena, dXlo, n);
+}
+
+void Context::solveMixed(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
+    ensureSolveBuffers();
+    ensureMixedBuffers();
+    cudaStream_t s = stream;
+    cudaEvent_t e0, e1;
+    GSGPU_CUDA_TRY(cudaEventCreate(&e0));
+    GSGPU_CUDA_TRY(cudaEventCreate(&e1));
+    GSGPU_CUDA_TRY(cudaEventRecord(e0, s));
+    launch::jacobiDiag32(pat.n, dDiag, dValHi, dDinv32, s);
+    CgBuffers B;
+    B.n = pat.n;
+    B.lanes_per_row = lanesPerRow(false);
+    B.ptr = dPtr;
+    B.col = dCol;
+    B.coff = dColOff;
+    B.b = dRhs;
+    B.x = dX;
+    B.r = dR;
+    B.part0 = dPart0; B.part1 = dPart1; B.part2 = dPart2;
+    B.st = dCg;
+    B.val_hi = dValHi; B.val_lo = dValLo; B.dinv32 = dDinv32;
+    B.r32 = dR32; B.z32 = dZ32; B.p32 = dP32; B.t32 = dT32; B.dx32 = dDx32; B.xhi = dXhi; B.xlo = dXlo;
+    const double tol = o.tol > 0 ? o.tol : 1e-10;
+    const int maxit = o.max_iters > 0 ? o.max_iters : 1000;
+    launch::mixedInit(B, tol, maxit, s);
+    CgState hs{};
+    spmvBytes = double(pat.col.size()) * (4 + (dColOff ? 2 : 4)) + double(pat.n + 1) * 4 + 2.0 * pat.n * 4;
+    const int chunk = 16;
+    if (profiling) {
+        cudaEvent_t a, b;
+        GSGPU_CUDA_TRY(cudaEventCreate(&a));
+        GSGPU_CUDA_TRY(cudaEventCreate(&b));
+        for (int c = 0; c < maxit / chunk + 2; ++c) {
+            for (int k = 0; k < chunk; ++k) {
+                GSGPU_CUDA_TRY(cudaMemcpyAsync(&hs, dCg, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+                GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
+                if (hs.done || hs.pause) break;
+                GSGPU_CUDA_TRY(cudaEventRecord(a, s));
+                launch::mixedSpmv(B, s);
+                GSGPU_CUDA_TRY(cudaEventRecord(b, s));
+                launch::mixedRest(B, s);
+                GSGPU_CUDA_TRY(cudaEventSynchronize(b));
+                float m = 0;
+                GSGPU_CUDA_TRY(cudaEventElapsedTime(&m, a, b));
+                spmvMs += m;
+                ++spmvLaunches;
+            }
+            launch::mixedReplace(B, s);
+            GSGPU_CUDA_TRY(cudaMemcpyAsync(&hs, dCg, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+            GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
+            if (hs.done) break;
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    } else {
+        // chunks of FP32 iterations followed by one residual replacement, captured as a graph
+        // (once per context)
+        if (!gexecMixed || gexecLpr[1] != B.lanes_per_row) {
+            if (gexecMixed) cudaGraphExecDestroy(gexecMixed);
+            gexecMixed = nullptr;
+            cudaGraph_t g;
+            GSGPU_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            for (int k = 0; k < chunk; ++k) launch::mixedIteration(B, s);
+            launch::mixedReplace(B, s);
+            GSGPU_CUDA_TRY(cudaStreamEndCapture(s, &g));
+            GSGPU_CUDA_TRY(cudaGraphInstantiate(&gexecMixed, g, 0));
+            cudaGraphDestroy(g);
+            gexecLpr[1] = B.lanes_per_row;
+        }
+        cudaGraphExec_t exec = gexecMixed;
+        for (int c = 0; c < maxit / chunk + 2; ++c) {
+            GSGPU_CUDA_TRY(cudaGraphLaunch(exec, s));
+            GSGPU_CUDA_TRY(cudaMemcpyAsync(&hs, dCg, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+            GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
+            if (hs.done) break;
+        }
+    }
+    GSGPU_CUDA_TRY(cudaEventRecord(e1, s));
+    GSGPU_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    info.iterations = hs.iters;
+    info.relres = hs.relres;
+    info.refinements = hs.replacements;
     info.t_solve_ms = ms;
     solved = true;
     lastConverged = hs.done == 1;
@@ -466,6 +730,7 @@ int gsgpu_destroy(gsgpu_context* ctx) {
     }
     cudaSetDevice(ctx->c.device);
     if (ctx->c.stream) cudaStreamSynchronize(ctx->c.stream);
+    ctx->c.dropGraphs();
     ctx->c.arena.releaseAll();
     for (int i = 0; i < 8; ++i)
         if (ctx->c.ev[i]) cudaEventDestroy(ctx->c.ev[i]);
@@ -480,7 +745,10 @@ int gsgpu_set_problem(gsgpu_context* ctx, const gsgpu_problem* prob) {
     return guarded(ctx, [&] {
         gsgpu::ProblemDesc pd;
         gsgpu::problemFromC(prob, pd);
-        if (ctx->c.device >= 0) ctx->c.arena.releaseAll();
+        if (ctx->c.device >= 0) {
+            ctx->c.dropGraphs();
+            ctx->c.arena.releaseAll();
+        }
         ctx->c = gsgpu::Context::reset(std::move(ctx->c));
         ctx->c.pd = std::move(pd);
         ctx->c.hasProblem = true;
@@ -517,7 +785,13 @@ int gsgpu_matrix_csr(gsgpu_context* ctx, int* ptr, int* col, double* val) {
         if (val && !c.assembled) throw gsgpu::StateError("matrix() values before assemble()");
         if (ptr) std::copy(c.pat.ptr.begin(), c.pat.ptr.end(), ptr);
         if (col) std::copy(c.pat.col.begin(), c.pat.col.end(), col);
-        if (val) {
+        if (val && c.assembledPrecision == gsgpu::kMixed) {  // the df32 operator as FP64 values hi + lo
+            std::vector<float> hi(c.pat.col.size()), lo(c.pat.col.size());
+            GSGPU_CUDA_TRY(cudaMemcpyAsync(hi.data(), c.dValHi, hi.size() * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+            GSGPU_CUDA_TRY(cudaMemcpyAsync(lo.data(), c.dValLo, lo.size() * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+            GSGPU_CUDA_TRY(cudaStreamSynchronize(c.stream));
+            for (size_t k = 0; k < hi.size(); ++k) val[k] = double(hi[k]) + double(lo[k]);
+        } else if (val) {
             GSGPU_CUDA_TRY(cudaMemcpyAsync(val, c.dVal, c.pat.col.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
             GSGPU_CUDA_TRY(cudaStreamSynchronize(c.stream));
         }

@@ -10,6 +10,7 @@
 
 #include "../../include/gsgpu.h"
 #include "gsgpu_internal.h"
+#include "device_funcs.cuh"
 #include "kernels_solve.h"
 #include "plan.h"
 
@@ -66,7 +67,8 @@ struct Context {
 
     // device buffers (assembly)
     DevPatch* dPatches = nullptr;
-    FieldParams* dFields = nullptr;
+    dev::FieldConst<double>* dFields = nullptr;
+    dev::FieldConst<df32>* dFieldsDf = nullptr;
     double *dKnots = nullptr, *dGknots = nullptr, *dTab = nullptr, *dGtab = nullptr, *dPf = nullptr, *dWq = nullptr;
     TabJob *dTabJobs = nullptr, *dGtabJobs = nullptr;
     PfJob* dPfJobs = nullptr;
@@ -75,17 +77,28 @@ struct Context {
            *dY2 = nullptr, *dS = nullptr, *dU = nullptr, *dBand = nullptr, *dLv1 = nullptr, *dLv2 = nullptr,
            *dLvec = nullptr;
     int *dPtr = nullptr, *dCol = nullptr, *dDiag = nullptr;
+    int16_t* dColOff = nullptr;  // column - row, when every offset fits in 16 bits
     uint32_t *dSrc = nullptr, *dOvfPtr = nullptr, *dOvfIdx = nullptr, *dLptr = nullptr, *dLidx = nullptr,
              *dFptr = nullptr, *dFband = nullptr, *dFbidx = nullptr;
     double *dVal = nullptr, *dRhs = nullptr, *dDdof = nullptr;
     unsigned long long* dDetKey = nullptr;
+    // mixed precision: df32 copies of the small inputs, the split CSR values and FP32 vectors
+    df32 *dCoefsDf = nullptr, *dWqDf = nullptr;
+    float *dValHi = nullptr, *dValLo = nullptr, *dDinv32 = nullptr;
+    float *dR32 = nullptr, *dZ32 = nullptr, *dP32 = nullptr, *dT32 = nullptr, *dDx32 = nullptr, *dXhi = nullptr,
+          *dXlo = nullptr;
     Tab tabPf, tabCoef, tabGeo1, tabGeo2, tabPoint, tabSt[3], tabLd[3];
+    Tab tabRow[3][5];  // [stage][degree along the stage axis]
 
     // device buffers (solve)
     int solveN = -1;
     double *dX = nullptr, *dR = nullptr, *dZ = nullptr, *dP = nullptr, *dT = nullptr, *dDinv = nullptr;
     double *dPart0 = nullptr, *dPart1 = nullptr, *dPart2 = nullptr;
     CgState* dCg = nullptr;
+    // instantiated solver graphs (16 iterations [+ replacement]); valid while the buffers live
+    cudaGraphExec_t gexecFp64 = nullptr, gexecMixed = nullptr;
+    int gexecLpr[2] = {0, 0};
+    void dropGraphs();
     // profiling of the solver's SpMV launches
     bool profiling = false;
     long long spmvLaunches = 0;
@@ -99,7 +112,10 @@ struct Context {
     void freeAssembly();
     void buildTables();
     void ensureSolveBuffers();
-    int lanesPerRow() const;
+    void ensureMixedBuffers();
+    void solveMixed(const gsgpu_solver_opts& o, gsgpu_solve_info& info);
+    int lanesPerRow(bool fp64) const;
+    bool rowGroup2() const;
     static Context reset(Context&& c);
 };
 

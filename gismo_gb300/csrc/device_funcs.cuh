@@ -4,6 +4,7 @@
 
 #include <cmath>
 
+#include "df32.cuh"
 #include "gsgpu_internal.h"
 
 #ifdef __CUDACC__
@@ -68,15 +69,82 @@ GS_HD T pairFactor(const double* __restrict__ tab, int p, int q, int E, long lon
 }
 
 // -------------------------------------------------------------------------------------------
+// real-type traits: the geometry / field code below is written once for FP64 (plain path) and
+// for df32 (mixed path: FP64-grade accuracy on the FP32 pipe)
+template <typename R>
+struct Real;
+template <>
+struct Real<double> {
+    GS_HD static double zero() { return 0.0; }
+    GS_HD static double abs(double v) { return fabs(v); }
+    GS_HD static double toD(double v) { return v; }
+    GS_HD static double exp(double v) {
+#ifdef __CUDA_ARCH__
+        return ::exp(v);
+#else
+        return std::exp(v);
+#endif
+    }
+    GS_HD static void sincospi(double x, double* s, double* c) {
+#ifdef __CUDA_ARCH__
+        ::sincospi(x, s, c);
+#else
+        *s = std::sin(M_PI * x);
+        *c = std::cos(M_PI * x);
+#endif
+    }
+    GS_HD static double mulInt(double a, int k) { return a * k; }
+};
+template <>
+struct Real<df32> {
+    GS_HD static df32 zero() { return df32(); }
+    GS_HD static df32 abs(df32 v) { return dfabs(v); }
+    GS_HD static double toD(df32 v) { return v.toDouble(); }
+    GS_HD static df32 exp(df32 v) { return expDf(v); }
+    GS_HD static void sincospi(df32 x, df32* s, df32* c) { sincospiDf(x, *s, *c); }
+    GS_HD static df32 mulInt(df32 a, int k) { return a * float(k); }
+};
+
+// the closed-form field constants in the arithmetic of R (built on the host)
+template <typename R>
+struct FieldConst {
+    int dim, fourier, nmodes, ufreq, kmax, pad;
+    R kconst, alpha, scale, wpi, pi;  // wpi = ufreq * pi
+    R amp[kMaxModes], cph[kMaxModes], sph[kMaxModes];
+    int kk[kMaxModes][3];
+};
+template <typename R>
+inline FieldConst<R> fieldConst(const FieldParams& F) {
+    FieldConst<R> c{};
+    c.dim = F.dim;
+    c.fourier = F.fourier;
+    c.nmodes = F.nmodes;
+    c.ufreq = F.ufreq;
+    c.kmax = F.kmax;
+    c.kconst = R(F.kconst);
+    c.alpha = R(F.alpha);
+    c.scale = R(F.scale);
+    c.wpi = R(F.ufreq * M_PI);
+    c.pi = R(M_PI);
+    for (int m = 0; m < kMaxModes; ++m) {
+        c.amp[m] = R(F.amp[m]);
+        c.cph[m] = R(F.cph[m]);
+        c.sph[m] = R(F.sph[m]);
+        for (int k = 0; k < 3; ++k) c.kk[m][k] = F.kk[m][k];
+    }
+    return c;
+}
+
+// -------------------------------------------------------------------------------------------
 // geometry map, sum-factorised over the control net: stage 1 (direction 0)
 // 3D: Y1[m][tau][i2][i1][g0] ; 2D: Y1[m][tau][i1][g0]  (tau: 0 value, 1 derivative)
-GS_HD double geoStage1(const DevPatch& D, long long item, const double* __restrict__ coefs,
-                       const double* __restrict__ gtab, const int* __restrict__ ibuf) {
+template <typename R>
+GS_HD R geoStage1(const DevPatch& D, long long item, const R* __restrict__ coefs, const R* __restrict__ gtab,
+                  const int* __restrict__ ibuf) {
     const int Q0 = D.Q[0];
     const int g0 = int(item % Q0);
     long long r = item / Q0;
     long long rest;  // (i2*gn1 + i1) or i1
-    int tau, m;
     if (D.dim == 3) {
         const long long plane = (long long)D.gn[2] * D.gn[1];
         rest = r % plane;
@@ -85,20 +153,21 @@ GS_HD double geoStage1(const DevPatch& D, long long item, const double* __restri
         rest = r % D.gn[1];
         r /= D.gn[1];
     }
-    tau = int(r % 2);
-    m = int(r / 2);
+    const int tau = int(r % 2);
+    const int m = int(r / 2);
     const int gp = D.gp[0];
     const int f0 = ibuf[D.gqoff[0] + g0];
-    const double* tb = gtab + D.gtoff[0] + (long long)g0 * 2 * (gp + 1) + tau * (gp + 1);
-    const double* c = coefs + D.coef_off + m * D.ngeo + rest * D.gn[0] + f0;
-    double acc = 0.0;
+    const R* tb = gtab + D.gtoff[0] + (long long)g0 * 2 * (gp + 1) + tau * (gp + 1);
+    const R* c = coefs + D.coef_off + m * D.ngeo + rest * D.gn[0] + f0;
+    R acc = Real<R>::zero();
     for (int s = 0; s <= gp; ++s) acc += tb[s] * c[s];
     return acc;
 }
 
 // 3D stage 2 (direction 1): Y2[m][tau][i2][g1][g0], tau: 0 vv, 1 dv (d/dxi0), 2 vd (d/dxi1)
-GS_HD double geoStage2(const DevPatch& D, long long item, const double* __restrict__ Y1,
-                       const double* __restrict__ gtab, const int* __restrict__ ibuf) {
+template <typename R>
+GS_HD R geoStage2(const DevPatch& D, long long item, const R* __restrict__ Y1, const R* __restrict__ gtab,
+                  const int* __restrict__ ibuf) {
     const int Q0 = D.Q[0], Q1 = D.Q[1];
     const int g0 = int(item % Q0);
     long long r = item / Q0;
@@ -112,9 +181,9 @@ GS_HD double geoStage2(const DevPatch& D, long long item, const double* __restri
     const int t2 = (tau == 2) ? 1 : 0;  // derivative in direction 1
     const int gp = D.gp[1];
     const int f1 = ibuf[D.gqoff[1] + g1];
-    const double* tb = gtab + D.gtoff[1] + (long long)g1 * 2 * (gp + 1) + t2 * (gp + 1);
-    const double* y = Y1 + D.y1_off + ((((long long)m * 2 + t1) * D.gn[2] + i2) * D.gn[1] + f1) * Q0 + g0;
-    double acc = 0.0;
+    const R* tb = gtab + D.gtoff[1] + (long long)g1 * 2 * (gp + 1) + t2 * (gp + 1);
+    const R* y = Y1 + D.y1_off + ((((long long)m * 2 + t1) * D.gn[2] + i2) * D.gn[1] + f1) * Q0 + g0;
+    R acc = Real<R>::zero();
     for (int s = 0; s <= gp; ++s) acc += tb[s] * y[(long long)s * Q0];
     return acc;
 }
@@ -122,93 +191,89 @@ GS_HD double geoStage2(const DevPatch& D, long long item, const double* __restri
 // closed-form fields at a physical point: kappa and f = -div(kappa grad u)
 // (g = scale sum_m amp_m cos(pi k_m.x + phase_m), kappa = exp(alpha g), u = prod sin(freq pi x_i)).
 // cos/sin of the mode phases use e^{i theta} = e^{i phase} prod_i (e^{i pi x_i})^{k_i}.
-struct Complex {
-    double re, im;
+template <typename R>
+struct Cplx {
+    R re, im;
 };
-GS_HD Complex cmul(Complex a, Complex b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
-
-GS_HD void sincospiD(double x, double* s, double* c) {
-#ifdef __CUDA_ARCH__
-    sincospi(x, s, c);
-#else
-    *s = std::sin(M_PI * x);
-    *c = std::cos(M_PI * x);
-#endif
+template <typename R>
+GS_HD Cplx<R> cmul(const Cplx<R>& a, const Cplx<R>& b) {
+    return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
 }
 
-GS_HD void fields(const FieldParams& F, const double* x, double& kappa, double& f) {
+template <typename R>
+GS_HD void fields(const FieldConst<R>& F, const R* x, R& kappa, R& f) {
     const int d = F.dim;
-    const double w = F.ufreq * M_PI;
-    double sn[3], cs[3];
-    for (int i = 0; i < d; ++i) sincospiD(F.ufreq * x[i], &sn[i], &cs[i]);
-    double u = 1.0;
-    for (int i = 0; i < d; ++i) u *= sn[i];
-    double gu[3];
+    R sn[3], cs[3];
+    for (int i = 0; i < d; ++i) Real<R>::sincospi(Real<R>::mulInt(x[i], F.ufreq), &sn[i], &cs[i]);
+    R u = sn[0];
+    for (int i = 1; i < d; ++i) u = u * sn[i];
+    R gu[3];
     for (int j = 0; j < d; ++j) {
-        double t = w * cs[j];
+        R t = F.wpi * cs[j];
         for (int i = 0; i < d; ++i)
-            if (i != j) t *= sn[i];
+            if (i != j) t = t * sn[i];
         gu[j] = t;
     }
+    const R lap = Real<R>::mulInt(F.wpi * F.wpi * u, d);  // -Laplace(u) = d (freq pi)^2 u
     if (!F.fourier) {
         kappa = F.kconst;
-        f = kappa * (d * w * w * u);
+        f = kappa * lap;
         return;
     }
-    Complex zp[3][kMaxKappaWave + 1];
+    Cplx<R> zp[3][kMaxKappaWave + 1];
     for (int i = 0; i < d; ++i) {
-        double s, c;
-        sincospiD(x[i], &s, &c);
-        zp[i][0] = {1.0, 0.0};
-        const Complex z{c, s};
+        R s, c;
+        if (F.ufreq == 1) { s = sn[i]; c = cs[i]; }
+        else Real<R>::sincospi(x[i], &s, &c);
+        zp[i][0].re = Real<R>::zero();
+        zp[i][0].re += R(1);
+        zp[i][0].im = Real<R>::zero();
+        const Cplx<R> z{c, s};
         for (int k = 1; k <= F.kmax; ++k) zp[i][k] = cmul(zp[i][k - 1], z);
     }
-    double g = 0.0, gg[3] = {0.0, 0.0, 0.0};
+    R g = Real<R>::zero(), gg[3] = {Real<R>::zero(), Real<R>::zero(), Real<R>::zero()};
     for (int m = 0; m < F.nmodes; ++m) {
-        Complex e{F.cph[m], F.sph[m]};
+        Cplx<R> e{F.cph[m], F.sph[m]};
         for (int i = 0; i < d; ++i) e = cmul(e, zp[i][F.kk[m][i]]);
         g += F.amp[m] * e.re;
-        const double as = F.amp[m] * e.im * M_PI;
-        for (int i = 0; i < d; ++i) gg[i] -= as * F.kk[m][i];
+        const R as = F.amp[m] * e.im;
+        for (int i = 0; i < d; ++i) gg[i] -= Real<R>::mulInt(as, F.kk[m][i]);
     }
-    g *= F.scale;
-    double dot = 0.0;
+    g = g * F.scale;
+    R dot = Real<R>::zero();
     for (int i = 0; i < d; ++i) dot += gg[i] * gu[i];
-    dot *= F.scale;
-#ifdef __CUDA_ARCH__
-    kappa = exp(F.alpha * g);
-#else
-    kappa = std::exp(F.alpha * g);
-#endif
-    f = kappa * (d * w * w * u - F.alpha * dot);
+    dot = dot * F.scale * F.pi;
+    kappa = Real<R>::exp(F.alpha * g);
+    f = kappa * (lap - F.alpha * dot);
 }
 
 // point-wise step: last geometry stage, metric and coefficient fields.
 // C^{ab} = w kappa |det J| (J^-1 J^-T)_{ab} = w kappa / |det J| sum_m cof_{ma} cof_{mb},
 // L = w |det J| f.  Component order 3D: 00 01 02 11 12 22 ; 2D: 00 01 11.
 // Returns det J.
-GS_HD double pointStep(const DevPatch& D, const FieldParams& F, long long item, const double* __restrict__ Y1,
-                       const double* __restrict__ Y2, const double* __restrict__ gtab, const int* __restrict__ ibuf,
-                       const double* __restrict__ wq, double* __restrict__ C, double* __restrict__ Lf) {
+template <typename R>
+GS_HD double pointStep(const DevPatch& D, const FieldConst<R>& F, long long item, const R* __restrict__ Y1,
+                       const R* __restrict__ Y2, const R* __restrict__ gtab, const int* __restrict__ ibuf,
+                       const R* __restrict__ wq, R* __restrict__ C, R* __restrict__ Lf) {
     const int d = D.dim;
     const int Q0 = D.Q[0], Q1 = D.Q[1];
     const int g0 = int(item % Q0);
     long long r = item / Q0;
     const int g1 = int(r % Q1);
     const int g2 = int(r / Q1);
-    double x[3], J[3][3];
+    R x[3], J[3][3];
     if (d == 3) {
         const int gp = D.gp[2];
         const int f2 = ibuf[D.gqoff[2] + g2];
-        const double* tb = gtab + D.gtoff[2] + (long long)g2 * 2 * (gp + 1);
+        const R* tb = gtab + D.gtoff[2] + (long long)g2 * 2 * (gp + 1);
         const long long plane = (long long)Q1 * Q0;
         for (int m = 0; m < 3; ++m) {
-            const double* yvv = Y2 + D.y2_off + (((long long)m * 3 + 0) * D.gn[2] + f2) * plane + (long long)g1 * Q0 + g0;
-            const double* ydv = yvv + (long long)D.gn[2] * plane;
-            const double* yvd = ydv + (long long)D.gn[2] * plane;
-            double a = 0, b = 0, c = 0, e = 0;
+            const R* yvv = Y2 + D.y2_off + (((long long)m * 3 + 0) * D.gn[2] + f2) * plane + (long long)g1 * Q0 + g0;
+            const R* ydv = yvv + (long long)D.gn[2] * plane;
+            const R* yvd = ydv + (long long)D.gn[2] * plane;
+            R a = Real<R>::zero(), b = Real<R>::zero(), c = Real<R>::zero(), e = Real<R>::zero();
             for (int s = 0; s <= gp; ++s) {
-                const double v = tb[s], dv = tb[gp + 1 + s];
+                const R v = tb[s], dv = tb[gp + 1 + s];
                 const long long o = (long long)s * plane;
                 a += v * yvv[o];
                 b += v * ydv[o];
@@ -223,13 +288,13 @@ GS_HD double pointStep(const DevPatch& D, const FieldParams& F, long long item, 
     } else {
         const int gp = D.gp[1];
         const int f1 = ibuf[D.gqoff[1] + g1];
-        const double* tb = gtab + D.gtoff[1] + (long long)g1 * 2 * (gp + 1);
+        const R* tb = gtab + D.gtoff[1] + (long long)g1 * 2 * (gp + 1);
         for (int m = 0; m < 2; ++m) {
-            const double* yv = Y1 + D.y1_off + (((long long)m * 2 + 0) * D.gn[1] + f1) * Q0 + g0;
-            const double* yd = yv + (long long)D.gn[1] * Q0;
-            double a = 0, b = 0, c = 0;
+            const R* yv = Y1 + D.y1_off + (((long long)m * 2 + 0) * D.gn[1] + f1) * Q0 + g0;
+            const R* yd = yv + (long long)D.gn[1] * Q0;
+            R a = Real<R>::zero(), b = Real<R>::zero(), c = Real<R>::zero();
             for (int s = 0; s <= gp; ++s) {
-                const double v = tb[s], dv = tb[gp + 1 + s];
+                const R v = tb[s], dv = tb[gp + 1 + s];
                 const long long o = (long long)s * Q0;
                 a += v * yv[o];
                 b += v * yd[o];
@@ -240,14 +305,14 @@ GS_HD double pointStep(const DevPatch& D, const FieldParams& F, long long item, 
             J[m][1] = c;
         }
     }
-    double w = wq[D.qoff[0] + g0] * wq[D.qoff[1] + g1];
-    if (d == 3) w *= wq[D.qoff[2] + g2];
-    double kappa, f;
+    R w = wq[D.qoff[0] + g0] * wq[D.qoff[1] + g1];
+    if (d == 3) w = w * wq[D.qoff[2] + g2];
+    R kappa, f;
     fields(F, x, kappa, f);
     const long long nq = D.nq;
-    double det;
+    R det;
     if (d == 3) {
-        double cof[3][3];
+        R cof[3][3];
         cof[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
         cof[0][1] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
         cof[0][2] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
@@ -258,8 +323,8 @@ GS_HD double pointStep(const DevPatch& D, const FieldParams& F, long long item, 
         cof[2][1] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
         cof[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
         det = J[0][0] * cof[0][0] + J[0][1] * cof[0][1] + J[0][2] * cof[0][2];
-        const double sc = w * kappa / fabs(det);
-        double* c = C + D.field_off + item;
+        const R sc = w * kappa / Real<R>::abs(det);
+        R* c = C + D.field_off + item;
         int k = 0;
         for (int a = 0; a < 3; ++a)
             for (int b = a; b < 3; ++b, ++k)
@@ -267,15 +332,15 @@ GS_HD double pointStep(const DevPatch& D, const FieldParams& F, long long item, 
     } else {
         det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
         // cof = [[J11, -J10], [-J01, J00]]
-        const double c00 = J[1][1], c01 = -J[1][0], c10 = -J[0][1], c11 = J[0][0];
-        const double sc = w * kappa / fabs(det);
-        double* c = C + D.field_off + item;
+        const R c00 = J[1][1], c01 = -J[1][0], c10 = -J[0][1], c11 = J[0][0];
+        const R sc = w * kappa / Real<R>::abs(det);
+        R* c = C + D.field_off + item;
         c[0] = sc * (c00 * c00 + c10 * c10);
         c[nq] = sc * (c00 * c01 + c10 * c11);
         c[2 * nq] = sc * (c01 * c01 + c11 * c11);
     }
-    Lf[D.lfield_off + item] = w * fabs(det) * f;
-    return det;
+    Lf[D.lfield_off + item] = w * Real<R>::abs(det) * f;
+    return Real<R>::toD(det);
 }
 
 // -------------------------------------------------------------------------------------------
@@ -422,6 +487,147 @@ GS_HD void contractItem(const DevPatch& D, long long item, const T* __restrict__
     for (int h = 0; h < S::NOUT; ++h) op[h * G.out_fs] = acc[h];
 }
 
+// the same contraction in df32 with compensated (Dot2) accumulation: each output keeps an FP32
+// running sum plus an error term, so the band comes out with FP64-grade accuracy
+template <int KIND>
+GS_HD void contractItemDF(const DevPatch& D, long long item, const df32* __restrict__ in, df32* __restrict__ out,
+                          const int* __restrict__ ibuf, const df32* __restrict__ pf) {
+    using S = Stage<KIND>;
+    const int ax = S::AX;
+    const StageGeom G = stageGeom<KIND>(D);
+    const int n = D.n[ax], W = D.W[ax], q = D.q[ax], p = D.p[ax], Qa = D.Q[ax], E = D.E[ax];
+    const long long c = item % G.inner;
+    long long r = item / G.inner;
+    const int oi = int(r % W);
+    r /= W;
+    const int i = int(r % n);
+    const long long o = r / n;
+    const int j = i + oi - p;
+    Dot2 acc[S::NOUT];
+    if (j >= 0 && j < n) {
+        const int* first = ibuf + D.eoff[ax];
+        const int* elo = ibuf + D.doff[ax];
+        const int* ehi = elo + n;
+        const int e0 = elo[i] > elo[j] ? elo[i] : elo[j];
+        const int e1 = ehi[i] < ehi[j] ? ehi[i] : ehi[j];
+        const int P1 = p + 1;
+        const long long tstride = (long long)E * q * P1 * P1;
+        const df32* pfa = pf + D.pfoff[ax];
+        for (int e = e0; e <= e1; ++e) {
+            const int fe = first[e];
+            const int s = i - fe, t = j - fe;
+            for (int rr = 0; rr < q; ++rr) {
+                const int g = e * q + rr;
+                const long long pidx = ((long long)(e * q + rr) * P1 + s) * P1 + t;
+                df32 x[S::NIN];
+                const df32* ip = in + G.in_base + (o * Qa + g) * G.inner + c;
+                for (int f = 0; f < S::NIN; ++f) x[f] = ip[f * G.in_fs];
+                df32 pv[4];
+                for (int tau = 0; tau < 4; ++tau) pv[tau] = pfa[tau * tstride + pidx];
+                for (int k = 0; k < S::NT; ++k) {
+                    const Term tm = S::term(k);
+                    acc[tm.h].mac(pv[tm.tau], x[tm.f]);
+                }
+            }
+        }
+    }
+    df32* op = out + G.out_base + ((o * n + i) * W + oi) * G.inner + c;
+    for (int h = 0; h < S::NOUT; ++h) op[h * G.out_fs] = acc[h].result();
+}
+
+// Row-blocked df32 contraction: one work item owns (o, i, c) and produces all W band offsets of
+// the output fields H0..H0+NH-1. For every quadrature abscissa g in the support of function i
+// the inputs are loaded once and combined with the pair factors of the p+1 functions j active
+// on g's element, so loads are amortised over (p+1) x terms multiply-adds.
+template <int KIND>
+GS_HD long long stageRowWork(const DevPatch& D) {
+    const StageGeom g = stageGeom<KIND>(D);
+    return g.outer * D.n[Stage<KIND>::AX] * g.inner;
+}
+
+// merge one element's partial sums (indexed by the local function t of j) into the band
+// accumulators (indexed by the band offset shift + t); shift is uniform across a warp whenever
+// the warp shares the row function i
+template <int P, int NH>
+GS_HD void mergeShift(Dot2 (&acc)[2 * P + 1][NH], const Dot2 (&tmp)[P + 1][NH], int shift) {
+#pragma unroll
+    for (int sh = 0; sh <= P; ++sh) {
+        if (sh != shift) continue;
+#pragma unroll
+        for (int t = 0; t <= P; ++t)
+#pragma unroll
+            for (int h = 0; h < NH; ++h) acc[sh + t][h].add(tmp[t][h]);
+    }
+}
+
+// QC > 0: the Gauss-point count per element is the compile-time QC (the default rule p+1), so
+// the element's whole quadrature loop unrolls and its loads issue together; QC == 0: runtime q
+template <int KIND, int P, int H0, int NH, int QC = 0>
+GS_HD void contractRowDF(const DevPatch& D, long long item, const df32* __restrict__ in, df32* __restrict__ out,
+                         const int* __restrict__ ibuf, const df32* __restrict__ pf) {
+    using S = Stage<KIND>;
+    constexpr int P1 = P + 1, W = 2 * P + 1;
+    const int ax = S::AX;
+    const StageGeom G = stageGeom<KIND>(D);
+    const int n = D.n[ax], q = QC > 0 ? QC : D.q[ax], Qa = D.Q[ax], E = D.E[ax];
+    const long long c = item % G.inner;
+    long long r = item / G.inner;
+    const int i = int(r % n);
+    const long long o = r / n;
+    Dot2 acc[W][NH];
+    const int* first = ibuf + D.eoff[ax];
+    const int* elo = ibuf + D.doff[ax];
+    const int* ehi = elo + n;
+    const long long tstride = (long long)E * q * P1 * P1;
+    const df32* pfa = pf + D.pfoff[ax];
+    for (int e = elo[i]; e <= ehi[i]; ++e) {
+        const int fe = first[e];
+        const int si = i - fe;
+        Dot2 tmp[P1][NH];
+#pragma unroll
+        for (int rr = 0; rr < (QC > 0 ? QC : q); ++rr) {
+            const int g = e * q + rr;
+            df32 x[S::NIN];
+            const df32* ip = in + G.in_base + (o * Qa + g) * G.inner + c;
+#pragma unroll
+            for (int f = 0; f < S::NIN; ++f) x[f] = ip[f * G.in_fs];
+            const df32* prow = pfa + ((long long)(e * q + rr) * P1 + si) * P1;
+#pragma unroll
+            for (int t = 0; t < P1; ++t) {
+                df32 pv[4];
+#pragma unroll
+                for (int tau = 0; tau < 4; ++tau) pv[tau] = prow[tau * tstride + t];
+#pragma unroll
+                for (int k = 0; k < S::NT; ++k) {
+                    const Term tm = S::term(k);
+                    if (tm.h >= H0 && tm.h < H0 + NH) tmp[t][tm.h - H0].mac(pv[tm.tau], x[tm.f]);
+                }
+            }
+        }
+        mergeShift<P, NH>(acc, tmp, P - si);  // band offset of j = fe + t is t + P - si
+    }
+    df32* op = out + G.out_base + (o * n + i) * W * G.inner + c;
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+#pragma unroll
+        for (int h = 0; h < NH; ++h) op[(H0 + h) * G.out_fs + w * G.inner] = acc[w][h].result();
+}
+
+// degree dispatch of the row-blocked contraction (uniform per patch)
+template <int KIND, int H0, int NH>
+GS_HD void contractRowDFp(const DevPatch& D, long long item, const df32* __restrict__ in, df32* __restrict__ out,
+                          const int* __restrict__ ibuf, const df32* __restrict__ pf) {
+    switch (D.p[Stage<KIND>::AX]) {
+        case 1: contractRowDF<KIND, 1, H0, NH>(D, item, in, out, ibuf, pf); break;
+        case 2: contractRowDF<KIND, 2, H0, NH>(D, item, in, out, ibuf, pf); break;
+        case 3: contractRowDF<KIND, 3, H0, NH>(D, item, in, out, ibuf, pf); break;
+        default: contractRowDF<KIND, 4, H0, NH>(D, item, in, out, ibuf, pf); break;
+    }
+}
+
+GS_HD double asDouble(double v) { return v; }
+GS_HD double asDouble(df32 v) { return v.toDouble(); }
+
 // -------------------------------------------------------------------------------------------
 // load vector: single-index contraction of L with the basis values along one axis
 //   3D: 31: L[g2][g1][g0] -> lv1[g2][g1][i0]; 32: lv1 -> lv2[g2][i1][i0]; 33: lv2 -> F[i2][i1][i0]
@@ -447,8 +653,8 @@ GS_HD long long loadWork(const DevPatch& D) {
 }
 // the input of stage 31/21 is the L field, of later stages the previous intermediate; the
 // caller passes the right base pointers (L field buffer or intermediate buffer)
-template <int KIND>
-GS_HD double loadItem(const DevPatch& D, long long item, const double* __restrict__ in, const double* __restrict__ tab,
+template <int KIND, typename Tin>
+GS_HD double loadItem(const DevPatch& D, long long item, const Tin* __restrict__ in, const double* __restrict__ tab,
                       const int* __restrict__ ibuf) {
     const int ax = Stage<KIND>::AX;
     const LoadGeom G = loadGeom<KIND>(D);
@@ -466,7 +672,7 @@ GS_HD double loadItem(const DevPatch& D, long long item, const double* __restric
         const int s = i - first[e];
         for (int rr = 0; rr < q; ++rr) {
             const int g = e * q + rr;
-            acc += tb[(long long)g * 2 * (p + 1) + s] * in[G.in_base + (o * Qa + g) * G.inner + c];
+            acc += tb[(long long)g * 2 * (p + 1) + s] * asDouble(in[G.in_base + (o * Qa + g) * G.inner + c]);
         }
     }
     return acc;
@@ -484,15 +690,25 @@ GS_HD T gatherSlot(uint32_t src, const T* __restrict__ band, const uint32_t* __r
     return acc;
 }
 
+GS_HD df32 gatherSlotDF(uint32_t src, const df32* __restrict__ band, const uint32_t* __restrict__ ovf_ptr,
+                        const uint32_t* __restrict__ ovf_idx) {
+    if (!(src & 0x80000000u)) return band[src];
+    const uint32_t o = src & 0x7fffffffu;
+    df32 acc;
+    for (uint32_t k = ovf_ptr[o]; k < ovf_ptr[o + 1]; ++k) acc += band[ovf_idx[k]];
+    return acc;
+}
+
 // rhs row: load-vector sources minus the Dirichlet lift sum_j K_ij g_j over eliminated j
 // (gsSparseSystem::push, src/gsAssembler/gsSparseSystem.h:972-1010)
+template <typename TB>
 GS_HD double rhsRow(int I, const double* __restrict__ lvec, const uint32_t* __restrict__ lptr,
-                    const uint32_t* __restrict__ lidx, const double* __restrict__ band,
+                    const uint32_t* __restrict__ lidx, const TB* __restrict__ band,
                     const uint32_t* __restrict__ fptr, const uint32_t* __restrict__ fband,
                     const uint32_t* __restrict__ fbidx, const double* __restrict__ ddof) {
     double acc = 0.0;
     for (uint32_t k = lptr[I]; k < lptr[I + 1]; ++k) acc += lvec[lidx[k]];
-    for (uint32_t k = fptr[I]; k < fptr[I + 1]; ++k) acc -= band[fband[k]] * ddof[fbidx[k]];
+    for (uint32_t k = fptr[I]; k < fptr[I + 1]; ++k) acc -= asDouble(band[fband[k]]) * ddof[fbidx[k]];
     return acc;
 }
 

@@ -5,6 +5,7 @@
 
 #include <cstdint>
 
+#include "device_funcs.cuh"
 #include "gsgpu_internal.h"
 
 namespace gsgpu {
@@ -16,23 +17,38 @@ constexpr int kBlock = 256;
 void basisTables(const TabJob* jobs, long long njobs, const double* knots, double* out, cudaStream_t s);
 template <typename T>
 void pairFactors(const PfJob* jobs, const BlkEnt* tab, long long nblk, const double* basis, T* pf, cudaStream_t s);
-void geoStage1(const DevPatch* P, const BlkEnt* tab, long long nblk, const double* coefs, const double* gtab,
-               const int* ibuf, double* Y1, cudaStream_t s);
-void geoStage2(const DevPatch* P, const BlkEnt* tab, long long nblk, const double* Y1, const double* gtab,
-               const int* ibuf, double* Y2, cudaStream_t s);
-void pointStep(const DevPatch* P, const BlkEnt* tab, long long nblk, const FieldParams* F, const double* Y1,
-               const double* Y2, const double* gtab, const int* ibuf, const double* wq, double* C, double* Lf,
-               unsigned long long* detkey, cudaStream_t s);
+template <typename R>
+void geoStage1(const DevPatch* P, const BlkEnt* tab, long long nblk, const R* coefs, const R* gtab, const int* ibuf,
+               R* Y1, cudaStream_t s);
+template <typename R>
+void geoStage2(const DevPatch* P, const BlkEnt* tab, long long nblk, const R* Y1, const R* gtab, const int* ibuf,
+               R* Y2, cudaStream_t s);
+template <typename R>
+void pointStep(const DevPatch* P, const BlkEnt* tab, long long nblk, const dev::FieldConst<R>* F, const R* Y1,
+               const R* Y2, const R* gtab, const int* ibuf, const R* wq, R* C, R* Lf, unsigned long long* detkey,
+               cudaStream_t s);
 template <typename T, int KIND>
 void contract(const DevPatch* P, const BlkEnt* tab, long long nblk, const T* in, T* out, const int* ibuf, const T* pf,
               cudaStream_t s);
 template <int KIND>
-void loadContract(const DevPatch* P, const BlkEnt* tab, long long nblk, const double* in, double* out,
+void contractDF(const DevPatch* P, const BlkEnt* tab, long long nblk, const df32* in, df32* out, const int* ibuf,
+                const df32* pf, cudaStream_t s);
+// degree-P specialisation over the patches whose degree along the stage axis is P
+// (degrees 1..4; the context checks the range)
+template <int KIND, int H0, int NH>
+void contractRowDF(int P, const DevPatch* Pd, const BlkEnt* tab, long long nblk, const df32* in, df32* out,
+                   const int* ibuf, const df32* pf, cudaStream_t s);
+template <int KIND, typename Tin>
+void loadContract(const DevPatch* P, const BlkEnt* tab, long long nblk, const Tin* in, double* out,
                   const double* basis, const int* ibuf, cudaStream_t s);
+void gatherCsrDF(long long nnz, const uint32_t* src, const df32* band, const uint32_t* ovf_ptr, const uint32_t* ovf_idx,
+                 float* hi, float* lo, cudaStream_t s);
+void toDF(long long n, const double* in, df32* out, cudaStream_t s);
 template <typename T>
 void gatherCsr(long long nnz, const uint32_t* src, const T* band, const uint32_t* ovf_ptr, const uint32_t* ovf_idx,
                T* val, cudaStream_t s);
-void rhsRows(int n, const double* lvec, const uint32_t* lptr, const uint32_t* lidx, const double* band,
+template <typename TB>
+void rhsRows(int n, const double* lvec, const uint32_t* lptr, const uint32_t* lidx, const TB* band,
              const uint32_t* fptr, const uint32_t* fband, const uint32_t* fbidx, const double* ddof, double* rhs,
              cudaStream_t s);
 

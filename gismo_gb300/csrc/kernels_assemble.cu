@@ -32,27 +32,29 @@ __global__ void __launch_bounds__(kBlock) k_pair(const PfJob* __restrict__ jobs,
     pf[j.pf + item] = dev::pairFactor<T>(basis + j.tab, j.p, j.q, j.E, item);
 }
 
+template <typename R>
 __global__ void __launch_bounds__(kBlock) k_geo1(const DevPatch* __restrict__ P, const BlkEnt* __restrict__ tab,
-                                                 const double* __restrict__ coefs, const double* __restrict__ gtab,
-                                                 const int* __restrict__ ibuf, double* __restrict__ Y1) {
+                                                 const R* __restrict__ coefs, const R* __restrict__ gtab,
+                                                 const int* __restrict__ ibuf, R* __restrict__ Y1) {
     const BlkEnt be = tab[blockIdx.x];
     const DevPatch& D = P[be.patch];
     const long long item = be.base + threadIdx.x;
     const long long work = D.dim == 3 ? (long long)D.dim * 2 * D.gn[2] * D.gn[1] * D.Q[0]
                                       : (long long)D.dim * 2 * D.gn[1] * D.Q[0];
     if (item >= work) return;
-    Y1[D.y1_off + item] = dev::geoStage1(D, item, coefs, gtab, ibuf);
+    Y1[D.y1_off + item] = dev::geoStage1<R>(D, item, coefs, gtab, ibuf);
 }
 
+template <typename R>
 __global__ void __launch_bounds__(kBlock) k_geo2(const DevPatch* __restrict__ P, const BlkEnt* __restrict__ tab,
-                                                 const double* __restrict__ Y1, const double* __restrict__ gtab,
-                                                 const int* __restrict__ ibuf, double* __restrict__ Y2) {
+                                                 const R* __restrict__ Y1, const R* __restrict__ gtab,
+                                                 const int* __restrict__ ibuf, R* __restrict__ Y2) {
     const BlkEnt be = tab[blockIdx.x];
     const DevPatch& D = P[be.patch];
     const long long item = be.base + threadIdx.x;
     const long long work = (long long)D.dim * 3 * D.gn[2] * D.Q[1] * D.Q[0];
     if (item >= work) return;
-    Y2[D.y2_off + item] = dev::geoStage2(D, item, Y1, gtab, ibuf);
+    Y2[D.y2_off + item] = dev::geoStage2<R>(D, item, Y1, gtab, ibuf);
 }
 
 __device__ __forceinline__ unsigned long long detKey(double v) {
@@ -60,16 +62,17 @@ __device__ __forceinline__ unsigned long long detKey(double v) {
     return (b & 0x8000000000000000ULL) ? ~b : (b | 0x8000000000000000ULL);
 }
 
+template <typename R>
 __global__ void __launch_bounds__(kBlock) k_point(const DevPatch* __restrict__ P, const BlkEnt* __restrict__ tab,
-                                                  const FieldParams* __restrict__ F, const double* __restrict__ Y1,
-                                                  const double* __restrict__ Y2, const double* __restrict__ gtab,
-                                                  const int* __restrict__ ibuf, const double* __restrict__ wq,
-                                                  double* __restrict__ C, double* __restrict__ Lf,
+                                                  const dev::FieldConst<R>* __restrict__ F, const R* __restrict__ Y1,
+                                                  const R* __restrict__ Y2, const R* __restrict__ gtab,
+                                                  const int* __restrict__ ibuf, const R* __restrict__ wq,
+                                                  R* __restrict__ C, R* __restrict__ Lf,
                                                   unsigned long long* __restrict__ detkey) {
-    __shared__ FieldParams sF;
+    __shared__ dev::FieldConst<R> sF;
     // stage the coefficient parameters in shared memory (uniform across the block)
     {
-        const int nw = int(sizeof(FieldParams) / sizeof(int));
+        const int nw = int(sizeof(dev::FieldConst<R>) / sizeof(int));
         const int* src = reinterpret_cast<const int*>(F);
         int* dst = reinterpret_cast<int*>(&sF);
         for (int k = threadIdx.x; k < nw; k += blockDim.x) dst[k] = src[k];
@@ -79,7 +82,7 @@ __global__ void __launch_bounds__(kBlock) k_point(const DevPatch* __restrict__ P
     const DevPatch& D = P[be.patch];
     const long long item = be.base + threadIdx.x;
     unsigned long long key = ~0ULL;
-    if (item < D.nq) key = detKey(dev::pointStep(D, sF, item, Y1, Y2, gtab, ibuf, wq, C, Lf));
+    if (item < D.nq) key = detKey(dev::pointStep<R>(D, sF, item, Y1, Y2, gtab, ibuf, wq, C, Lf));
     for (int o = 16; o > 0; o >>= 1) {
         const unsigned long long other = __shfl_xor_sync(0xffffffffu, key, o);
         key = other < key ? other : key;
@@ -106,14 +109,41 @@ __global__ void __launch_bounds__(kBlock) k_contract(const DevPatch* __restrict_
 }
 
 template <int KIND>
+__global__ void __launch_bounds__(kBlock) k_contract_df(const DevPatch* __restrict__ P, const BlkEnt* __restrict__ tab,
+                                                        const df32* __restrict__ in, df32* __restrict__ out,
+                                                        const int* __restrict__ ibuf, const df32* __restrict__ pf) {
+    const BlkEnt be = tab[blockIdx.x];
+    const DevPatch& D = P[be.patch];
+    const long long item = be.base + threadIdx.x;
+    if (item >= dev::stageWork<KIND>(D)) return;
+    dev::contractItemDF<KIND>(D, item, in, out, ibuf, pf);
+}
+
+template <int KIND, int DEG, int H0, int NH>
+__global__ void __launch_bounds__(kBlock) k_contract_row_df(const DevPatch* __restrict__ P,
+                                                            const BlkEnt* __restrict__ tab,
+                                                            const df32* __restrict__ in, df32* __restrict__ out,
+                                                            const int* __restrict__ ibuf,
+                                                            const df32* __restrict__ pf) {
+    const BlkEnt be = tab[blockIdx.x];
+    const DevPatch& D = P[be.patch];
+    const long long item = be.base + threadIdx.x;
+    if (item >= dev::stageRowWork<KIND>(D)) return;
+    if (D.q[dev::Stage<KIND>::AX] == DEG + 1)
+        dev::contractRowDF<KIND, DEG, H0, NH, DEG + 1>(D, item, in, out, ibuf, pf);
+    else
+        dev::contractRowDF<KIND, DEG, H0, NH, 0>(D, item, in, out, ibuf, pf);
+}
+
+template <int KIND, typename Tin>
 __global__ void __launch_bounds__(kBlock) k_load(const DevPatch* __restrict__ P, const BlkEnt* __restrict__ tab,
-                                                 const double* __restrict__ in, double* __restrict__ out,
+                                                 const Tin* __restrict__ in, double* __restrict__ out,
                                                  const double* __restrict__ basis, const int* __restrict__ ibuf) {
     const BlkEnt be = tab[blockIdx.x];
     const DevPatch& D = P[be.patch];
     const long long item = be.base + threadIdx.x;
     if (item >= dev::loadWork<KIND>(D)) return;
-    out[dev::loadGeom<KIND>(D).out_base + item] = dev::loadItem<KIND>(D, item, in, basis, ibuf);
+    out[dev::loadGeom<KIND>(D).out_base + item] = dev::loadItem<KIND, Tin>(D, item, in, basis, ibuf);
 }
 
 template <typename T>
@@ -125,14 +155,31 @@ __global__ void __launch_bounds__(kBlock) k_gather(long long nnz, const uint32_t
     val[s] = dev::gatherSlot<T>(src[s], band, ovf_ptr, ovf_idx);
 }
 
+__global__ void __launch_bounds__(kBlock) k_gather_df(long long nnz, const uint32_t* __restrict__ src,
+                                                      const df32* __restrict__ band, const uint32_t* __restrict__ ovf_ptr,
+                                                      const uint32_t* __restrict__ ovf_idx, float* __restrict__ hi,
+                                                      float* __restrict__ lo) {
+    const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nnz) return;
+    const df32 v = dev::gatherSlotDF(src[s], band, ovf_ptr, ovf_idx);
+    hi[s] = v.hi;
+    lo[s] = v.lo;
+}
+
+__global__ void __launch_bounds__(kBlock) k_to_df(long long n, const double* __restrict__ in, df32* __restrict__ out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = df32(in[i]);
+}
+
+template <typename TB>
 __global__ void __launch_bounds__(kBlock) k_rhs(int n, const double* __restrict__ lvec, const uint32_t* __restrict__ lptr,
-                                                const uint32_t* __restrict__ lidx, const double* __restrict__ band,
+                                                const uint32_t* __restrict__ lidx, const TB* __restrict__ band,
                                                 const uint32_t* __restrict__ fptr, const uint32_t* __restrict__ fband,
                                                 const uint32_t* __restrict__ fbidx, const double* __restrict__ ddof,
                                                 double* __restrict__ rhs) {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     if (I >= n) return;
-    rhs[I] = dev::rhsRow(I, lvec, lptr, lidx, band, fptr, fband, fbidx, ddof);
+    rhs[I] = dev::rhsRow<TB>(I, lvec, lptr, lidx, band, fptr, fband, fbidx, ddof);
 }
 
 __global__ void __launch_bounds__(kBlock) k_coef_soa(const DevPatch* __restrict__ P, const BlkEnt* __restrict__ tab,
@@ -160,21 +207,80 @@ void pairFactors(const PfJob* jobs, const BlkEnt* tab, long long nblk, const dou
     if (nblk > 0) k_pair<T><<<unsigned(nblk), kBlock, 0, s>>>(jobs, tab, basis, pf);
 }
 template void pairFactors<double>(const PfJob*, const BlkEnt*, long long, const double*, double*, cudaStream_t);
-template void pairFactors<float>(const PfJob*, const BlkEnt*, long long, const double*, float*, cudaStream_t);
+template void pairFactors<df32>(const PfJob*, const BlkEnt*, long long, const double*, df32*, cudaStream_t);
 
-void geoStage1(const DevPatch* P, const BlkEnt* tab, long long nblk, const double* coefs, const double* gtab,
-               const int* ibuf, double* Y1, cudaStream_t s) {
-    if (nblk > 0) k_geo1<<<unsigned(nblk), kBlock, 0, s>>>(P, tab, coefs, gtab, ibuf, Y1);
+template <typename R>
+void geoStage1(const DevPatch* P, const BlkEnt* tab, long long nblk, const R* coefs, const R* gtab, const int* ibuf,
+               R* Y1, cudaStream_t s) {
+    if (nblk > 0) k_geo1<R><<<unsigned(nblk), kBlock, 0, s>>>(P, tab, coefs, gtab, ibuf, Y1);
 }
-void geoStage2(const DevPatch* P, const BlkEnt* tab, long long nblk, const double* Y1, const double* gtab,
-               const int* ibuf, double* Y2, cudaStream_t s) {
-    if (nblk > 0) k_geo2<<<unsigned(nblk), kBlock, 0, s>>>(P, tab, Y1, gtab, ibuf, Y2);
+template <typename R>
+void geoStage2(const DevPatch* P, const BlkEnt* tab, long long nblk, const R* Y1, const R* gtab, const int* ibuf,
+               R* Y2, cudaStream_t s) {
+    if (nblk > 0) k_geo2<R><<<unsigned(nblk), kBlock, 0, s>>>(P, tab, Y1, gtab, ibuf, Y2);
 }
-void pointStep(const DevPatch* P, const BlkEnt* tab, long long nblk, const FieldParams* F, const double* Y1,
-               const double* Y2, const double* gtab, const int* ibuf, const double* wq, double* C, double* Lf,
-               unsigned long long* detkey, cudaStream_t s) {
-    if (nblk > 0) k_point<<<unsigned(nblk), kBlock, 0, s>>>(P, tab, F, Y1, Y2, gtab, ibuf, wq, C, Lf, detkey);
+template <typename R>
+void pointStep(const DevPatch* P, const BlkEnt* tab, long long nblk, const dev::FieldConst<R>* F, const R* Y1,
+               const R* Y2, const R* gtab, const int* ibuf, const R* wq, R* C, R* Lf, unsigned long long* detkey,
+               cudaStream_t s) {
+    if (nblk > 0) k_point<R><<<unsigned(nblk), kBlock, 0, s>>>(P, tab, F, Y1, Y2, gtab, ibuf, wq, C, Lf, detkey);
 }
+#define INST_GEO(R)                                                                                                \
+    template void geoStage1<R>(const DevPatch*, const BlkEnt*, long long, const R*, const R*, const int*, R*,       \
+                               cudaStream_t);                                                                      \
+    template void geoStage2<R>(const DevPatch*, const BlkEnt*, long long, const R*, const R*, const int*, R*,       \
+                               cudaStream_t);                                                                      \
+    template void pointStep<R>(const DevPatch*, const BlkEnt*, long long, const dev::FieldConst<R>*, const R*,      \
+                               const R*, const R*, const int*, const R*, R*, R*, unsigned long long*, cudaStream_t);
+INST_GEO(double)
+INST_GEO(df32)
+
+template <int KIND>
+void contractDF(const DevPatch* P, const BlkEnt* tab, long long nblk, const df32* in, df32* out, const int* ibuf,
+                const df32* pf, cudaStream_t s) {
+    if (nblk > 0) k_contract_df<KIND><<<unsigned(nblk), kBlock, 0, s>>>(P, tab, in, out, ibuf, pf);
+}
+template void contractDF<31>(const DevPatch*, const BlkEnt*, long long, const df32*, df32*, const int*, const df32*, cudaStream_t);
+template void contractDF<32>(const DevPatch*, const BlkEnt*, long long, const df32*, df32*, const int*, const df32*, cudaStream_t);
+template void contractDF<33>(const DevPatch*, const BlkEnt*, long long, const df32*, df32*, const int*, const df32*, cudaStream_t);
+template void contractDF<21>(const DevPatch*, const BlkEnt*, long long, const df32*, df32*, const int*, const df32*, cudaStream_t);
+template void contractDF<22>(const DevPatch*, const BlkEnt*, long long, const df32*, df32*, const int*, const df32*, cudaStream_t);
+
+template <int KIND, int H0, int NH>
+void contractRowDF(int P, const DevPatch* Pd, const BlkEnt* tab, long long nblk, const df32* in, df32* out,
+                   const int* ibuf, const df32* pf, cudaStream_t s) {
+    if (nblk <= 0) return;
+    switch (P) {
+        case 1: k_contract_row_df<KIND, 1, H0, NH><<<unsigned(nblk), kBlock, 0, s>>>(Pd, tab, in, out, ibuf, pf); break;
+        case 2: k_contract_row_df<KIND, 2, H0, NH><<<unsigned(nblk), kBlock, 0, s>>>(Pd, tab, in, out, ibuf, pf); break;
+        case 3: k_contract_row_df<KIND, 3, H0, NH><<<unsigned(nblk), kBlock, 0, s>>>(Pd, tab, in, out, ibuf, pf); break;
+        case 4: k_contract_row_df<KIND, 4, H0, NH><<<unsigned(nblk), kBlock, 0, s>>>(Pd, tab, in, out, ibuf, pf); break;
+        default: break;
+    }
+}
+#define INST_ROW(K, H0, NH) \
+    template void contractRowDF<K, H0, NH>(int, const DevPatch*, const BlkEnt*, long long, const df32*, df32*, const int*, const df32*, cudaStream_t);
+INST_ROW(31, 0, 4)
+INST_ROW(31, 4, 4)
+INST_ROW(32, 0, 4)
+INST_ROW(31, 0, 2)
+INST_ROW(31, 2, 2)
+INST_ROW(31, 4, 2)
+INST_ROW(31, 6, 2)
+INST_ROW(32, 0, 2)
+INST_ROW(32, 2, 2)
+INST_ROW(33, 0, 1)
+INST_ROW(21, 0, 4)
+INST_ROW(22, 0, 1)
+
+void gatherCsrDF(long long nnz, const uint32_t* src, const df32* band, const uint32_t* ovf_ptr, const uint32_t* ovf_idx,
+                 float* hi, float* lo, cudaStream_t s) {
+    if (nnz > 0) k_gather_df<<<grid1(nnz), kBlock, 0, s>>>(nnz, src, band, ovf_ptr, ovf_idx, hi, lo);
+}
+void toDF(long long n, const double* in, df32* out, cudaStream_t s) {
+    if (n > 0) k_to_df<<<grid1(n), kBlock, 0, s>>>(n, in, out);
+}
+
 template <typename T, int KIND>
 void contract(const DevPatch* P, const BlkEnt* tab, long long nblk, const T* in, T* out, const int* ibuf, const T* pf,
               cudaStream_t s) {
@@ -187,22 +293,21 @@ INST_CONTRACT(double, 32)
 INST_CONTRACT(double, 33)
 INST_CONTRACT(double, 21)
 INST_CONTRACT(double, 22)
-INST_CONTRACT(float, 31)
-INST_CONTRACT(float, 32)
-INST_CONTRACT(float, 33)
-INST_CONTRACT(float, 21)
-INST_CONTRACT(float, 22)
 
-template <int KIND>
-void loadContract(const DevPatch* P, const BlkEnt* tab, long long nblk, const double* in, double* out,
+template <int KIND, typename Tin>
+void loadContract(const DevPatch* P, const BlkEnt* tab, long long nblk, const Tin* in, double* out,
                   const double* basis, const int* ibuf, cudaStream_t s) {
-    if (nblk > 0) k_load<KIND><<<unsigned(nblk), kBlock, 0, s>>>(P, tab, in, out, basis, ibuf);
+    if (nblk > 0) k_load<KIND, Tin><<<unsigned(nblk), kBlock, 0, s>>>(P, tab, in, out, basis, ibuf);
 }
-template void loadContract<31>(const DevPatch*, const BlkEnt*, long long, const double*, double*, const double*, const int*, cudaStream_t);
-template void loadContract<32>(const DevPatch*, const BlkEnt*, long long, const double*, double*, const double*, const int*, cudaStream_t);
-template void loadContract<33>(const DevPatch*, const BlkEnt*, long long, const double*, double*, const double*, const int*, cudaStream_t);
-template void loadContract<21>(const DevPatch*, const BlkEnt*, long long, const double*, double*, const double*, const int*, cudaStream_t);
-template void loadContract<22>(const DevPatch*, const BlkEnt*, long long, const double*, double*, const double*, const int*, cudaStream_t);
+#define INST_LOAD(K, Tin) \
+    template void loadContract<K, Tin>(const DevPatch*, const BlkEnt*, long long, const Tin*, double*, const double*, const int*, cudaStream_t);
+INST_LOAD(31, double)
+INST_LOAD(32, double)
+INST_LOAD(33, double)
+INST_LOAD(21, double)
+INST_LOAD(22, double)
+INST_LOAD(31, df32)
+INST_LOAD(21, df32)
 
 template <typename T>
 void gatherCsr(long long nnz, const uint32_t* src, const T* band, const uint32_t* ovf_ptr, const uint32_t* ovf_idx,
@@ -212,11 +317,16 @@ void gatherCsr(long long nnz, const uint32_t* src, const T* band, const uint32_t
 template void gatherCsr<double>(long long, const uint32_t*, const double*, const uint32_t*, const uint32_t*, double*, cudaStream_t);
 template void gatherCsr<float>(long long, const uint32_t*, const float*, const uint32_t*, const uint32_t*, float*, cudaStream_t);
 
-void rhsRows(int n, const double* lvec, const uint32_t* lptr, const uint32_t* lidx, const double* band,
+template <typename TB>
+void rhsRows(int n, const double* lvec, const uint32_t* lptr, const uint32_t* lidx, const TB* band,
              const uint32_t* fptr, const uint32_t* fband, const uint32_t* fbidx, const double* ddof, double* rhs,
              cudaStream_t s) {
-    if (n > 0) k_rhs<<<grid1(n), kBlock, 0, s>>>(n, lvec, lptr, lidx, band, fptr, fband, fbidx, ddof, rhs);
+    if (n > 0) k_rhs<TB><<<grid1(n), kBlock, 0, s>>>(n, lvec, lptr, lidx, band, fptr, fband, fbidx, ddof, rhs);
 }
+template void rhsRows<double>(int, const double*, const uint32_t*, const uint32_t*, const double*, const uint32_t*,
+                              const uint32_t*, const uint32_t*, const double*, double*, cudaStream_t);
+template void rhsRows<df32>(int, const double*, const uint32_t*, const uint32_t*, const df32*, const uint32_t*,
+                            const uint32_t*, const uint32_t*, const double*, double*, cudaStream_t);
 
 void coefsToSoa(const DevPatch* P, const BlkEnt* tab, long long nblk, const double* raw, double* soa, cudaStream_t s) {
     if (nblk > 0) k_coef_soa<<<unsigned(nblk), kBlock, 0, s>>>(P, tab, raw, soa);

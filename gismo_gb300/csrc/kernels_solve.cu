@@ -6,12 +6,20 @@
 // Iteration (gsConjugateGradient::step, src/gsSolver/gsConjugateGradient.hpp:54-84):
 //   t = A p; alpha = rho / (p.t); x += alpha p; r -= alpha t; stop if ||r||/||b|| < tol;
 //   z = D^-1 r; beta = (r.z)/rho; p = z + beta p.
+#include "df32.cuh"
 #include "kernels_solve.h"
 
 namespace gsgpu {
 namespace {
 
 constexpr int kB = 256;
+
+// column of slot k of row `row`: absolute int32 columns, or 16-bit offsets from the row
+template <bool REL>
+__device__ __forceinline__ int colOf(int row, int k, const int* __restrict__ col, const int16_t* __restrict__ coff) {
+    if (REL) return row + int(coff[k]);
+    return col[k];
+}
 
 __device__ __forceinline__ double warpSum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -43,6 +51,48 @@ __device__ __forceinline__ void blockSumStore2(double a, double b, double* outa,
         outb[blockIdx.x] = sb;
     }
 }
+// FP32 values: warp sums in FP32, per-warp results summed in FP64 (fixed order)
+__device__ __forceinline__ float warpSumF(float v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ void blockSumStoreF2(float a, float b, double* outa, double* outb) {
+    __shared__ double wa[kB / 32], wb[kB / 32];
+    a = warpSumF(a);
+    b = warpSumF(b);
+    if ((threadIdx.x & 31) == 0) { wa[threadIdx.x >> 5] = a; wb[threadIdx.x >> 5] = b; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sa = 0.0, sb = 0.0;
+        for (int w = 0; w < kB / 32; ++w) { sa += wa[w]; sb += wb[w]; }
+        outa[blockIdx.x] = sa;
+        outb[blockIdx.x] = sb;
+    }
+}
+__device__ __forceinline__ void blockSumStoreF(float a, double* outa) {
+    __shared__ double wa[kB / 32];
+    a = warpSumF(a);
+    if ((threadIdx.x & 31) == 0) wa[threadIdx.x >> 5] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sa = 0.0;
+        for (int w = 0; w < kB / 32; ++w) sa += wa[w];
+        outa[blockIdx.x] = sa;
+    }
+}
+// only the leader lane of each row group holds a value: sum the groups' values (fixed order)
+template <int RPB>
+__device__ __forceinline__ void leaderSumStore(double v, bool leader, int group, double* out) {
+    __shared__ double sm[RPB];
+    if (leader) sm[group] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int g = 0; g < RPB; ++g) s += sm[g];
+        out[blockIdx.x] = s;
+    }
+}
+
 // single-block reduction of n partials (fixed order)
 __device__ __forceinline__ double reducePartials(const double* part, int n) {
     __shared__ double ws[kB / 32];
@@ -57,27 +107,30 @@ __device__ __forceinline__ double reducePartials(const double* part, int n) {
     return s;
 }
 
-// t = A p (LPR lanes per row) and partial sums of p.t
-template <int LPR>
+// t = A p (LPR lanes per row, grid-stride over row groups) and block partial sums of p.t
+template <int LPR, bool REL>
 __global__ void __launch_bounds__(kB) k_spmv_dot(int n, const int* __restrict__ ptr, const int* __restrict__ col,
+                                                 const int16_t* __restrict__ coff,
                                                  const double* __restrict__ val, const double* __restrict__ p,
                                                  double* __restrict__ t, double* __restrict__ part,
                                                  const CgState* __restrict__ st) {
     if (st->done) return;
     const int rowsPerBlock = kB / LPR;
     const int lane = threadIdx.x % LPR;
-    const int row = blockIdx.x * rowsPerBlock + threadIdx.x / LPR;
     double contrib = 0.0;
-    double s = 0.0;
-    if (row < n)
-        for (int k = ptr[row] + lane; k < ptr[row + 1]; k += LPR) s += val[k] * p[col[k]];
-    // every lane of the warp takes part in the shuffles (rows past n contribute 0)
-    for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (row < n && lane == 0) {
-        t[row] = s;
-        contrib = s * p[row];
+    for (int base = blockIdx.x * rowsPerBlock; base < n; base += gridDim.x * rowsPerBlock) {
+        const int row = base + threadIdx.x / LPR;
+        double s = 0.0;
+        if (row < n)
+            for (int k = ptr[row] + lane; k < ptr[row + 1]; k += LPR) s += val[k] * p[colOf<REL>(row, k, col, coff)];
+        // every lane of the warp takes part in the shuffles (rows past n contribute 0)
+        for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (row < n && lane == 0) {
+            t[row] = s;
+            contrib += s * p[row];
+        }
     }
-    blockSumStore(contrib, part);
+    leaderSumStore<kB / LPR>(contrib, lane == 0, threadIdx.x / LPR, part);
 }
 
 __global__ void __launch_bounds__(kB) k_alpha(int nparts, const double* __restrict__ part, CgState* __restrict__ st) {
@@ -94,16 +147,15 @@ __global__ void __launch_bounds__(kB) k_update(int n, double* __restrict__ x, do
                                                const CgState* __restrict__ st) {
     if (st->done) return;
     const double alpha = st->alpha;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double rr = 0.0, rz = 0.0;
-    if (i < n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         x[i] += alpha * p[i];
         const double ri = r[i] - alpha * t[i];
         r[i] = ri;
         const double zi = dinv[i] * ri;
         z[i] = zi;
-        rr = ri * ri;
-        rz = ri * zi;
+        rr += ri * ri;
+        rz += ri * zi;
     }
     blockSumStore2(rr, rz, prr, prz);
 }
@@ -131,8 +183,7 @@ __global__ void __launch_bounds__(kB) k_pupd(int n, double* __restrict__ p, cons
                                              const CgState* __restrict__ st) {
     if (st->done) return;
     const double beta = st->beta;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) p[i] = z[i] + beta * p[i];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = z[i] + beta * p[i];
 }
 
 // start: x = 0, r = b, z = D^-1 b, p = z; partial sums of b.b and r.z
@@ -140,17 +191,16 @@ __global__ void __launch_bounds__(kB) k_init(int n, const double* __restrict__ b
                                              double* __restrict__ r, double* __restrict__ z, double* __restrict__ p,
                                              const double* __restrict__ dinv, double* __restrict__ pbb,
                                              double* __restrict__ prz) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double bb = 0.0, rz = 0.0;
-    if (i < n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const double bi = b[i];
         x[i] = 0.0;
         r[i] = bi;
         const double zi = dinv[i] * bi;
         z[i] = zi;
         p[i] = zi;
-        bb = bi * bi;
-        rz = bi * zi;
+        bb += bi * bi;
+        rz += bi * zi;
     }
     blockSumStore2(bb, rz, pbb, prz);
 }
@@ -168,6 +218,13 @@ __global__ void __launch_bounds__(kB) k_init_reduce(int nparts, const double* __
         st->rho = rz;
         st->alpha = st->beta = 0.0;
         st->relres = bb > 0.0 ? 1.0 : 0.0;
+        st->pause = 0;
+        st->pupd_skip = 0;
+        st->replacements = 0;
+        st->replaced = 0;
+        st->restart = 0;
+        st->last_true = 1.0;
+        st->delta = 1e-2;
         // zero rhs: x = 0 is the solution; x0 = 0 gives ||r||/||b|| = 1 >= tol otherwise
         st->done = (bb == 0.0 || 1.0 < tol) ? 1 : (maxit <= 0 ? 2 : 0);
     }
@@ -179,13 +236,228 @@ __global__ void __launch_bounds__(kB) k_dinv(int n, const int* __restrict__ diag
     if (i < n) dinv[i] = damping / val[diag[i]];
 }
 
+// ---------------------------------------------------------------------------------------------
+// mixed precision: the inner PCG runs in FP32 on the operator A_hi = fl32(A); every chunk of
+// iterations ends with a residual replacement r = b - (A_hi + A_lo) x evaluated in df32 from the
+// FP64 iterate, so the stopping test is on the true FP64-accurate residual (iterative refinement
+// with the Krylov direction kept across replacements). Dot products accumulate in FP64.
+
+template <int LPR, bool REL>
+__global__ void __launch_bounds__(kB) k_spmv32_dot(int n, const int* __restrict__ ptr, const int* __restrict__ col,
+                                                   const int16_t* __restrict__ coff,
+                                                   const float* __restrict__ val, const float* __restrict__ p,
+                                                   float* __restrict__ t, double* __restrict__ part,
+                                                   const CgState* __restrict__ st) {
+    if (st->done || st->pause) return;
+    const int rowsPerBlock = kB / LPR;
+    const int lane = threadIdx.x % LPR;
+    double contrib = 0.0;
+    for (int base = blockIdx.x * rowsPerBlock; base < n; base += gridDim.x * rowsPerBlock) {
+        const int row = base + threadIdx.x / LPR;
+        float s = 0.f;
+        if (row < n)
+            for (int k = ptr[row] + lane; k < ptr[row + 1]; k += LPR) s = fmaf(val[k], p[colOf<REL>(row, k, col, coff)], s);
+        for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (row < n && lane == 0) {
+            t[row] = s;
+            contrib += double(s) * double(p[row]);
+        }
+    }
+    leaderSumStore<kB / LPR>(contrib, lane == 0, threadIdx.x / LPR, part);
+}
+
+__global__ void __launch_bounds__(kB) k_alpha_m(int nparts, const double* __restrict__ part, CgState* __restrict__ st) {
+    if (st->done || st->pause) return;
+    const double pAp = reducePartials(part, nparts);
+    if (threadIdx.x == 0) st->alpha = st->rho / pAp;
+}
+
+__global__ void __launch_bounds__(kB) k_update32(int n, float* __restrict__ dx, float* __restrict__ r,
+                                                 float* __restrict__ z, const float* __restrict__ p,
+                                                 const float* __restrict__ t, const float* __restrict__ dinv,
+                                                 double* __restrict__ prr, double* __restrict__ prz,
+                                                 const CgState* __restrict__ st) {
+    if (st->done || st->pause) return;
+    const float alpha = float(st->alpha);
+    float rr = 0.f, rz = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        dx[i] = fmaf(alpha, p[i], dx[i]);
+        const float ri = fmaf(-alpha, t[i], r[i]);
+        r[i] = ri;
+        const float zi = dinv[i] * ri;
+        z[i] = zi;
+        rr = fmaf(ri, ri, rr);
+        rz = fmaf(ri, zi, rz);
+    }
+    blockSumStoreF2(rr, rz, prr, prz);
+}
+
+__global__ void __launch_bounds__(kB) k_beta_m(int nparts, const double* __restrict__ prr,
+                                               const double* __restrict__ prz, CgState* __restrict__ st) {
+    if (st->done || st->pause) {
+        if (threadIdx.x == 0) st->pupd_skip = 1;
+        return;
+    }
+    const double rr = reducePartials(prr, nparts);
+    const double rz = reducePartials(prz, nparts);
+    if (threadIdx.x == 0) {
+        st->pupd_skip = 0;
+        st->iters += 1;
+        st->relres = sqrt(rr) / st->bnorm;  // recursive estimate; the true value comes at replacement
+        // replace the residual once the recursion has gained delta (the FP32 recursion cannot
+        // follow the true residual much further), at the tolerance, or at the iteration limit
+        if (st->relres < st->tol || st->relres < st->delta * st->last_true || st->iters >= st->maxit) st->pause = 1;
+        st->beta = rz / st->rho;
+        st->rho = rz;
+    }
+}
+
+__global__ void __launch_bounds__(kB) k_pupd32(int n, float* __restrict__ p, const float* __restrict__ z,
+                                               const CgState* __restrict__ st) {
+    if (st->done || st->pupd_skip) return;
+    const float beta = float(st->beta);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        p[i] = fmaf(beta, p[i], z[i]);
+}
+
+// x += dx (FP64), dx = 0, and the df32 split of x for the residual SpMV
+__global__ void __launch_bounds__(kB) k_xupd(int n, double* __restrict__ x, float* __restrict__ dx,
+                                             float* __restrict__ xhi, float* __restrict__ xlo,
+                                             const CgState* __restrict__ st) {
+    if (st->done || !st->pause) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double xi = x[i] + double(dx[i]);
+        x[i] = xi;
+        dx[i] = 0.f;
+        const df32 v(xi);
+        xhi[i] = v.hi;
+        xlo[i] = v.lo;
+    }
+}
+
+// r = b - (A_hi + A_lo) x with df32 products and compensated accumulation; partial sums of r.r
+template <int LPR, bool REL>
+__global__ void __launch_bounds__(kB) k_resid_df(int n, const int* __restrict__ ptr, const int* __restrict__ col,
+                                                 const int16_t* __restrict__ coff,
+                                                 const float* __restrict__ hi, const float* __restrict__ lo,
+                                                 const float* __restrict__ xhi, const float* __restrict__ xlo,
+                                                 const double* __restrict__ b, double* __restrict__ r,
+                                                 double* __restrict__ part, const CgState* __restrict__ st) {
+    if (st->done || !st->pause) return;
+    const int rowsPerBlock = kB / LPR;
+    const int lane = threadIdx.x % LPR;
+    double contrib = 0.0;
+    for (int base = blockIdx.x * rowsPerBlock; base < n; base += gridDim.x * rowsPerBlock) {
+        const int row = base + threadIdx.x / LPR;
+        Dot2 acc;
+        if (row < n)
+            for (int k = ptr[row] + lane; k < ptr[row + 1]; k += LPR) {
+                const int c = colOf<REL>(row, k, col, coff);
+                acc.mac(df32(hi[k], lo[k]), df32(xhi[c], xlo[c]));
+            }
+        df32 y = acc.result();
+        for (int o = LPR / 2; o > 0; o >>= 1) {
+            df32 oth(__shfl_xor_sync(0xffffffffu, y.hi, o), __shfl_xor_sync(0xffffffffu, y.lo, o));
+            y = y + oth;
+        }
+        if (row < n && lane == 0) {
+            const double ri = b[row] - y.toDouble();
+            r[row] = ri;
+            contrib += ri * ri;
+        }
+    }
+    leaderSumStore<kB / LPR>(contrib, lane == 0, threadIdx.x / LPR, part);
+}
+
+__global__ void __launch_bounds__(kB) k_rel_check(int nparts, const double* __restrict__ part,
+                                                  CgState* __restrict__ st) {
+    if (st->done || !st->pause) return;
+    const double rr = reducePartials(part, nparts);
+    if (threadIdx.x == 0) {
+        const double rec = st->relres;  // the recursive estimate that triggered the replacement
+        st->replacements += 1;
+        st->relres = sqrt(rr) / st->bnorm;
+        st->restart = st->relres > 4.0 * rec ? 1 : 0;
+        st->last_true = st->relres;
+        if (st->relres < st->tol) st->done = 1;
+        else if (st->iters >= st->maxit) st->done = 2;
+        else {
+            st->pause = 0;
+            st->replaced = 1;
+        }
+    }
+}
+
+// restart the FP32 recursion from the replaced residual: r32 = fl32(r), z = D^-1 r32, partial r.z;
+// the search direction is kept unless the replacement moved the residual a lot
+__global__ void __launch_bounds__(kB) k_r32(int n, const double* __restrict__ r, float* __restrict__ r32,
+                                            float* __restrict__ z, float* __restrict__ p,
+                                            const float* __restrict__ dinv, double* __restrict__ prz,
+                                            const CgState* __restrict__ st) {
+    if (!st->replaced) return;
+    const int restart = st->restart;
+    float rz = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float ri = float(r[i]);
+        r32[i] = ri;
+        const float zi = dinv[i] * ri;
+        z[i] = zi;
+        if (restart) p[i] = zi;
+        rz = fmaf(ri, zi, rz);
+    }
+    blockSumStoreF(rz, prz);
+}
+
+__global__ void __launch_bounds__(kB) k_rho(int nparts, const double* __restrict__ prz, CgState* __restrict__ st) {
+    if (!st->replaced) return;
+    const double rz = reducePartials(prz, nparts);
+    if (threadIdx.x == 0) {
+        st->rho = rz;
+        st->replaced = 0;
+    }
+}
+
+// start: x = 0, dx = 0, r = b, r32 = fl32(b), z = D^-1 r32, p = z; partial b.b and r.z
+__global__ void __launch_bounds__(kB) k_init_m(int n, const double* __restrict__ b, double* __restrict__ x,
+                                               double* __restrict__ r, float* __restrict__ dx, float* __restrict__ r32,
+                                               float* __restrict__ z, float* __restrict__ p,
+                                               const float* __restrict__ dinv, double* __restrict__ pbb,
+                                               double* __restrict__ prz) {
+    double bb = 0.0, rz = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double bi = b[i];
+        x[i] = 0.0;
+        r[i] = bi;
+        dx[i] = 0.f;
+        const float ri = float(bi);
+        r32[i] = ri;
+        const float zi = dinv[i] * ri;
+        z[i] = zi;
+        p[i] = zi;
+        bb += bi * bi;
+        rz += double(ri) * double(zi);
+    }
+    blockSumStore2(bb, rz, pbb, prz);
+}
+
+__global__ void __launch_bounds__(kB) k_dinv32(int n, const int* __restrict__ diag, const float* __restrict__ val,
+                                               float* __restrict__ dinv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dinv[i] = 1.0f / val[diag[i]];
+}
+
 inline unsigned g1(long long n) { return unsigned((n + kB - 1) / kB); }
 
 }  // namespace
 
 namespace launch {
 
-int cgPartials(int n) { return int(g1(n > 0 ? n : 1)); }
+// vector kernels run grid-stride on at most kMaxVecBlocks blocks, so dot products leave few partials
+constexpr int kMaxVecBlocks = 512;
+int cgPartials(int n) {
+    const int g = int(g1(n > 0 ? n : 1));
+    return g < kMaxVecBlocks ? g : kMaxVecBlocks;
+}
 
 void jacobiDiag(int n, const int* diag, const double* val, double damping, double* dinv, cudaStream_t s) {
     if (n > 0) k_dinv<<<g1(n), kB, 0, s>>>(n, diag, val, damping, dinv);
@@ -197,17 +469,21 @@ void cgInit(const CgBuffers& B, double tol, int maxit, cudaStream_t s) {
     k_init_reduce<<<1, kB, 0, s>>>(np, B.part0, B.part1, B.st, tol, maxit);
 }
 
+// launch a row kernel template for the lanes-per-row and column-format choice of B
+#define GSGPU_ROW_DISPATCH(KERNEL, NB, ...)                                                                    \
+    do {                                                                                                       \
+        const bool rel = B.coff != nullptr;                                                                    \
+        switch (B.lanes_per_row) {                                                                             \
+            case 4: rel ? KERNEL<4, true><<<NB, kB, 0, s>>>(__VA_ARGS__) : KERNEL<4, false><<<NB, kB, 0, s>>>(__VA_ARGS__); break; \
+            case 8: rel ? KERNEL<8, true><<<NB, kB, 0, s>>>(__VA_ARGS__) : KERNEL<8, false><<<NB, kB, 0, s>>>(__VA_ARGS__); break; \
+            case 16: rel ? KERNEL<16, true><<<NB, kB, 0, s>>>(__VA_ARGS__) : KERNEL<16, false><<<NB, kB, 0, s>>>(__VA_ARGS__); break; \
+            default: rel ? KERNEL<32, true><<<NB, kB, 0, s>>>(__VA_ARGS__) : KERNEL<32, false><<<NB, kB, 0, s>>>(__VA_ARGS__); break; \
+        }                                                                                                      \
+    } while (0)
+
 void cgSpmv(const CgBuffers& B, cudaStream_t s) {
-    const int lpr = B.lanes_per_row;
-    const int rows_per_block = kB / lpr;
-    const int nb = (B.n + rows_per_block - 1) / rows_per_block;
-    // B.part2 holds spmvPartials(n, 32) >= nb entries for every lanes-per-row choice below
-    switch (lpr) {
-        case 4: k_spmv_dot<4><<<nb, kB, 0, s>>>(B.n, B.ptr, B.col, B.val, B.p, B.t, B.part2, B.st); break;
-        case 8: k_spmv_dot<8><<<nb, kB, 0, s>>>(B.n, B.ptr, B.col, B.val, B.p, B.t, B.part2, B.st); break;
-        case 16: k_spmv_dot<16><<<nb, kB, 0, s>>>(B.n, B.ptr, B.col, B.val, B.p, B.t, B.part2, B.st); break;
-        default: k_spmv_dot<32><<<nb, kB, 0, s>>>(B.n, B.ptr, B.col, B.val, B.p, B.t, B.part2, B.st); break;
-    }
+    const int nb = spmvPartials(B.n, B.lanes_per_row);
+    GSGPU_ROW_DISPATCH(k_spmv_dot, nb, B.n, B.ptr, B.col, B.coff, B.val, B.p, B.t, B.part2, B.st);
 }
 
 void cgRest(const CgBuffers& B, cudaStream_t s) {
@@ -226,7 +502,48 @@ void cgIteration(const CgBuffers& B, cudaStream_t s) {
 
 int spmvPartials(int n, int lanes_per_row) {
     const int rows_per_block = kB / lanes_per_row;
-    return (n + rows_per_block - 1) / rows_per_block;
+    const int nb = (n + rows_per_block - 1) / rows_per_block;
+    return nb < kMaxSpmvBlocks ? (nb > 0 ? nb : 1) : kMaxSpmvBlocks;
+}
+
+void jacobiDiag32(int n, const int* diag, const float* val_hi, float* dinv32, cudaStream_t s) {
+    if (n > 0) k_dinv32<<<g1(n), kB, 0, s>>>(n, diag, val_hi, dinv32);
+}
+
+void mixedInit(const CgBuffers& B, double tol, int maxit, cudaStream_t s) {
+    const int np = cgPartials(B.n);
+    k_init_m<<<np, kB, 0, s>>>(B.n, B.b, B.x, B.r, B.dx32, B.r32, B.z32, B.p32, B.dinv32, B.part0, B.part1);
+    k_init_reduce<<<1, kB, 0, s>>>(np, B.part0, B.part1, B.st, tol, maxit);
+}
+
+void mixedSpmv(const CgBuffers& B, cudaStream_t s) {
+    const int nb = spmvPartials(B.n, B.lanes_per_row);
+    GSGPU_ROW_DISPATCH(k_spmv32_dot, nb, B.n, B.ptr, B.col, B.coff, B.val_hi, B.p32, B.t32, B.part2, B.st);
+}
+
+void mixedRest(const CgBuffers& B, cudaStream_t s) {
+    const int np = cgPartials(B.n);
+    const int nb = spmvPartials(B.n, B.lanes_per_row);
+    k_alpha_m<<<1, kB, 0, s>>>(nb, B.part2, B.st);
+    k_update32<<<np, kB, 0, s>>>(B.n, B.dx32, B.r32, B.z32, B.p32, B.t32, B.dinv32, B.part0, B.part1, B.st);
+    k_beta_m<<<1, kB, 0, s>>>(np, B.part0, B.part1, B.st);
+    k_pupd32<<<np, kB, 0, s>>>(B.n, B.p32, B.z32, B.st);
+}
+
+void mixedIteration(const CgBuffers& B, cudaStream_t s) {
+    mixedSpmv(B, s);
+    mixedRest(B, s);
+}
+
+void mixedReplace(const CgBuffers& B, cudaStream_t s) {
+    const int np = cgPartials(B.n);
+    const int nb = spmvPartials(B.n, B.lanes_per_row);
+    k_xupd<<<np, kB, 0, s>>>(B.n, B.x, B.dx32, B.xhi, B.xlo, B.st);
+    GSGPU_ROW_DISPATCH(k_resid_df, nb, B.n, B.ptr, B.col, B.coff, B.val_hi, B.val_lo, B.xhi, B.xlo, B.b, B.r, B.part2,
+                       B.st);
+    k_rel_check<<<1, kB, 0, s>>>(nb, B.part2, B.st);
+    k_r32<<<np, kB, 0, s>>>(B.n, B.r, B.r32, B.z32, B.p32, B.dinv32, B.part1, B.st);
+    k_rho<<<1, kB, 0, s>>>(np, B.part1, B.st);
 }
 
 }  // namespace launch

@@ -248,7 +248,8 @@ void buildLayout(const ProblemDesc& pd, Layout& L) {
             D.W[k] = 2 * B.p + 1;
             D.gp[k] = G.p;
             D.gn[k] = G.n();
-            if (B.p > 15 || G.p > 15 || D.q[k] > 32) throw std::invalid_argument("degree / quadrature too large");
+            if (B.p < 1 || B.p > 4 || G.p > 15 || D.q[k] > 32)
+                throw std::invalid_argument("discretisation degree must be 1..4 (geometry degree <= 15, <= 32 Gauss points)");
             D.ngeo *= D.gn[k];
             D.nq *= D.Q[k];
             D.ndof *= D.n[k];

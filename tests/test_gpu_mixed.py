@@ -1,0 +1,74 @@
+"""Mixed precision on the GPU: the double-float (two-FP32) assembly reproduces the FP64 operator,
+and the FP32 inner CG with FP64-accurate residual replacement reaches the FP64 solution.
+
+Bars: the df32 operator and rhs within 1e-11 relative of the FP64 oracle (absolute floor 1e-13 x
+the row's largest entry); the mixed solution within 1e-8 relative (2-norm) of a tightly converged
+FP64 GPU solution, its reported residual being the true residual."""
+import numpy as np
+import pytest
+
+from gismo_gb300 import problems as P
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "square_p2_64": lambda: P.square_poisson(64, 2),
+    "disp2d_p4_40x33": lambda: P.displaced_single_patch(2, (40, 33), (4, 4), 9, 0.05, ufreq=3),
+    "disp3d_p3_16": lambda: P.volume_poisson(16, 3, seed=2),
+    "cubegrid2_p2_n4": lambda: P.cube_grid(n=2, n_elem=4, p=2, seed=3, kappa_modes=8),
+}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__ as g
+    g.build()
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_df32_operator_matches_fp64_oracle(case):
+    from gismo_gb300.assembler import GpuPoissonAssembler
+    from oracle import oracle as O
+    prob = CASES[case]()
+    o = O.OracleProblem(prob)
+    o.assemble()
+    optr, ocol, oval = o.csr()
+    A = GpuPoissonAssembler(prob)
+    A.assemble("mixed")
+    ptr, col, val = A.csr()
+    assert np.array_equal(ptr, optr) and np.array_equal(col, ocol)
+    rowmax = np.maximum.reduceat(np.abs(oval), optr[:-1])
+    floor = np.repeat(rowmax, np.diff(optr)) * 1e-13
+    assert np.all(np.abs(val - oval) <= 1e-11 * np.abs(oval) + floor)
+    assert np.abs(A.rhs() - o.rhs()).max() <= 1e-11 * np.abs(o.rhs()).max()
+    A.close()
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_mixed_solution_matches_fp64(case):
+    from gismo_gb300.assembler import GpuPoissonAssembler
+    prob = CASES[case]()
+    A = GpuPoissonAssembler(prob)
+    A.assemble("fp64")
+    x64, i64 = A.solve(tol=1e-13, max_iters=20000)
+    A.assemble("mixed")
+    xm, im = A.solve(tol=1e-11, precision="mixed", max_iters=20000)
+    assert im["converged"], im
+    assert im["relres"] < 1e-11 and im["refinements"] >= 1
+    err = np.linalg.norm(xm - x64) / np.linalg.norm(x64)
+    assert err <= 1e-8, (err, im, i64)
+    # the reported residual is the true one: check it on the host in FP64
+    K, b = A.matrix(), A.rhs()
+    assert np.linalg.norm(b - K @ xm) <= 2e-11 * np.linalg.norm(b)
+    A.close()
+
+
+def test_mixed_needs_mixed_assembly():
+    from gismo_gb300.assembler import GpuPoissonAssembler
+    from gismo_gb300._lib import GsGpuError, ERR_STATE
+    A = GpuPoissonAssembler(P.square_poisson(8, 2))
+    A.assemble("fp64")
+    with pytest.raises(GsGpuError) as e:
+        A.solve(precision="mixed")
+    assert e.value.code == ERR_STATE
+    A.close()
