@@ -53,17 +53,6 @@ void DeviceArena::releaseAll() {
     used = 0;
 }
 
-template <typename T>
-static void upload(DeviceArena& A, T*& dptr, const std::vector<T>& h, cudaStream_t s) {
-    A.release(dptr);
-    dptr = static_cast<T*>(A.alloc(h.size() * sizeof(T)));
-    if (!h.empty()) GSGPU_CUDA_TRY(cudaMemcpyAsync(dptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
-}
-template <typename T>
-static void allocN(DeviceArena& A, T*& dptr, long long n) {
-    A.release(dptr);
-    dptr = static_cast<T*>(A.alloc(size_t(std::max(0LL, n)) * sizeof(T)));
-}
 
 }  // namespace gsgpu
 
@@ -376,6 +365,7 @@ void Context::assemble(int precision) {
     assembled = true;
     solved = false;
     assembledPrecision = precision;
+    ++assembleSerial;
     if (!(detMin > 0.0)) throw JacobianError("geometry map has det J <= 0 at a quadrature point");
 }
 
@@ -392,7 +382,9 @@ void Context::times(double* ms) {
 void Context::dropGraphs() {
     if (gexecFp64) cudaGraphExecDestroy(gexecFp64);
     if (gexecMixed) cudaGraphExecDestroy(gexecMixed);
-    gexecFp64 = gexecMixed = nullptr;
+    if (gexecMg) cudaGraphExecDestroy(gexecMg);
+    gexecFp64 = gexecMixed = gexecMg = nullptr;
+    gexecMgKey = MgGraphKey();
 }
 
 void Context::freeAssembly() {
@@ -458,7 +450,17 @@ int Context::lanesPerRow(bool fp64) const {
 
 void Context::solve(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
     if (!assembled) throw StateError("solve() before assemble()");
-    if (o.method != GSGPU_SOLVER_CG_JACOBI) throw std::invalid_argument("solver method not available in this build");
+    if (o.method == GSGPU_SOLVER_CG_MG) {
+        if (o.precision == GSGPU_PREC_MIXED && assembledPrecision != kMixed)
+            throw StateError("mixed-precision solve needs assemble(GSGPU_PREC_MIXED)");
+        if (o.precision == GSGPU_PREC_FP64 && assembledPrecision != kFP64)
+            throw StateError("FP64 solve needs assemble(GSGPU_PREC_FP64)");
+        if (o.precision != GSGPU_PREC_MIXED && o.precision != GSGPU_PREC_FP64)
+            throw std::invalid_argument("unknown precision mode");
+        solveMG(o, info);
+        return;
+    }
+    if (o.method != GSGPU_SOLVER_CG_JACOBI) throw std::invalid_argument("unknown solver method");
     if (o.precision == GSGPU_PREC_MIXED) {
         if (assembledPrecision != kMixed) throw StateError("mixed-precision solve needs assemble(GSGPU_PREC_MIXED)");
         solveMixed(o, info);

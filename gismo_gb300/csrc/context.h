@@ -11,7 +11,9 @@
 #include "../../include/gsgpu.h"
 #include "gsgpu_internal.h"
 #include "device_funcs.cuh"
+#include "kernels_mg.h"
 #include "kernels_solve.h"
+#include "mg_plan.h"
 #include "plan.h"
 
 namespace gsgpu {
@@ -43,6 +45,46 @@ struct DeviceArena {
 struct Tab {
     std::vector<BlkEnt> h;
     BlkEnt* d = nullptr;
+};
+
+template <typename T>
+inline void upload(DeviceArena& A, T*& dptr, const std::vector<T>& h, cudaStream_t s) {
+    A.release(dptr);
+    dptr = static_cast<T*>(A.alloc(h.size() * sizeof(T)));
+    if (!h.empty()) GSGPU_CUDA_TRY(cudaMemcpyAsync(dptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+template <typename T>
+inline void allocN(DeviceArena& A, T*& dptr, long long n) {
+    A.release(dptr);
+    dptr = static_cast<T*>(A.alloc(size_t(n > 0 ? n : 0) * sizeof(T)));
+}
+
+// one coarse level of the multigrid hierarchy on the device (level 0 is the assembled system)
+struct MgLevelBuf {
+    MgLevelPlan plan;
+    int lpr64 = 8, lpr32 = 16;
+    DevPatch* dPatches = nullptr;
+    double *dKnots = nullptr, *dTab = nullptr, *dPf = nullptr;
+    TabJob* dTabJobs = nullptr;
+    PfJob* dPfJobs = nullptr;
+    int* dIbuf = nullptr;
+    Tab tabPf, tabSt[3];
+    int *dPtr = nullptr, *dCol = nullptr, *dDiag = nullptr;
+    int16_t* dColOff = nullptr;
+    uint32_t *dSrc = nullptr, *dOvfPtr = nullptr, *dOvfIdx = nullptr;
+    int *dPptr = nullptr, *dPcol = nullptr, *dRptr = nullptr, *dRcol = nullptr;
+    double *dPval = nullptr, *dRval = nullptr, *dVal = nullptr, *dVec = nullptr;  // dVec: dinv b x r z p t
+    float *dPval32 = nullptr, *dRval32 = nullptr, *dVal32 = nullptr, *dVec32 = nullptr;
+};
+
+// what a captured multigrid solver graph depends on
+struct MgGraphKey {
+    int mixed = -1, levels = 0, npre = 0, npost = 0, coarse_iters = 0;
+    double damping = 0.0, coarse_tol = 0.0;
+    bool operator==(const MgGraphKey& o) const {
+        return mixed == o.mixed && levels == o.levels && npre == o.npre && npost == o.npost &&
+               coarse_iters == o.coarse_iters && damping == o.damping && coarse_tol == o.coarse_tol;
+    }
 };
 
 namespace launch {
@@ -99,6 +141,22 @@ struct Context {
     cudaGraphExec_t gexecFp64 = nullptr, gexecMixed = nullptr;
     int gexecLpr[2] = {0, 0};
     void dropGraphs();
+    // h-multigrid: coarse levels, level-0 vectors, coarsest-level state and the solver graph
+    std::vector<MgLevelBuf> mgl;
+    int mgLevels = 0;
+    long long assembleSerial = 0, mgSerial = -1;
+    int mgPrecision = -1, mgCoarseIters = 0;
+    double mgCoarseTol = 0.0;
+    double *dMgVec0 = nullptr, *dMgPart = nullptr, *dRold = nullptr;  // level 0 FP64: dinv b x r z
+    float* dMgVec0f = nullptr;                                       // level 0 FP32: dinv b x r z
+    CgState *dMgCoarseSt = nullptr, *dMgSt = nullptr;
+    cudaGraphExec_t gexecMg = nullptr;
+    MgGraphKey gexecMgKey;
+    void mgSetup(int levels);
+    void mgAssemble(bool mixed);
+    void solveMG(const gsgpu_solver_opts& o, gsgpu_solve_info& info);
+    template <typename T>
+    void mgRun(const gsgpu_solver_opts& o, gsgpu_solve_info& info, bool mixed);
     // profiling of the solver's SpMV launches
     bool profiling = false;
     long long spmvLaunches = 0;

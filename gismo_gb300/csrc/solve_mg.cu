@@ -1,0 +1,388 @@
+// CG preconditioned by the h-multigrid V-cycle (gsConjugateGradient + gsMultiGridOp, as set up by
+// examples/multiGrid_example.cpp:243-300): hierarchy set-up, coarse Galerkin operators on the
+// device, and the solver loop under a captured CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <random>
+#include <stdexcept>
+#include <vector>
+
+#include "context.h"
+#include "kernels.h"
+#include "kernels_mg.h"
+#include "mg_plan.h"
+
+namespace gsgpu {
+
+namespace {
+
+// lanes per CSR row from the average row length (same rule as the fine-level solvers)
+int lanesFor(const Pattern& pat, bool fp64) {
+    const double avg = pat.n ? double(pat.col.size()) / pat.n : 1.0;
+    if (avg > 20) return fp64 ? 8 : 16;
+    if (avg > 10) return 8;
+    return 4;
+}
+
+void tableFor(DeviceArena& A, cudaStream_t s, Tab& T, const std::vector<long long>& work) {
+    blockTable(work, launch::kBlock, T.h);
+    upload(A, T.d, T.h, s);
+}
+
+std::vector<float> toFloat(const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); }
+
+// the FP64 or the FP32 member of a buffer pair
+template <typename T>
+T*& pick(double*& d, float*& f);
+template <>
+double*& pick<double>(double*& d, float*&) {
+    return d;
+}
+template <>
+float*& pick<float>(double*&, float*& f) {
+    return f;
+}
+
+double envOr(const char* name, double dflt) {
+    const char* e = std::getenv(name);
+    return e ? std::atof(e) : dflt;
+}
+
+}  // namespace
+
+// host plan of levels 1..levels-1 and their static device data (once per refresh and level count)
+void Context::mgSetup(int levels) {
+    if (mgLevels == levels && !mgl.empty()) return;
+    if (gexecMg) cudaGraphExecDestroy(gexecMg);
+    gexecMg = nullptr;
+    gexecMgKey = MgGraphKey();
+    for (MgLevelBuf& M : mgl) {
+        for (void* p : {(void*)M.dPatches, (void*)M.dKnots, (void*)M.dTab, (void*)M.dPf, (void*)M.dTabJobs,
+                        (void*)M.dPfJobs, (void*)M.dIbuf, (void*)M.tabPf.d, (void*)M.tabSt[0].d, (void*)M.tabSt[1].d,
+                        (void*)M.tabSt[2].d, (void*)M.dPtr, (void*)M.dCol, (void*)M.dDiag, (void*)M.dColOff,
+                        (void*)M.dSrc, (void*)M.dOvfPtr, (void*)M.dOvfIdx, (void*)M.dPptr, (void*)M.dPcol,
+                        (void*)M.dRptr, (void*)M.dRcol, (void*)M.dPval, (void*)M.dRval, (void*)M.dVal, (void*)M.dVec,
+                        (void*)M.dPval32, (void*)M.dRval32, (void*)M.dVal32, (void*)M.dVec32})
+            arena.release(p);
+    }
+    mgl.clear();
+    mgLevels = 0;
+    mgSerial = -1;
+    std::vector<MgLevelPlan> plans;
+    buildMgPlan(pd, map, L, levels, plans);
+    mgl.resize(plans.size());
+    cudaStream_t s = stream;
+    for (size_t i = 0; i < plans.size(); ++i) {
+        MgLevelBuf& M = mgl[i];
+        M.plan = std::move(plans[i]);
+        const Layout& LL = M.plan.L;
+        const Pattern& P = M.plan.pat;
+        // the coarse contractions reuse the finest level's intermediate buffers
+        if (LL.s > L.s || LL.u > std::max(1LL, L.u) || LL.band > L.band)
+            throw std::runtime_error("multigrid level needs larger contraction buffers than the finest level");
+        upload(arena, M.dPatches, LL.dev, s);
+        upload(arena, M.dKnots, LL.knots, s);
+        upload(arena, M.dTabJobs, LL.tabjobs, s);
+        upload(arena, M.dPfJobs, LL.pfjobs, s);
+        upload(arena, M.dIbuf, LL.ibuf, s);
+        allocN(arena, M.dTab, LL.ntab);
+        allocN(arena, M.dPf, LL.npf);
+        {
+            std::vector<long long> w;
+            for (const PfJob& j : LL.pfjobs) w.push_back(j.count);
+            tableFor(arena, s, M.tabPf, w);
+        }
+        auto stageTab = [&](Tab& T, auto fn) {
+            std::vector<long long> w;
+            for (const DevPatch& D : LL.dev) w.push_back(fn(D));
+            tableFor(arena, s, T, w);
+        };
+        if (pd.dim == 3) {
+            stageTab(M.tabSt[0], [](const DevPatch& D) { return dev::stageWork<31>(D); });
+            stageTab(M.tabSt[1], [](const DevPatch& D) { return dev::stageWork<32>(D); });
+            stageTab(M.tabSt[2], [](const DevPatch& D) { return dev::stageWork<33>(D); });
+        } else {
+            stageTab(M.tabSt[0], [](const DevPatch& D) { return dev::stageWork<21>(D); });
+            stageTab(M.tabSt[1], [](const DevPatch& D) { return dev::stageWork<22>(D); });
+        }
+        upload(arena, M.dPtr, P.ptr, s);
+        upload(arena, M.dCol, P.col, s);
+        upload(arena, M.dDiag, M.plan.diag, s);
+        upload(arena, M.dSrc, P.src, s);
+        upload(arena, M.dOvfPtr, P.ovf_ptr.empty() ? std::vector<uint32_t>(1, 0) : P.ovf_ptr, s);
+        upload(arena, M.dOvfIdx, P.ovf_idx.empty() ? std::vector<uint32_t>(1, 0) : P.ovf_idx, s);
+        bool fits = !P.col.empty();
+        for (int r = 0; r < P.n && fits; ++r)
+            for (int k = P.ptr[r]; k < P.ptr[r + 1]; ++k)
+                if (P.col[k] - r > 32767 || P.col[k] - r < -32768) { fits = false; break; }
+        if (fits) {
+            std::vector<int16_t> off(P.col.size());
+            for (int r = 0; r < P.n; ++r)
+                for (int k = P.ptr[r]; k < P.ptr[r + 1]; ++k) off[k] = int16_t(P.col[k] - r);
+            upload(arena, M.dColOff, off, s);
+        }
+        upload(arena, M.dPptr, M.plan.Pptr, s);
+        upload(arena, M.dPcol, M.plan.Pcol, s);
+        upload(arena, M.dRptr, M.plan.Rptr, s);
+        upload(arena, M.dRcol, M.plan.Rcol, s);
+        M.lpr64 = lanesFor(P, true);
+        M.lpr32 = lanesFor(P, false);
+    }
+    GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    mgLevels = levels;
+}
+
+// Galerkin operators of the coarse levels from the current fields (FP64, or df32 rounded to FP32)
+void Context::mgAssemble(bool mixed) {
+    const int prec = mixed ? kMixed : kFP64;
+    if (mgSerial == assembleSerial && mgPrecision == prec) return;
+    cudaStream_t s = stream;
+    const df32* cDf = reinterpret_cast<const df32*>(dFieldC);
+    df32* sDf = reinterpret_cast<df32*>(dS);
+    df32* uDf = reinterpret_cast<df32*>(dU);
+    df32* bandDf = reinterpret_cast<df32*>(dBand);
+    for (MgLevelBuf& M : mgl) {
+        const Layout& LL = M.plan.L;
+        const Pattern& P = M.plan.pat;
+        const long long nnz = (long long)P.col.size();
+        auto nb = [&](int st) { return (long long)M.tabSt[st].h.size(); };
+        launch::basisTables(M.dTabJobs, (long long)LL.tabjobs.size(), M.dKnots, M.dTab, s);
+        if (!mixed) {
+            launch::pairFactors<double>(M.dPfJobs, M.tabPf.d, (long long)M.tabPf.h.size(), M.dTab, M.dPf, s);
+            if (pd.dim == 3) {
+                launch::contract<double, 31>(M.dPatches, M.tabSt[0].d, nb(0), dFieldC, dS, M.dIbuf, M.dPf, s);
+                launch::contract<double, 32>(M.dPatches, M.tabSt[1].d, nb(1), dS, dU, M.dIbuf, M.dPf, s);
+                launch::contract<double, 33>(M.dPatches, M.tabSt[2].d, nb(2), dU, dBand, M.dIbuf, M.dPf, s);
+            } else {
+                launch::contract<double, 21>(M.dPatches, M.tabSt[0].d, nb(0), dFieldC, dS, M.dIbuf, M.dPf, s);
+                launch::contract<double, 22>(M.dPatches, M.tabSt[1].d, nb(1), dS, dBand, M.dIbuf, M.dPf, s);
+            }
+            if (!M.dVal) allocN(arena, M.dVal, nnz);
+            launch::gatherCsr<double>(nnz, M.dSrc, dBand, M.dOvfPtr, M.dOvfIdx, M.dVal, s);
+            if (!M.dPval) {
+                upload(arena, M.dPval, M.plan.Pval, s);
+                upload(arena, M.dRval, M.plan.Rval, s);
+            }
+        } else {
+            df32* pf = reinterpret_cast<df32*>(M.dPf);
+            launch::pairFactors<df32>(M.dPfJobs, M.tabPf.d, (long long)M.tabPf.h.size(), M.dTab, pf, s);
+            if (pd.dim == 3) {
+                launch::contractDF<31>(M.dPatches, M.tabSt[0].d, nb(0), cDf, sDf, M.dIbuf, pf, s);
+                launch::contractDF<32>(M.dPatches, M.tabSt[1].d, nb(1), sDf, uDf, M.dIbuf, pf, s);
+                launch::contractDF<33>(M.dPatches, M.tabSt[2].d, nb(2), uDf, bandDf, M.dIbuf, pf, s);
+            } else {
+                launch::contractDF<21>(M.dPatches, M.tabSt[0].d, nb(0), cDf, sDf, M.dIbuf, pf, s);
+                launch::contractDF<22>(M.dPatches, M.tabSt[1].d, nb(1), sDf, bandDf, M.dIbuf, pf, s);
+            }
+            if (!M.dVal32) allocN(arena, M.dVal32, nnz);
+            // the low halves are not used by the FP32 V-cycle: they go to the free stage-1 buffer
+            float* loScratch = reinterpret_cast<float*>(dS);
+            float* loOwn = nullptr;
+            if (2 * L.s < nnz) allocN(arena, loOwn, nnz), loScratch = loOwn;
+            launch::gatherCsrDF(nnz, M.dSrc, bandDf, M.dOvfPtr, M.dOvfIdx, M.dVal32, loScratch, s);
+            if (loOwn) {
+                GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
+                arena.release(loOwn);
+            }
+            if (!M.dPval32) {
+                upload(arena, M.dPval32, toFloat(M.plan.Pval), s);
+                upload(arena, M.dRval32, toFloat(M.plan.Rval), s);
+            }
+        }
+    }
+    GSGPU_CUDA_TRY(cudaGetLastError());
+    mgSerial = assembleSerial;
+    mgPrecision = prec;
+    mgCoarseIters = 0;  // the coarse operator changed: size the coarse iteration cap again
+}
+
+template <typename T>
+void Context::mgRun(const gsgpu_solver_opts& o, gsgpu_solve_info& info, bool mixed) {
+    cudaStream_t s = stream;
+    const int n = pat.n;
+    const int nl = int(mgl.size()) + 1;
+    // device vectors: level 0 (dinv b x r z), coarse levels (dinv b x r z p t), FP64 outer state
+    T*& vec0 = pick<T>(dMgVec0, dMgVec0f);
+    if (!vec0) allocN(arena, vec0, 5LL * n);
+    for (MgLevelBuf& M : mgl) {
+        T*& v = pick<T>(M.dVec, M.dVec32);
+        if (!v) allocN(arena, v, 7LL * M.plan.pat.n);
+    }
+    const int np = launch::mgPartials();
+    if (!dMgPart) allocN(arena, dMgPart, 6LL * np);
+    if (!dRold) allocN(arena, dRold, n);
+    if (!dMgCoarseSt) dMgCoarseSt = static_cast<CgState*>(arena.alloc(sizeof(CgState)));
+    if (!dMgSt) dMgSt = static_cast<CgState*>(arena.alloc(sizeof(CgState)));
+
+    std::vector<MgLevelDev<T>> lv(nl);
+    {
+        MgLevelDev<T>& A = lv[0];
+        A.n = n;
+        A.lpr = lanesPerRow(!mixed);
+        A.ptr = dPtr;
+        A.col = dCol;
+        A.coff = dColOff;
+        A.val = pick<T>(dVal, dValHi);
+        A.diag = dDiag;
+        A.dinv = vec0;
+        A.b = vec0 + n;
+        A.x = vec0 + 2LL * n;
+        A.r = vec0 + 3LL * n;
+        A.z = vec0 + 4LL * n;
+    }
+    for (int l = 1; l < nl; ++l) {
+        MgLevelBuf& M = mgl[l - 1];
+        MgLevelDev<T>& C = lv[l];
+        const int m = M.plan.pat.n;
+        T* v = pick<T>(M.dVec, M.dVec32);
+        C.n = m;
+        C.lpr = mixed ? M.lpr32 : M.lpr64;
+        C.ptr = M.dPtr;
+        C.col = M.dCol;
+        C.coff = M.dColOff;
+        C.val = pick<T>(M.dVal, M.dVal32);
+        C.diag = M.dDiag;
+        C.dinv = v;
+        C.b = v + m;
+        C.x = v + 2LL * m;
+        C.r = v + 3LL * m;
+        C.z = v + 4LL * m;
+        C.p = v + 5LL * m;
+        C.t = v + 6LL * m;
+        C.Pptr = M.dPptr;
+        C.Pcol = M.dPcol;
+        C.Rptr = M.dRptr;
+        C.Rcol = M.dRcol;
+        C.Pval = pick<T>(M.dPval, M.dPval32);
+        C.Rval = pick<T>(M.dRval, M.dRval32);
+        if (l == nl - 1) {
+            C.part0 = dMgPart + 3LL * np;
+            C.part1 = dMgPart + 4LL * np;
+            C.part2 = dMgPart + 5LL * np;
+            C.st = dMgCoarseSt;
+        }
+    }
+    for (const MgLevelDev<T>& A : lv) launch::mgDinv<T>(A, s);
+
+    MgParams prm;
+    prm.npre = o.mg_npre >= 0 ? o.mg_npre : 2;
+    prm.npost = o.mg_npost >= 0 ? o.mg_npost : 2;
+    prm.damping = o.mg_damping > 0 ? o.mg_damping : 0.6;
+    prm.coarse_tol = envOr("GSGPU_MG_COARSE_TOL", mixed ? 1e-5 : 1e-10);
+    if (mgCoarseIters == 0 || mgCoarseTol != prm.coarse_tol) {
+        // size the coarse iteration cap: iterations of the coarsest Jacobi-PCG on a seeded random
+        // right-hand side (all eigenmodes present) plus a margin; later coarse solves stop at the
+        // tolerance or at this cap
+        const MgLevelDev<T>& C = lv[nl - 1];
+        std::vector<T> rb(C.n);
+        std::mt19937_64 g(12345);
+        std::uniform_real_distribution<double> u(-1.0, 1.0);
+        for (T& v : rb) v = T(u(g));
+        GSGPU_CUDA_TRY(cudaMemcpyAsync(C.b, rb.data(), rb.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+        launch::coarseStart<T>(C, prm.coarse_tol, nullptr, s);
+        CgState hs{};
+        const int limit = 4 * C.n + 100;
+        for (int done = 0; done < limit; done += 16) {
+            launch::coarseIters<T>(C, 16, nullptr, s);
+            GSGPU_CUDA_TRY(cudaMemcpyAsync(&hs, C.st, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+            GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
+            if (hs.done) break;
+        }
+        mgCoarseIters = std::min(1000, std::max(1, hs.iters + std::max(4, hs.iters / 8)));
+        mgCoarseTol = prm.coarse_tol;
+    }
+    prm.coarse_iters = mgCoarseIters;
+
+    MgOuter O;
+    O.n = n;
+    O.lpr = lanesPerRow(true);
+    O.ptr = dPtr;
+    O.col = dCol;
+    O.coff = dColOff;
+    if (mixed) {
+        O.hi = dValHi;
+        O.lo = dValLo;
+    } else {
+        O.val = dVal;
+    }
+    O.b = dRhs;
+    O.x = dX;
+    O.r = dR;
+    O.rold = dRold;
+    O.p = dP;
+    O.t = dT;
+    O.part0 = dMgPart;
+    O.part1 = dMgPart + np;
+    O.part2 = dMgPart + 2LL * np;
+    O.st = dMgSt;
+    const double tol = o.tol > 0 ? o.tol : 1e-10;
+    const int maxit = o.max_iters > 0 ? o.max_iters : 1000;
+    launch::mgPcgStart(O, tol, maxit, s);
+
+    // outer iterations in chunks captured as one graph (once per parameter set); the kernels
+    // become no-ops once the outer CG has converged
+    const int chunk = 2;
+    MgGraphKey key;
+    key.mixed = mixed;
+    key.levels = nl;
+    key.npre = prm.npre;
+    key.npost = prm.npost;
+    key.coarse_iters = prm.coarse_iters;
+    key.damping = prm.damping;
+    key.coarse_tol = prm.coarse_tol;
+    if (!gexecMg || !(gexecMgKey == key)) {
+        if (gexecMg) cudaGraphExecDestroy(gexecMg);
+        gexecMg = nullptr;
+        cudaGraph_t g;
+        GSGPU_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < chunk; ++k) {
+            launch::mgPcgPrecond<T>(O, lv, prm, s);
+            launch::mgPcgStep(O, s);
+        }
+        GSGPU_CUDA_TRY(cudaStreamEndCapture(s, &g));
+        GSGPU_CUDA_TRY(cudaGraphInstantiate(&gexecMg, g, 0));
+        cudaGraphDestroy(g);
+        gexecMgKey = key;
+    }
+    CgState hs{};
+    for (int it = 0; it < maxit + chunk; it += chunk) {
+        GSGPU_CUDA_TRY(cudaGraphLaunch(gexecMg, s));
+        GSGPU_CUDA_TRY(cudaMemcpyAsync(&hs, dMgSt, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+        GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
+        if (hs.done) break;
+    }
+    info.iterations = hs.iters;
+    info.relres = hs.relres;
+    info.refinements = 0;
+    lastConverged = hs.done == 1;
+}
+
+void Context::solveMG(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
+    const bool mixed = o.precision == GSGPU_PREC_MIXED;
+    const int levels = o.mg_levels > 0 ? o.mg_levels : 4;
+    if (levels < 2) throw std::invalid_argument("multigrid needs at least 2 levels");
+    ensureSolveBuffers();
+    if (mixed) ensureMixedBuffers();
+    cudaStream_t s = stream;
+    cudaEvent_t e0, e1;
+    GSGPU_CUDA_TRY(cudaEventCreate(&e0));
+    GSGPU_CUDA_TRY(cudaEventCreate(&e1));
+    GSGPU_CUDA_TRY(cudaEventRecord(e0, s));
+    mgSetup(levels);
+    mgAssemble(mixed);
+    if (mixed) mgRun<float>(o, info, true);
+    else mgRun<double>(o, info, false);
+    GSGPU_CUDA_TRY(cudaEventRecord(e1, s));
+    GSGPU_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    info.t_solve_ms = ms;
+    solved = true;
+}
+
+}  // namespace gsgpu
