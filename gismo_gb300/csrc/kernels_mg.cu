@@ -15,18 +15,16 @@
 #include <cstdint>
 
 #include "kernels_mg.h"
+#include "spmv_row.cuh"
 
 namespace gsgpu {
 namespace {
 
 constexpr int kB = 256;
-constexpr int kMaxBlocks = 512;
+// grid cap: 8 resident blocks of 256 threads on each of the 152 SMs (full occupancy)
+constexpr int kMaxBlocks = 8 * 152;
 
-template <bool REL>
-__device__ __forceinline__ int colAt(int row, int k, const int* __restrict__ col, const int16_t* __restrict__ coff) {
-    if (REL) return row + int(coff[k]);
-    return col[k];
-}
+constexpr int kUnroll = 4;  // independent (value, column) -> x load chains per lane
 
 template <typename T>
 __device__ __forceinline__ T warpSum(T v) {
@@ -75,7 +73,8 @@ __device__ __forceinline__ void rowLoop(int n, const int* __restrict__ ptr, cons
         const int row = base + threadIdx.x / LPR;
         T s = T(0);
         if (row < n)
-            for (int k = ptr[row] + lane; k < ptr[row + 1]; k += LPR) s += val(k) * x[colAt<REL>(row, k, col, coff)];
+            dev::rowMac<LPR, kUnroll, REL>(row, ptr[row], ptr[row + 1], lane, col, coff, val,
+                                           [&](int c) { return x[c]; }, [&](T v, T xv) { s += v * xv; });
         for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (row < n && lane == 0) epi(row, s);
     }

@@ -8,18 +8,13 @@
 //   z = D^-1 r; beta = (r.z)/rho; p = z + beta p.
 #include "df32.cuh"
 #include "kernels_solve.h"
+#include "spmv_row.cuh"
 
 namespace gsgpu {
 namespace {
 
 constexpr int kB = 256;
-
-// column of slot k of row `row`: absolute int32 columns, or 16-bit offsets from the row
-template <bool REL>
-__device__ __forceinline__ int colOf(int row, int k, const int* __restrict__ col, const int16_t* __restrict__ coff) {
-    if (REL) return row + int(coff[k]);
-    return col[k];
-}
+constexpr int kUnroll = 4;  // independent (value, column) -> x load chains per lane in the SpMV loops
 
 __device__ __forceinline__ double warpSum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -122,7 +117,9 @@ __global__ void __launch_bounds__(kB) k_spmv_dot(int n, const int* __restrict__ 
         const int row = base + threadIdx.x / LPR;
         double s = 0.0;
         if (row < n)
-            for (int k = ptr[row] + lane; k < ptr[row + 1]; k += LPR) s += val[k] * p[colOf<REL>(row, k, col, coff)];
+            dev::rowMac<LPR, kUnroll, REL>(
+                row, ptr[row], ptr[row + 1], lane, col, coff, [&](int k) { return val[k]; },
+                [&](int c) { return p[c]; }, [&](double v, double x) { s += v * x; });
         // every lane of the warp takes part in the shuffles (rows past n contribute 0)
         for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (row < n && lane == 0) {
@@ -256,7 +253,9 @@ __global__ void __launch_bounds__(kB) k_spmv32_dot(int n, const int* __restrict_
         const int row = base + threadIdx.x / LPR;
         float s = 0.f;
         if (row < n)
-            for (int k = ptr[row] + lane; k < ptr[row + 1]; k += LPR) s = fmaf(val[k], p[colOf<REL>(row, k, col, coff)], s);
+            dev::rowMac<LPR, kUnroll, REL>(
+                row, ptr[row], ptr[row + 1], lane, col, coff, [&](int k) { return val[k]; },
+                [&](int c) { return p[c]; }, [&](float v, float x) { s = fmaf(v, x, s); });
         for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (row < n && lane == 0) {
             t[row] = s;
@@ -351,10 +350,9 @@ __global__ void __launch_bounds__(kB) k_resid_df(int n, const int* __restrict__ 
         const int row = base + threadIdx.x / LPR;
         Dot2 acc;
         if (row < n)
-            for (int k = ptr[row] + lane; k < ptr[row + 1]; k += LPR) {
-                const int c = colOf<REL>(row, k, col, coff);
-                acc.mac(df32(hi[k], lo[k]), df32(xhi[c], xlo[c]));
-            }
+            dev::rowMac<LPR, kUnroll, REL>(
+                row, ptr[row], ptr[row + 1], lane, col, coff, [&](int k) { return df32(hi[k], lo[k]); },
+                [&](int c) { return df32(xhi[c], xlo[c]); }, [&](df32 v, df32 x) { acc.mac(v, x); });
         df32 y = acc.result();
         for (int o = LPR / 2; o > 0; o >>= 1) {
             df32 oth(__shfl_xor_sync(0xffffffffu, y.hi, o), __shfl_xor_sync(0xffffffffu, y.lo, o));

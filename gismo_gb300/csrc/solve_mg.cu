@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <random>
 #include <stdexcept>
@@ -292,6 +293,9 @@ void Context::mgRun(const gsgpu_solver_opts& o, gsgpu_solve_info& info, bool mix
             if (hs.done) break;
         }
         mgCoarseIters = std::min(1000, std::max(1, hs.iters + std::max(4, hs.iters / 8)));
+        if (std::getenv("GSGPU_MG_DEBUG"))
+            fprintf(stderr, "[mg] coarse n %d probe iters %d done %d rel %.3e cap %d\n", C.n, hs.iters, hs.done,
+                    hs.bnorm > 0 ? 0.0 : 0.0, mgCoarseIters);
         mgCoarseTol = prm.coarse_tol;
     }
     prm.coarse_iters = mgCoarseIters;

@@ -1,0 +1,44 @@
+// Row products of the CSR SpMV-type kernels: the LPR-strided share of sum_k A(row, col_k) x[col_k]
+// taken by one lane. The loop is unrolled U times and issues all U (value, column) loads before
+// the U dependent x loads, so each lane keeps U independent load chains in flight. With a single
+// chain per lane the kernels wait on load latency instead of filling HBM (measured: 31% of DRAM
+// peak on a 512-patch matrix with 32-bit column indices). The accumulation order is the plain
+// k = kb+lane, kb+lane+LPR, ... order, so results do not depend on U.
+#pragma once
+
+#include <cstdint>
+
+namespace gsgpu {
+namespace dev {
+
+// column of CSR slot k: absolute (col) or relative to the row (coff, banded patterns)
+template <bool REL>
+__device__ __forceinline__ int csrCol(int row, int k, const int* __restrict__ col, const int16_t* __restrict__ coff) {
+    if (REL) return row + int(coff[k]);
+    return col[k];
+}
+
+// fv(k): matrix value of slot k; fx(c): vector entry c; fm(v, x): accumulate v * x
+template <int LPR, int U, bool REL, class FV, class FX, class FM>
+__device__ __forceinline__ void rowMac(int row, int kb, int ke, int lane, const int* __restrict__ col,
+                                       const int16_t* __restrict__ coff, FV fv, FX fx, FM fm) {
+    int k = kb + lane;
+    for (; k + (U - 1) * LPR < ke; k += U * LPR) {
+        decltype(fv(0)) v[U];
+        int c[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            v[u] = fv(k + u * LPR);
+            c[u] = csrCol<REL>(row, k + u * LPR, col, coff);
+        }
+        decltype(fx(0)) xv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) xv[u] = fx(c[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u) fm(v[u], xv[u]);
+    }
+    for (; k < ke; k += LPR) fm(fv(k), fx(csrCol<REL>(row, k, col, coff)));
+}
+
+}  // namespace dev
+}  // namespace gsgpu
