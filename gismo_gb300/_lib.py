@@ -13,7 +13,8 @@ EXPORTS = [
     "gsgpu_create", "gsgpu_destroy", "gsgpu_last_error", "gsgpu_set_problem", "gsgpu_refresh", "gsgpu_set_coefs",
     "gsgpu_assemble", "gsgpu_sizes", "gsgpu_matrix_csr", "gsgpu_rhs", "gsgpu_fixed_dofs", "gsgpu_dof_map",
     "gsgpu_solve", "gsgpu_l2_error", "gsgpu_min_jacobian", "gsgpu_assemble_times", "gsgpu_stream",
-    "gsgpu_set_profiling", "gsgpu_spmv_stats", "gsgpu_cg_jacobi_noalloc",
+    "gsgpu_set_profiling", "gsgpu_spmv_stats", "gsgpu_cg_jacobi_noalloc", "gsgpu_set_batch", "gsgpu_batch_info",
+    "gsgpu_batch_l2_error",
 ]
 
 OK, ERR_INVALID, ERR_CUDA, ERR_BUDGET, ERR_NOT_CONVERGED, ERR_JACOBIAN, ERR_STATE, ERR_TIMEOUT = range(8)
@@ -79,6 +80,9 @@ def lib() -> C.CDLL:
         L.gsgpu_dof_map.argtypes = [vp, vp]
         L.gsgpu_solve.argtypes = [vp, C.POINTER(SolverOpts), vp, C.POINTER(SolveInfo)]
         L.gsgpu_l2_error.argtypes = [vp, C.POINTER(C.c_double)]
+        L.gsgpu_set_batch.argtypes = [vp, C.c_int, vp]
+        L.gsgpu_batch_info.argtypes = [vp, vp, vp, vp]
+        L.gsgpu_batch_l2_error.argtypes = [vp, vp]
         L.gsgpu_min_jacobian.argtypes = [vp, C.POINTER(C.c_double)]
         L.gsgpu_assemble_times.argtypes = [vp, vp]
         L.gsgpu_stream.argtypes = [vp, C.POINTER(vp)]

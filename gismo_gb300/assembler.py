@@ -146,6 +146,12 @@ class GpuPoissonAssembler:
         self._check(self.L.gsgpu_dof_map(self.h, out.ctypes.data))
         return out
 
+    def l2_error(self) -> float:
+        """gsField::distanceL2 of the last solution against the manufactured solution."""
+        v = C.c_double()
+        self._check(self.L.gsgpu_l2_error(self.h, C.byref(v)))
+        return v.value
+
     def min_jacobian(self) -> float:
         v = C.c_double()
         self._check(self.L.gsgpu_min_jacobian(self.h, C.byref(v)))
@@ -186,3 +192,49 @@ class GpuPoissonAssembler:
             self._check(rc)
         return x, dict(iterations=info.iterations, relres=info.relres, refinements=info.refinements,
                        t_solve_ms=info.t_solve_ms, converged=(rc == _lib.OK))
+
+
+class GpuPoissonBatch(GpuPoissonAssembler):
+    """A batch of independent single-patch problems in one context: what G+Smo runs as one
+    gsPoissonAssembler + gsConjugateGradient per problem, assembled by the same launches and solved
+    by a segmented CG with per-problem scalars and stopping tests (include/gsgpu.h gsgpu_set_batch)."""
+
+    def __init__(self, problems, device: int = 0, refresh: bool = True):
+        self.L = _lib.lib()
+        self.problems = list(problems)
+        self.prob = None
+        self.h = C.c_void_p()
+        rc = self.L.gsgpu_create(C.byref(self.h), device)
+        if rc != _lib.OK:
+            raise GsGpuError(rc, "could not create a context on CUDA device %d" % device)
+        self._packed = [PackedProblem(p) for p in self.problems]
+        arr = (_CProblem * len(self._packed))(*[pp.struct for pp in self._packed])
+        self._structs = arr
+        self._check(self.L.gsgpu_set_batch(self.h, len(self._packed), C.cast(arr, C.c_void_p)))
+        if refresh:
+            self.refresh()
+
+    def offsets(self) -> np.ndarray:
+        out = np.zeros(len(self.problems) + 1, np.int32)
+        self._check(self.L.gsgpu_batch_info(self.h, out.ctypes.data, None, None))
+        return out
+
+    def solve(self, tol: float = 1e-10, max_iters: int = 1000, precision: str = "fp64", inner_tol: float = 1e-5,
+              download: bool = True, **_unused):
+        """Per problem: solution, iterations and relative residual (info['per_problem'])."""
+        x, info = super().solve(tol=tol, max_iters=max_iters, method="jacobi", precision=precision,
+                                inner_tol=inner_tol, download=download)
+        n = len(self.problems)
+        its = np.zeros(n, np.int32)
+        rr = np.zeros(n, np.float64)
+        self._check(self.L.gsgpu_batch_info(self.h, None, its.ctypes.data, rr.ctypes.data))
+        info["per_problem"] = dict(iterations=its, relres=rr)
+        if download:
+            off = self.offsets()
+            x = [x[off[j]:off[j + 1]] for j in range(n)]
+        return x, info
+
+    def l2_errors(self) -> np.ndarray:
+        out = np.zeros(len(self.problems), np.float64)
+        self._check(self.L.gsgpu_batch_l2_error(self.h, out.ctypes.data))
+        return out

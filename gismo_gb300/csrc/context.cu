@@ -112,6 +112,7 @@ void Context::refresh() {
     buildDofMap(pd, map);
     buildLayout(pd, L);
     buildPattern(pd, map, L, pat, 0);
+    if (batch) segRow = segmentRows(pd, map);
     if (device < 0) {  // host-only context: the plan, no device buffers
         refreshed = true;
         return;
@@ -126,10 +127,16 @@ void Context::refresh() {
         diag[r] = pat.ptr[r] + int(f - b);
     }
     upload(arena, dPatches, L.dev, stream);
-    std::vector<dev::FieldConst<double>> fc64(1, dev::fieldConst<double>(pd.fields));
-    upload(arena, dFields, fc64, stream);
-    std::vector<dev::FieldConst<df32>> fcdf(1, dev::fieldConst<df32>(pd.fields));
-    upload(arena, dFieldsDf, fcdf, stream);
+    {
+        std::vector<dev::FieldConst<double>> fc64;
+        std::vector<dev::FieldConst<df32>> fcdf;
+        for (const FieldParams& F : pd.fieldTable()) {
+            fc64.push_back(dev::fieldConst<double>(F));
+            fcdf.push_back(dev::fieldConst<df32>(F));
+        }
+        upload(arena, dFields, fc64, stream);
+        upload(arena, dFieldsDf, fcdf, stream);
+    }
     {
         std::vector<df32> w(L.wq.size());
         for (size_t i = 0; i < w.size(); ++i) w[i] = df32(L.wq[i]);
@@ -168,6 +175,8 @@ void Context::refresh() {
     upload(arena, dFband, pat.fband.empty() ? std::vector<uint32_t>(1, 0) : pat.fband, stream);
     upload(arena, dFbidx, pat.fbidx.empty() ? std::vector<uint32_t>(1, 0) : pat.fbidx, stream);
     upload(arena, dDiag, diag, stream);
+    upload(arena, dIndex, map.index, stream);
+    if (batch) batchSetup();
     {
         // banded patterns (single patches) store columns as 16-bit offsets from the row
         bool fits = true;
@@ -369,6 +378,43 @@ void Context::assemble(int precision) {
     if (!(detMin > 0.0)) throw JacobianError("geometry map has det J <= 0 at a quadrature point");
 }
 
+// gsField::distanceL2 of the last solution: the geometry stages are re-run in FP64 (after a
+// mixed-precision assembly their buffers hold double-float values), then one quadrature kernel
+std::vector<double> Context::l2PerPatch() {
+    if (!solved) throw StateError("l2_error() before solve()");
+    cudaStream_t s = stream;
+    // after a mixed assembly the geometry table holds double-float values: rebuild it in FP64
+    launch::basisTables(dGtabJobs, (long long)L.gtabjobs.size(), dGknots, dGtab, s);
+    launch::basisTables(dTabJobs, (long long)L.tabjobs.size(), dKnots, dTab, s);
+    launch::geoStage1<double>(dPatches, tabGeo1.d, (long long)tabGeo1.h.size(), dCoefs, dGtab, dIbuf, dY1, s);
+    if (pd.dim == 3)
+        launch::geoStage2<double>(dPatches, tabGeo2.d, (long long)tabGeo2.h.size(), dY1, dGtab, dIbuf, dY2, s);
+    const long long nlocal = (long long)map.index.size();
+    const long long nblk = (long long)tabPoint.h.size();
+    double* coef = nullptr;
+    double* part = nullptr;
+    allocN(arena, coef, nlocal);
+    allocN(arena, part, nblk);
+    launch::solutionCoefs(nlocal, dIndex, map.freeSize, dX, dDdof, coef, s);
+    launch::l2Partials(dPatches, tabPoint.d, nblk, dFields, dY1, dY2, dGtab, dIbuf, dWq, dTab, coef, part, s);
+    std::vector<double> h(nblk);
+    GSGPU_CUDA_TRY(cudaGetLastError());
+    GSGPU_CUDA_TRY(cudaMemcpyAsync(h.data(), part, nblk * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    arena.release(coef);
+    arena.release(part);
+    // per patch, in block order (the blocks of a patch are contiguous in the table)
+    std::vector<double> acc(pd.patches.size(), 0.0);
+    for (long long b = 0; b < nblk; ++b) acc[size_t(tabPoint.h[size_t(b)].patch)] += h[size_t(b)];
+    return acc;
+}
+
+double Context::l2Error() {
+    double acc = 0.0;
+    for (double v : l2PerPatch()) acc += v;
+    return std::sqrt(acc);
+}
+
 void Context::times(double* ms) {
     float t[6];
     for (int i = 0; i < 6; ++i) GSGPU_CUDA_TRY(cudaEventElapsedTime(&t[i], ev[i], ev[i + 1]));
@@ -383,6 +429,8 @@ void Context::dropGraphs() {
     if (gexecFp64) cudaGraphExecDestroy(gexecFp64);
     if (gexecMixed) cudaGraphExecDestroy(gexecMixed);
     if (gexecMg) cudaGraphExecDestroy(gexecMg);
+    for (cudaGraphExec_t& g : gexecSeg)
+        if (g) cudaGraphExecDestroy(g), g = nullptr;
     gexecFp64 = gexecMixed = gexecMg = nullptr;
     gexecMgKey = MgGraphKey();
 }
@@ -400,6 +448,7 @@ Context Context::reset(Context&& c) {
     for (int i = 0; i < 8; ++i) n.ev[i] = c.ev[i];
     n.pd = std::move(c.pd);
     n.hasProblem = c.hasProblem;
+    n.batch = c.batch;
     n.arena.budget = c.arena.budget;
     c.stream = nullptr;
     for (int i = 0; i < 8; ++i) c.ev[i] = nullptr;
@@ -450,6 +499,10 @@ int Context::lanesPerRow(bool fp64) const {
 
 void Context::solve(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
     if (!assembled) throw StateError("solve() before assemble()");
+    if (batch) {
+        solveBatch(o, info);
+        return;
+    }
     if (o.method == GSGPU_SOLVER_CG_MG) {
         if (o.precision == GSGPU_PREC_MIXED && assembledPrecision != kMixed)
             throw StateError("mixed-precision solve needs assemble(GSGPU_PREC_MIXED)");
@@ -754,6 +807,47 @@ int gsgpu_set_problem(gsgpu_context* ctx, const gsgpu_problem* prob) {
         ctx->c = gsgpu::Context::reset(std::move(ctx->c));
         ctx->c.pd = std::move(pd);
         ctx->c.hasProblem = true;
+        ctx->c.batch = false;
+    });
+}
+
+int gsgpu_set_batch(gsgpu_context* ctx, int count, const gsgpu_problem* problems) {
+    return guarded(ctx, [&] {
+        gsgpu::ProblemDesc pd;
+        gsgpu::batchFromC(count, problems, pd);
+        if (ctx->c.device >= 0) {
+            ctx->c.dropGraphs();
+            ctx->c.arena.releaseAll();
+        }
+        ctx->c = gsgpu::Context::reset(std::move(ctx->c));
+        ctx->c.pd = std::move(pd);
+        ctx->c.hasProblem = true;
+        ctx->c.batch = true;
+    });
+}
+
+int gsgpu_batch_info(gsgpu_context* ctx, int* offsets, int* iterations, double* relres) {
+    return guarded(ctx, [&] {
+        auto& c = ctx->c;
+        if (!c.batch) throw gsgpu::StateError("batch_info() on a context without a batch");
+        if (!c.refreshed) throw gsgpu::StateError("batch_info() before refresh()");
+        if (offsets) std::copy(c.segRow.begin(), c.segRow.end(), offsets);
+        if (iterations || relres) {
+            if (!c.solved) throw gsgpu::StateError("batch_info() iterations before solve()");
+            for (size_t j = 0; j < c.segLast.size(); ++j) {
+                if (iterations) iterations[j] = c.segLast[j].total;
+                if (relres) relres[j] = c.segLast[j].relres;
+            }
+        }
+    });
+}
+
+int gsgpu_batch_l2_error(gsgpu_context* ctx, double* err) {
+    if (!err) return GSGPU_ERR_INVALID;
+    return guarded(ctx, [&] {
+        if (!ctx->c.batch) throw gsgpu::StateError("batch_l2_error() on a context without a batch");
+        const std::vector<double> sq = ctx->c.l2PerPatch();
+        for (size_t j = 0; j < sq.size(); ++j) err[j] = std::sqrt(sq[j]);
     });
 }
 
@@ -845,10 +939,8 @@ int gsgpu_solve(gsgpu_context* ctx, const gsgpu_solver_opts* opts, double* x, gs
 }
 
 int gsgpu_l2_error(gsgpu_context* ctx, double* err) {
-    return guarded(ctx, [&] {
-        (void)err;
-        throw std::invalid_argument("l2_error is not available in this build");
-    });
+    if (!err) return GSGPU_ERR_INVALID;
+    return guarded(ctx, [&] { *err = ctx->c.l2Error(); });
 }
 
 int gsgpu_stream(gsgpu_context* ctx, void** stream) {

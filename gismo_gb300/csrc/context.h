@@ -11,6 +11,7 @@
 #include "../../include/gsgpu.h"
 #include "gsgpu_internal.h"
 #include "device_funcs.cuh"
+#include "kernels_batch.h"
 #include "kernels_mg.h"
 #include "kernels_solve.h"
 #include "mg_plan.h"
@@ -91,6 +92,9 @@ namespace launch {
 void coefsToSoa(const DevPatch* P, const BlkEnt* tab, long long nblk, const double* raw, double* soa, cudaStream_t s);
 }
 
+// free-dof row offsets of the problems of a batch (one patch per problem)
+std::vector<int> segmentRows(const ProblemDesc& pd, const DofMap& map);
+
 struct Context {
     int device = -1;
     cudaStream_t stream = nullptr;
@@ -123,6 +127,7 @@ struct Context {
     uint32_t *dSrc = nullptr, *dOvfPtr = nullptr, *dOvfIdx = nullptr, *dLptr = nullptr, *dLidx = nullptr,
              *dFptr = nullptr, *dFband = nullptr, *dFbidx = nullptr;
     double *dVal = nullptr, *dRhs = nullptr, *dDdof = nullptr;
+    int* dIndex = nullptr;  // dof map (patch-local -> global), for the L2 error
     unsigned long long* dDetKey = nullptr;
     // mixed precision: df32 copies of the small inputs, the split CSR values and FP32 vectors
     df32 *dCoefsDf = nullptr, *dWqDf = nullptr;
@@ -155,6 +160,22 @@ struct Context {
     void mgSetup(int levels);
     void mgAssemble(bool mixed);
     void solveMG(const gsgpu_solver_opts& o, gsgpu_solve_info& info);
+    double l2Error();
+    std::vector<double> l2PerPatch();  // squared L2 error per patch
+    // batches of independent problems (one patch each): segment = problem
+    bool batch = false;
+    std::vector<int> segRow;  // free-dof offsets per problem (nseg + 1)
+    std::vector<int> segSpH, segVH;
+    Tab tabSegSp, tabSegV;
+    int *dSegRow = nullptr, *dSegSp = nullptr, *dSegV = nullptr, *dSegDone = nullptr;
+    double *dSegPartSp = nullptr, *dSegPartV0 = nullptr, *dSegPartV1 = nullptr;
+    SegState *dSegSt = nullptr, *dSegOuter = nullptr;
+    cudaGraphExec_t gexecSeg[2] = {nullptr, nullptr};
+    std::vector<SegState> segLast;
+    void batchSetup();
+    void solveBatch(const gsgpu_solver_opts& o, gsgpu_solve_info& info);
+    template <typename T>
+    void segRun(const SegCg<T>& B, cudaGraphExec_t& exec, int maxit);
     template <typename T>
     void mgRun(const gsgpu_solver_opts& o, gsgpu_solve_info& info, bool mixed);
     // profiling of the solver's SpMV launches

@@ -247,21 +247,17 @@ GS_HD void fields(const FieldConst<R>& F, const R* x, R& kappa, R& f) {
     f = kappa * (lap - F.alpha * dot);
 }
 
-// point-wise step: last geometry stage, metric and coefficient fields.
-// C^{ab} = w kappa |det J| (J^-1 J^-T)_{ab} = w kappa / |det J| sum_m cof_{ma} cof_{mb},
-// L = w |det J| f.  Component order 3D: 00 01 02 11 12 22 ; 2D: 00 01 11.
-// Returns det J.
+// last geometry stage at quadrature point `item` of patch D: physical point x and Jacobian J
+// (J[m][k] = d x_m / d xi_k) from the stage-1/2 partial contractions
 template <typename R>
-GS_HD double pointStep(const DevPatch& D, const FieldConst<R>& F, long long item, const R* __restrict__ Y1,
-                       const R* __restrict__ Y2, const R* __restrict__ gtab, const int* __restrict__ ibuf,
-                       const R* __restrict__ wq, R* __restrict__ C, R* __restrict__ Lf) {
+GS_HD void pointMap(const DevPatch& D, long long item, const R* __restrict__ Y1, const R* __restrict__ Y2,
+                    const R* __restrict__ gtab, const int* __restrict__ ibuf, R x[3], R J[3][3]) {
     const int d = D.dim;
     const int Q0 = D.Q[0], Q1 = D.Q[1];
     const int g0 = int(item % Q0);
     long long r = item / Q0;
     const int g1 = int(r % Q1);
     const int g2 = int(r / Q1);
-    R x[3], J[3][3];
     if (d == 3) {
         const int gp = D.gp[2];
         const int f2 = ibuf[D.gqoff[2] + g2];
@@ -305,6 +301,24 @@ GS_HD double pointStep(const DevPatch& D, const FieldConst<R>& F, long long item
             J[m][1] = c;
         }
     }
+}
+
+// point-wise step: last geometry stage, metric and coefficient fields.
+// C^{ab} = w kappa |det J| (J^-1 J^-T)_{ab} = w kappa / |det J| sum_m cof_{ma} cof_{mb},
+// L = w |det J| f.  Component order 3D: 00 01 02 11 12 22 ; 2D: 00 01 11.
+// Returns det J.
+template <typename R>
+GS_HD double pointStep(const DevPatch& D, const FieldConst<R>& F, long long item, const R* __restrict__ Y1,
+                       const R* __restrict__ Y2, const R* __restrict__ gtab, const int* __restrict__ ibuf,
+                       const R* __restrict__ wq, R* __restrict__ C, R* __restrict__ Lf) {
+    const int d = D.dim;
+    const int Q0 = D.Q[0], Q1 = D.Q[1];
+    const int g0 = int(item % Q0);
+    long long r = item / Q0;
+    const int g1 = int(r % Q1);
+    const int g2 = int(r / Q1);
+    R x[3], J[3][3];
+    pointMap<R>(D, item, Y1, Y2, gtab, ibuf, x, J);
     R w = wq[D.qoff[0] + g0] * wq[D.qoff[1] + g1];
     if (d == 3) w = w * wq[D.qoff[2] + g2];
     R kappa, f;

@@ -21,6 +21,7 @@ constexpr int kMaxDim = 3;
 
 struct DevPatch {
     int dim;
+    int field_id;  // index of the patch's closed-form field constants (batches of independent problems)
     int p[3], n[3], E[3], q[3], Q[3], W[3];
     int gp[3], gn[3];
     long long ngeo;   // geometry control points

@@ -52,6 +52,14 @@ void rhsRows(int n, const double* lvec, const uint32_t* lptr, const uint32_t* li
              const uint32_t* fptr, const uint32_t* fband, const uint32_t* fbidx, const double* ddof, double* rhs,
              cudaStream_t s);
 
+// discrete L2 error: solution coefficients per patch-local dof, then per-block partial sums of
+// (u_h - u)^2 w |det J| over the quadrature points (tabPoint blocks)
+void solutionCoefs(long long nlocal, const int* index, int nfree, const double* x, const double* ddof, double* coef,
+                   cudaStream_t s);
+void l2Partials(const DevPatch* P, const BlkEnt* tab, long long nblk, const dev::FieldConst<double>* F,
+                const double* Y1, const double* Y2, const double* gtab, const int* ibuf, const double* wq,
+                const double* btab, const double* coef, double* part, cudaStream_t s);
+
 // order-preserving uint64 key of a double (for atomicMin over signed values)
 inline unsigned long long detKeyInit() { return ~0ULL; }
 double detKeyDecode(unsigned long long key);

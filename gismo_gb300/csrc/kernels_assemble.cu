@@ -70,16 +70,16 @@ __global__ void __launch_bounds__(kBlock) k_point(const DevPatch* __restrict__ P
                                                   R* __restrict__ C, R* __restrict__ Lf,
                                                   unsigned long long* __restrict__ detkey) {
     __shared__ dev::FieldConst<R> sF;
-    // stage the coefficient parameters in shared memory (uniform across the block)
+    const BlkEnt be = tab[blockIdx.x];
+    const DevPatch& D = P[be.patch];
+    // stage the patch's coefficient parameters in shared memory (uniform across the block)
     {
         const int nw = int(sizeof(dev::FieldConst<R>) / sizeof(int));
-        const int* src = reinterpret_cast<const int*>(F);
+        const int* src = reinterpret_cast<const int*>(F + D.field_id);
         int* dst = reinterpret_cast<int*>(&sF);
         for (int k = threadIdx.x; k < nw; k += blockDim.x) dst[k] = src[k];
     }
     __syncthreads();
-    const BlkEnt be = tab[blockIdx.x];
-    const DevPatch& D = P[be.patch];
     const long long item = be.base + threadIdx.x;
     unsigned long long key = ~0ULL;
     if (item < D.nq) key = detKey(dev::pointStep<R>(D, sF, item, Y1, Y2, gtab, ibuf, wq, C, Lf));

@@ -229,6 +229,7 @@ void buildLayout(const ProblemDesc& pd, Layout& L) {
     for (const HostPatch& P : pd.patches) {
         DevPatch D{};
         D.dim = d;
+        D.field_id = pd.pfields.empty() ? 0 : P.field;
         D.ngeo = 1;
         D.nq = 1;
         D.ndof = 1;
@@ -589,7 +590,7 @@ void dirichletValues(const ProblemDesc& pd, const DofMap& map, std::vector<doubl
             xi[dir] = fixv;
             geoEvalHost(P, xi, x);
             double kap, ff, u;
-            evalFields(pd.fields, x, kap, ff, u);
+            evalFields(pd.fieldsOf(pd.dsides[si]), x, kap, ff, u);
             f[i] = u;
         }
         // tensor collocation solve, one direction at a time (banded LU with partial pivoting)
@@ -715,6 +716,37 @@ void problemFromC(const void* ptr, ProblemDesc& pd) {
     F.ufreq = pr->ufreq;
     pd.quA = pr->quA;
     pd.quB = pr->quB;
+}
+
+void batchFromC(int count, const void* ptr, ProblemDesc& pd) {
+    const gsgpu_problem* pr = static_cast<const gsgpu_problem*>(ptr);
+    if (!pr || count < 1) throw std::invalid_argument("batch: count must be >= 1");
+    pd = ProblemDesc();
+    int off = 0;
+    for (int j = 0; j < count; ++j) {
+        ProblemDesc one;
+        problemFromC(&pr[j], one);
+        if (one.patches.size() != 1 || !one.ifaces.empty())
+            throw std::invalid_argument("batch: every problem must be a single patch without interfaces");
+        if (j == 0) {
+            pd.dim = one.dim;
+            pd.quA = one.quA;
+            pd.quB = one.quB;
+            pd.fields = one.fields;
+        } else if (one.dim != pd.dim || one.quA != pd.quA || one.quB != pd.quB) {
+            throw std::invalid_argument("batch: dimension and quadrature rule must agree across problems");
+        }
+        HostPatch P = std::move(one.patches[0]);
+        P.field = j;
+        P.offset = off;
+        off += P.ndofs;
+        pd.patches.push_back(std::move(P));
+        for (size_t i = 0; i < one.dsides.size(); i += 2) {
+            pd.dsides.push_back(j);
+            pd.dsides.push_back(one.dsides[i + 1]);
+        }
+        pd.pfields.push_back(one.fields);
+    }
 }
 
 void blockTable(const std::vector<long long>& work, int block, std::vector<BlkEnt>& tab) {

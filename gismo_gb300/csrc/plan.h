@@ -30,6 +30,7 @@ struct Basis1D {
 
 struct HostPatch {
     int dim = 2;
+    int field = 0;  // index into ProblemDesc::pfields (0 when the problem has one field set)
     Basis1D b[3], g[3];
     std::vector<double> coefs;  // ngeo x dim, row-major
     int nd[3] = {1, 1, 1};
@@ -43,8 +44,16 @@ struct ProblemDesc {
     std::vector<int> ifaces;    // 4 per interface
     std::vector<int> dsides;    // 2 per Dirichlet side
     FieldParams fields{};
+    // batches of independent problems: one field set per problem (HostPatch::field indexes it);
+    // empty for a single problem, whose patches all use `fields`
+    std::vector<FieldParams> pfields;
     double quA = 1.0;
     int quB = 1;
+    const FieldParams& fieldsOf(int patch) const {
+        return pfields.empty() ? fields : pfields[size_t(patches[size_t(patch)].field)];
+    }
+    // the device field table: one entry per field set
+    std::vector<FieldParams> fieldTable() const { return pfields.empty() ? std::vector<FieldParams>(1, fields) : pfields; }
 };
 
 // gsDofMapper numbering (src/gsCore/gsDofMapper.cpp:99-344) for a list of patches
@@ -60,6 +69,9 @@ void buildDofMap(const ProblemDesc& pd, DofMap& map);
 // copy and validate a C-ABI problem description (include/gsgpu.h)
 struct ProblemC;
 void problemFromC(const void* gsgpu_problem_ptr, ProblemDesc& pd);
+// a batch of independent single-patch problems as one ProblemDesc (patch j = problem j, with its
+// own field set); quA/quB and the dimension must agree
+void batchFromC(int count, const void* gsgpu_problem_array, ProblemDesc& pd);
 
 // symbolic CSR + gather maps
 struct Pattern {

@@ -294,8 +294,8 @@ void Context::mgRun(const gsgpu_solver_opts& o, gsgpu_solve_info& info, bool mix
         }
         mgCoarseIters = std::min(1000, std::max(1, hs.iters + std::max(4, hs.iters / 8)));
         if (std::getenv("GSGPU_MG_DEBUG"))
-            fprintf(stderr, "[mg] coarse n %d probe iters %d done %d rel %.3e cap %d\n", C.n, hs.iters, hs.done,
-                    hs.bnorm > 0 ? 0.0 : 0.0, mgCoarseIters);
+            fprintf(stderr, "[mg] coarsest level: %d dofs, probe %d iterations (converged %d), cap %d\n", C.n, hs.iters,
+                    hs.done, mgCoarseIters);
         mgCoarseTol = prm.coarse_tol;
     }
     prm.coarse_iters = mgCoarseIters;

@@ -132,6 +132,22 @@ int gsgpu_solve(gsgpu_context* ctx, const gsgpu_solver_opts* opts, double* x, gs
 /* gsField::distanceL2 of the last solution against u (gsField.hpp:23-41) */
 int gsgpu_l2_error(gsgpu_context* ctx, double* err);
 
+/* Batches of independent problems. No counterpart in the reference, where each problem is its own
+ * gsPoissonAssembler + gsConjugateGradient run. `count` single-patch problems (each with its own
+ * geometry, degree, knots and closed-form fields; quA/quB shared) form one block-diagonal system
+ * that the same launches assemble as a multipatch problem; gsgpu_solve then runs a segmented
+ * Jacobi-PCG whose scalars, stopping test and iteration count are per problem, i.e. one
+ * gsConjugateGradient per problem. The free dofs of problem j are rows [offsets[j], offsets[j+1])
+ * of the batch system, in problem order; refresh / assemble / solve / matrix_csr / rhs / dof_map
+ * act on the whole batch. GSGPU_PREC_MIXED solves each problem by an FP32 segmented PCG inside an
+ * iterative refinement whose residual b - A x (FP64 operator, FP64 x) and norms stay FP64. */
+int gsgpu_set_batch(gsgpu_context* ctx, int count, const gsgpu_problem* problems);
+/* per problem: free-dof offsets (count + 1 values), iterations (inner FP32 iterations summed over
+ * the refinements in mixed precision) and relative residual of the last solve; any pointer may be NULL */
+int gsgpu_batch_info(gsgpu_context* ctx, int* offsets, int* iterations, double* relres);
+/* per problem: gsField::distanceL2 of the last solution (count values) */
+int gsgpu_batch_l2_error(gsgpu_context* ctx, double* err);
+
 /* Utilities with no counterpart in the reference. */
 /* the CUDA stream (cudaStream_t) all device work of the context is issued on */
 int gsgpu_stream(gsgpu_context* ctx, void** stream);

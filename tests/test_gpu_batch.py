@@ -1,0 +1,97 @@
+"""Batches of independent problems on the GPU (uneven degree and refinement, per-problem fields)
+against the CPU oracle run problem by problem, as the reference would run them.
+
+Bars: every problem's matrix and rhs block within 1e-12 relative of the oracle (floor 1e-14 of
+the row's largest entry); per-problem CG iteration counts within one of the oracle's; per-problem
+solutions within 1e-8 of the oracle's; per-problem L2 errors to 1e-9 of the oracle's quadrature of
+the same solution. Mixed precision: per-problem solution within 1e-8 (relative 2-norm) of a tightly
+converged FP64 batch solution, with the reported FP64 residual under the tolerance."""
+import numpy as np
+import pytest
+
+from gismo_gb300 import problems as P
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__ as g
+    g.build()
+
+
+@pytest.fixture(scope="module")
+def batch():
+    return P.patch_batch(count=48, seed=21, nmin=6, nmax=40)
+
+
+def _batch(probs):
+    from gismo_gb300.assembler import GpuPoissonBatch
+    return GpuPoissonBatch(probs, device=0)
+
+
+def test_batch_fp64_matches_oracle_per_problem(batch):
+    from oracle import oracle as O
+    B = _batch(batch)
+    B.assemble("fp64")
+    ptr, col, val = B.csr()
+    rhs = B.rhs()
+    off = B.offsets()
+    xs, info = B.solve(tol=1e-8, max_iters=5000)
+    assert info["converged"], info
+    its = info["per_problem"]["iterations"]
+    rr = info["per_problem"]["relres"]
+    l2 = B.l2_errors()
+    for j, pr in enumerate(batch):
+        o = O.OracleProblem(pr)
+        o.assemble()
+        optr, ocol, oval = o.csr()
+        a, b = off[j], off[j + 1]
+        k0, k1 = ptr[a], ptr[b]
+        assert np.array_equal(col[k0:k1] - a, ocol)
+        rowmax = np.maximum.reduceat(np.abs(oval), optr[:-1])
+        floor = np.repeat(rowmax, np.diff(optr)) * 1e-14
+        assert np.all(np.abs(val[k0:k1] - oval) <= 1e-12 * np.abs(oval) + floor), j
+        orhs = o.rhs()
+        assert np.abs(rhs[a:b] - orhs).max() <= 1e-12 * np.abs(orhs).max(), j
+        xo, it, _, _ = o.solve_cg(1e-8, 5000)
+        assert abs(int(its[j]) - it) <= 1, (j, its[j], it)
+        assert rr[j] < 1e-8
+        assert np.linalg.norm(xs[j] - xo) <= 1e-7 * np.linalg.norm(xo), j
+        ol2 = o.l2_error(xs[j])
+        assert abs(l2[j] - ol2) <= 1e-9 * ol2, (j, l2[j], ol2)
+    B.close()
+
+
+def test_batch_mixed_matches_fp64(batch):
+    B = _batch(batch)
+    B.assemble("fp64")
+    x64, i64 = B.solve(tol=1e-13, max_iters=20000)
+    assert i64["converged"], i64
+    B.assemble("mixed")
+    xm, im = B.solve(tol=1e-10, max_iters=20000, precision="mixed")
+    assert im["converged"], im
+    assert im["refinements"] >= 1
+    assert np.all(im["per_problem"]["relres"] < 1e-10)
+    K = B.matrix()
+    b = B.rhs()
+    off = B.offsets()
+    xcat = np.concatenate(xm)
+    for j in range(len(batch)):
+        err = np.linalg.norm(xm[j] - x64[j]) / np.linalg.norm(x64[j])
+        assert err <= 1e-8, (j, err)
+        a, c = off[j], off[j + 1]
+        # the reported residual is the true FP64 residual of the problem's block
+        r = b[a:c] - K[a:c] @ xcat
+        assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(b[a:c])
+    B.close()
+
+
+def test_batch_solve_is_repeatable(batch):
+    B = _batch(batch[:12])
+    B.assemble("mixed")
+    xa, ia = B.solve(tol=1e-9, precision="mixed")
+    xb, ib = B.solve(tol=1e-9, precision="mixed")
+    assert all(np.array_equal(u, v) for u, v in zip(xa, xb))
+    assert np.array_equal(ia["per_problem"]["iterations"], ib["per_problem"]["iterations"])
+    B.close()

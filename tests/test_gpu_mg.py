@@ -51,6 +51,7 @@ def test_mg_matches_reference_fixture():
     o.assemble()
     l2 = o.l2_error(x)
     assert abs(l2 - float(g["l2"])) <= 5e-4 * float(g["l2"])
+    assert abs(A.l2_error() - l2) <= 1e-9 * l2
     A.close()
 
 
