@@ -165,10 +165,8 @@ struct Context {
     // batches of independent problems (one patch each): segment = problem
     bool batch = false;
     std::vector<int> segRow;  // free-dof offsets per problem (nseg + 1)
-    std::vector<int> segSpH, segVH;
-    Tab tabSegSp, tabSegV;
-    int *dSegRow = nullptr, *dSegSp = nullptr, *dSegV = nullptr, *dSegDone = nullptr;
-    double *dSegPartSp = nullptr, *dSegPartV0 = nullptr, *dSegPartV1 = nullptr;
+    int *dSegRow = nullptr, *dRowSeg = nullptr, *dSegDone = nullptr;
+    double *dSegRc0 = nullptr, *dSegRc1 = nullptr;
     SegState *dSegSt = nullptr, *dSegOuter = nullptr;
     cudaGraphExec_t gexecSeg[2] = {nullptr, nullptr};
     std::vector<SegState> segLast;

@@ -1,9 +1,10 @@
 // sm_103a kernels of the segmented Jacobi-PCG over a batch of independent systems: one
 // gsConjugateGradient (src/gsSolver/gsConjugateGradient.hpp:19-84) per segment, with the
 // segment's scalars (rho, alpha, beta), ||b|| and stopping test kept apart, and all segments
-// advanced by the same launches. The kernels are persistent: a grid of at most 8 CTAs per SM walks
-// the (segment, first row) block tables, so converged segments cost one table read per block.
-// Dot products are per block partial sums in a fixed order, reduced per segment by one warp.
+// advanced by the same launches. The batch matrix is swept as one CSR matrix by row-parallel
+// grid-stride kernels (rows of converged segments are skipped after one rowSeg / done lookup);
+// dot products are per-row contributions summed per segment by one warp in a fixed order, so
+// the results do not depend on the launch shape.
 #include "context.h"
 #include "kernels_batch.h"
 #include "spmv_row.cuh"
@@ -12,51 +13,19 @@ namespace gsgpu {
 namespace {
 
 constexpr int kB = 256;
-constexpr int kGridCap = 8 * 152;
+constexpr int kGridCap = 8 * 152;  // 8 resident CTAs of 256 threads on each of the 152 SMs
+constexpr int kLanes = 8;          // lanes per CSR row in the SpMV kernels
 constexpr int kUnroll = 4;
 
-inline int gridFor(int entries) { return entries < 1 ? 1 : (entries < kGridCap ? entries : kGridCap); }
+inline int gridFor(long long items, int perBlock) {
+    const long long g = (items + perBlock - 1) / perBlock;
+    return int(g < 1 ? 1 : (g < kGridCap ? g : kGridCap));
+}
+inline int segGrid(int nseg) { return (nseg * 32 + kB - 1) / kB > 0 ? (nseg * 32 + kB - 1) / kB : 1; }
 
 __device__ __forceinline__ double warpSum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
-}
-
-// block sums of two values per thread into *o0, *o1 (fixed order); ends with a barrier so the
-// shared scratch can be reused by the next table entry
-__device__ __forceinline__ void blockSum2(double a, double b, double* o0, double* o1) {
-    __shared__ double ws[2][kB / 32];
-    a = warpSum(a);
-    b = warpSum(b);
-    if ((threadIdx.x & 31) == 0) {
-        ws[0][threadIdx.x >> 5] = a;
-        ws[1][threadIdx.x >> 5] = b;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s0 = 0.0, s1 = 0.0;
-        for (int w = 0; w < kB / 32; ++w) {
-            s0 += ws[0][w];
-            s1 += ws[1][w];
-        }
-        *o0 = s0;
-        if (o1) *o1 = s1;
-    }
-    __syncthreads();
-}
-
-// every thread gets sum(part[a..b))
-__device__ __forceinline__ double blockRange(const double* __restrict__ part, int a, int b) {
-    __shared__ double ws[kB / 32];
-    double v = 0.0;
-    for (int i = a + threadIdx.x; i < b; i += kB) v += part[i];
-    v = warpSum(v);
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
-    __syncthreads();
-    double s = 0.0;
-    for (int w = 0; w < kB / 32; ++w) s += ws[w];
-    __syncthreads();
-    return s;
 }
 
 // one warp sums part[a..b) (lane-strided, then a fixed shuffle tree)
@@ -64,6 +33,10 @@ __device__ __forceinline__ double warpRange(const double* __restrict__ part, int
     double v = 0.0;
     for (int i = a + lane; i < b; i += 32) v += part[i];
     return warpSum(v);
+}
+
+__device__ __forceinline__ bool rowActive(const int* __restrict__ rowSeg, const SegState* __restrict__ st, int row) {
+    return !st[rowSeg[row]].done;
 }
 
 template <typename T>
@@ -75,24 +48,16 @@ __global__ void __launch_bounds__(kB) k_seg_dinv(int n, const int* __restrict__ 
 
 template <typename T>
 __global__ void __launch_bounds__(kB) k_seg_init(SegCg<T> B) {
-    for (int e = blockIdx.x; e < B.nV; e += gridDim.x) {
-        const BlkEnt be = B.tabV[e];
-        const int s = be.patch;
-        double bb = 0.0, rz = 0.0;
-        if (!(B.outer && B.outer[s].done)) {
-            const int row = B.segRow[s] + int(be.base) + threadIdx.x;
-            if (row < B.segRow[s + 1]) {
-                const T bi = B.b[row];
-                B.x[row] = T(0);
-                B.r[row] = bi;
-                const T zi = B.dinv[row] * bi;
-                B.z[row] = zi;
-                B.p[row] = zi;
-                bb = double(bi) * double(bi);
-                rz = double(bi) * double(zi);
-            }
-        }
-        blockSum2(bb, rz, B.partV0 + e, B.partV1 + e);
+    for (int i = blockIdx.x * kB + threadIdx.x; i < B.n; i += gridDim.x * kB) {
+        if (B.outer && B.outer[B.rowSeg[i]].done) continue;
+        const T bi = B.b[i];
+        B.x[i] = T(0);
+        B.r[i] = bi;
+        const T zi = B.dinv[i] * bi;
+        B.z[i] = zi;
+        B.p[i] = zi;
+        B.rc0[i] = double(bi) * double(bi);
+        B.rc1[i] = double(bi) * double(zi);
     }
 }
 
@@ -101,13 +66,17 @@ __global__ void __launch_bounds__(kB) k_seg_init_seg(SegCg<T> B, double tol, int
     const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (s >= B.nseg) return;
-    const double bb = warpRange(B.partV0, B.segV[s], B.segV[s + 1], lane);
-    const double rz = warpRange(B.partV1, B.segV[s], B.segV[s + 1], lane);
+    const bool skip = B.outer && B.outer[s].done;
+    double bb = 0.0, rz = 0.0;
+    if (!skip) {
+        bb = warpRange(B.rc0, B.segRow[s], B.segRow[s + 1], lane);
+        rz = warpRange(B.rc1, B.segRow[s], B.segRow[s + 1], lane);
+    }
     if (lane == 0) {
         SegState& S = B.st[s];
-        const bool skip = B.outer && B.outer[s].done;
         S.bnorm = sqrt(bb);
         S.rho = rz;
+        S.alpha = 0.0;
         S.beta = 0.0;
         S.tol = tol;
         S.maxit = maxit;
@@ -118,53 +87,50 @@ __global__ void __launch_bounds__(kB) k_seg_init_seg(SegCg<T> B, double tol, int
     }
 }
 
+// t = A p on the rows of running segments; rc0 = t .* p
 template <typename T, bool REL>
 __global__ void __launch_bounds__(kB) k_seg_spmv(SegCg<T> B) {
-    const int lane = threadIdx.x % kBatchLanes;
-    for (int e = blockIdx.x; e < B.nSp; e += gridDim.x) {
-        const BlkEnt be = B.tabSp[e];
-        const int s = be.patch;
-        if (B.st[s].done) {
-            if (threadIdx.x == 0) B.partSp[e] = 0.0;
-            continue;
-        }
-        const int row = B.segRow[s] + int(be.base) + threadIdx.x / kBatchLanes;
-        const bool valid = row < B.segRow[s + 1];
+    constexpr int rpb = kB / kLanes;
+    const int lane = threadIdx.x % kLanes;
+    for (int base = blockIdx.x * rpb; base < B.n; base += gridDim.x * rpb) {
+        const int row = base + threadIdx.x / kLanes;
+        const bool act = row < B.n && rowActive(B.rowSeg, B.st, row);
         T acc = T(0);
-        if (valid)
-            dev::rowMac<kBatchLanes, kUnroll, REL>(
+        if (act)
+            dev::rowMac<kLanes, kUnroll, REL>(
                 row, B.ptr[row], B.ptr[row + 1], lane, B.col, B.coff, [&](int k) { return B.val[k]; },
                 [&](int c) { return B.p[c]; }, [&](T v, T x) { acc += v * x; });
-        for (int o = kBatchLanes / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        double c = 0.0;
-        if (valid && lane == 0) {
+        for (int o = kLanes / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (act && lane == 0) {
             B.t[row] = acc;
-            c = double(acc) * double(B.p[row]);
+            B.rc0[row] = double(acc) * double(B.p[row]);
         }
-        blockSum2(c, 0.0, B.partSp + e, nullptr);
     }
 }
 
 template <typename T>
+__global__ void __launch_bounds__(kB) k_seg_alpha(SegCg<T> B) {
+    const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (s >= B.nseg || B.st[s].done) return;
+    const double pAp = warpRange(B.rc0, B.segRow[s], B.segRow[s + 1], lane);
+    if (lane == 0) B.st[s].alpha = B.st[s].rho / pAp;
+}
+
+// x += alpha p; r -= alpha t; z = D^-1 r; rc0 = r .* r, rc1 = r .* z
+template <typename T>
 __global__ void __launch_bounds__(kB) k_seg_update(SegCg<T> B) {
-    for (int e = blockIdx.x; e < B.nV; e += gridDim.x) {
-        const BlkEnt be = B.tabV[e];
-        const int s = be.patch;
-        if (B.st[s].done) continue;
-        const double pAp = blockRange(B.partSp, B.segSp[s], B.segSp[s + 1]);
-        const T alpha = T(B.st[s].rho / pAp);
-        const int row = B.segRow[s] + int(be.base) + threadIdx.x;
-        double rr = 0.0, rz = 0.0;
-        if (row < B.segRow[s + 1]) {
-            B.x[row] += alpha * B.p[row];
-            const T ri = B.r[row] - alpha * B.t[row];
-            B.r[row] = ri;
-            const T zi = B.dinv[row] * ri;
-            B.z[row] = zi;
-            rr = double(ri) * double(ri);
-            rz = double(ri) * double(zi);
-        }
-        blockSum2(rr, rz, B.partV0 + e, B.partV1 + e);
+    for (int i = blockIdx.x * kB + threadIdx.x; i < B.n; i += gridDim.x * kB) {
+        const SegState& S = B.st[B.rowSeg[i]];
+        if (S.done) continue;
+        const T alpha = T(S.alpha);
+        B.x[i] += alpha * B.p[i];
+        const T ri = B.r[i] - alpha * B.t[i];
+        B.r[i] = ri;
+        const T zi = B.dinv[i] * ri;
+        B.z[i] = zi;
+        B.rc0[i] = double(ri) * double(ri);
+        B.rc1[i] = double(ri) * double(zi);
     }
 }
 
@@ -173,8 +139,8 @@ __global__ void __launch_bounds__(kB) k_seg_scalars(SegCg<T> B) {
     const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (s >= B.nseg || B.st[s].done) return;
-    const double rr = warpRange(B.partV0, B.segV[s], B.segV[s + 1], lane);
-    const double rz = warpRange(B.partV1, B.segV[s], B.segV[s + 1], lane);
+    const double rr = warpRange(B.rc0, B.segRow[s], B.segRow[s + 1], lane);
+    const double rz = warpRange(B.rc1, B.segRow[s], B.segRow[s + 1], lane);
     if (lane == 0) {
         SegState& S = B.st[s];
         S.iters += 1;
@@ -189,44 +155,35 @@ __global__ void __launch_bounds__(kB) k_seg_scalars(SegCg<T> B) {
 
 template <typename T>
 __global__ void __launch_bounds__(kB) k_seg_pupd(SegCg<T> B) {
-    for (int e = blockIdx.x; e < B.nV; e += gridDim.x) {
-        const BlkEnt be = B.tabV[e];
-        const int s = be.patch;
-        if (B.st[s].done) continue;
-        const T beta = T(B.st[s].beta);
-        const int row = B.segRow[s] + int(be.base) + threadIdx.x;
-        if (row < B.segRow[s + 1]) B.p[row] = B.z[row] + beta * B.p[row];
+    for (int i = blockIdx.x * kB + threadIdx.x; i < B.n; i += gridDim.x * kB) {
+        const SegState& S = B.st[B.rowSeg[i]];
+        if (S.done) continue;
+        B.p[i] = B.z[i] + T(S.beta) * B.p[i];
     }
 }
 
 // ---- iterative refinement (outer FP64) ----
 
+// r = b - (hi + lo) x on the rows of segments not yet converged; rc0 = r .* r
 template <bool REL>
 __global__ void __launch_bounds__(kB) k_ref_resid(SegCg<float> B, SegRefine R) {
-    const int lane = threadIdx.x % kBatchLanes;
-    for (int e = blockIdx.x; e < B.nSp; e += gridDim.x) {
-        const BlkEnt be = B.tabSp[e];
-        const int s = be.patch;
-        if (R.st[s].done) {
-            if (threadIdx.x == 0) B.partSp[e] = 0.0;
-            continue;
-        }
-        const int row = B.segRow[s] + int(be.base) + threadIdx.x / kBatchLanes;
-        const bool valid = row < B.segRow[s + 1];
+    constexpr int rpb = kB / kLanes;
+    const int lane = threadIdx.x % kLanes;
+    for (int base = blockIdx.x * rpb; base < B.n; base += gridDim.x * rpb) {
+        const int row = base + threadIdx.x / kLanes;
+        const bool act = row < B.n && rowActive(B.rowSeg, R.st, row);
         double acc = 0.0;
-        if (valid)
-            dev::rowMac<kBatchLanes, kUnroll, REL>(
+        if (act)
+            dev::rowMac<kLanes, kUnroll, REL>(
                 row, B.ptr[row], B.ptr[row + 1], lane, B.col, B.coff,
                 [&](int k) { return double(R.hi[k]) + double(R.lo[k]); }, [&](int c) { return R.x[c]; },
                 [&](double v, double x) { acc += v * x; });
-        for (int o = kBatchLanes / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        double c = 0.0;
-        if (valid && lane == 0) {
+        for (int o = kLanes / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (act && lane == 0) {
             const double ri = R.b[row] - acc;
             R.r[row] = ri;
-            c = ri * ri;
+            B.rc0[row] = ri * ri;
         }
-        blockSum2(c, 0.0, B.partSp + e, nullptr);
     }
 }
 
@@ -234,7 +191,7 @@ __global__ void __launch_bounds__(kB) k_ref_seg(SegCg<float> B, SegRefine R, dou
     const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (s >= B.nseg || R.st[s].done) return;
-    const double rr = warpRange(B.partSp, B.segSp[s], B.segSp[s + 1], lane);
+    const double rr = warpRange(B.rc0, B.segRow[s], B.segRow[s + 1], lane);
     if (lane == 0) {
         SegState& S = R.st[s];
         if (first) {
@@ -254,23 +211,13 @@ __global__ void __launch_bounds__(kB) k_ref_seg(SegCg<float> B, SegRefine R, dou
 }
 
 __global__ void __launch_bounds__(kB) k_ref_rhs(SegCg<float> B, SegRefine R) {
-    for (int e = blockIdx.x; e < B.nV; e += gridDim.x) {
-        const BlkEnt be = B.tabV[e];
-        const int s = be.patch;
-        if (R.st[s].done) continue;
-        const int row = B.segRow[s] + int(be.base) + threadIdx.x;
-        if (row < B.segRow[s + 1]) R.r32[row] = float(R.r[row]);
-    }
+    for (int i = blockIdx.x * kB + threadIdx.x; i < B.n; i += gridDim.x * kB)
+        if (rowActive(B.rowSeg, R.st, i)) R.r32[i] = float(R.r[i]);
 }
 
 __global__ void __launch_bounds__(kB) k_ref_correct(SegCg<float> B, SegRefine R) {
-    for (int e = blockIdx.x; e < B.nV; e += gridDim.x) {
-        const BlkEnt be = B.tabV[e];
-        const int s = be.patch;
-        if (R.st[s].done) continue;
-        const int row = B.segRow[s] + int(be.base) + threadIdx.x;
-        if (row < B.segRow[s + 1]) R.x[row] += double(R.d32[row]);
-    }
+    for (int i = blockIdx.x * kB + threadIdx.x; i < B.n; i += gridDim.x * kB)
+        if (rowActive(B.rowSeg, R.st, i)) R.x[i] += double(R.d32[i]);
 }
 
 __global__ void __launch_bounds__(kB) k_ref_count(SegCg<float> B, SegRefine R) {
@@ -290,17 +237,19 @@ void segDinv(const SegCg<T>& B, const int* diag, cudaStream_t s) {
 template <typename T>
 void segInit(const SegCg<T>& B, double tol, int maxit, cudaStream_t s) {
     GSGPU_CUDA_TRY(cudaMemsetAsync(B.ndone, 0, sizeof(int), s));
-    k_seg_init<T><<<gridFor(B.nV), kB, 0, s>>>(B);
-    k_seg_init_seg<T><<<(B.nseg * 32 + kB - 1) / kB, kB, 0, s>>>(B, tol, maxit);
+    k_seg_init<T><<<gridFor(B.n, kB), kB, 0, s>>>(B);
+    k_seg_init_seg<T><<<segGrid(B.nseg), kB, 0, s>>>(B, tol, maxit);
 }
 
 template <typename T>
 void segIteration(const SegCg<T>& B, cudaStream_t s) {
-    if (B.coff) k_seg_spmv<T, true><<<gridFor(B.nSp), kB, 0, s>>>(B);
-    else k_seg_spmv<T, false><<<gridFor(B.nSp), kB, 0, s>>>(B);
-    k_seg_update<T><<<gridFor(B.nV), kB, 0, s>>>(B);
-    k_seg_scalars<T><<<(B.nseg * 32 + kB - 1) / kB, kB, 0, s>>>(B);
-    k_seg_pupd<T><<<gridFor(B.nV), kB, 0, s>>>(B);
+    const int gs = gridFor(B.n, kB / kLanes);
+    if (B.coff) k_seg_spmv<T, true><<<gs, kB, 0, s>>>(B);
+    else k_seg_spmv<T, false><<<gs, kB, 0, s>>>(B);
+    k_seg_alpha<T><<<segGrid(B.nseg), kB, 0, s>>>(B);
+    k_seg_update<T><<<gridFor(B.n, kB), kB, 0, s>>>(B);
+    k_seg_scalars<T><<<segGrid(B.nseg), kB, 0, s>>>(B);
+    k_seg_pupd<T><<<gridFor(B.n, kB), kB, 0, s>>>(B);
 }
 
 void refineResidual(const SegCg<float>& B, const SegRefine& R, double tol, int maxref, int first, cudaStream_t s) {
@@ -309,17 +258,18 @@ void refineResidual(const SegCg<float>& B, const SegRefine& R, double tol, int m
         GSGPU_CUDA_TRY(cudaMemsetAsync(R.st, 0, sizeof(SegState) * size_t(B.nseg), s));
         GSGPU_CUDA_TRY(cudaMemsetAsync(R.ndone, 0, sizeof(int), s));
     }
-    if (B.coff) k_ref_resid<true><<<gridFor(B.nSp), kB, 0, s>>>(B, R);
-    else k_ref_resid<false><<<gridFor(B.nSp), kB, 0, s>>>(B, R);
-    k_ref_seg<<<(B.nseg * 32 + kB - 1) / kB, kB, 0, s>>>(B, R, tol, maxref, first);
+    const int gs = gridFor(B.n, kB / kLanes);
+    if (B.coff) k_ref_resid<true><<<gs, kB, 0, s>>>(B, R);
+    else k_ref_resid<false><<<gs, kB, 0, s>>>(B, R);
+    k_ref_seg<<<segGrid(B.nseg), kB, 0, s>>>(B, R, tol, maxref, first);
 }
 
 void refineRhs(const SegCg<float>& B, const SegRefine& R, cudaStream_t s) {
-    k_ref_rhs<<<gridFor(B.nV), kB, 0, s>>>(B, R);
+    k_ref_rhs<<<gridFor(B.n, kB), kB, 0, s>>>(B, R);
 }
 
 void refineCorrect(const SegCg<float>& B, const SegRefine& R, cudaStream_t s) {
-    k_ref_correct<<<gridFor(B.nV), kB, 0, s>>>(B, R);
+    k_ref_correct<<<gridFor(B.n, kB), kB, 0, s>>>(B, R);
 }
 
 void refineCount(const SegCg<float>& B, const SegRefine& R, cudaStream_t s) {

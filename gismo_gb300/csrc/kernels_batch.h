@@ -11,26 +11,18 @@ namespace gsgpu {
 
 // CG scalars and stopping state of one system of the batch
 struct SegState {
-    double rho, beta, bnorm, relres, tol;
+    double rho, alpha, beta, bnorm, relres, tol;
     int iters, maxit, done, total;  // done: 0 running, 1 converged, 2 reached maxit; total: iterations summed
 };
 
-// rows of segment s: [segRow[s], segRow[s+1]); tables of (segment, first row within the segment)
-// blocks: SpMV blocks of kBatchSpRows rows, vector blocks of kBatchVecRows rows
-constexpr int kBatchLanes = 8;
-constexpr int kBatchSpRows = 256 / kBatchLanes;
-constexpr int kBatchVecRows = 256;
-
+// The batch matrix is one CSR matrix (block diagonal, rows of segment s in [segRow[s], segRow[s+1]))
+// swept by row-parallel kernels; rowSeg maps a row to its segment. Dot products go through
+// per-row contributions (rc0, rc1) that one warp per segment sums in a fixed order.
 template <typename T>
 struct SegCg {
     int n = 0, nseg = 0;
-    const int* segRow = nullptr;
-    const BlkEnt* tabSp = nullptr;
-    const int* segSp = nullptr;  // first SpMV block of each segment (nseg + 1)
-    int nSp = 0;
-    const BlkEnt* tabV = nullptr;
-    const int* segV = nullptr;   // first vector block of each segment (nseg + 1)
-    int nV = 0;
+    const int* segRow = nullptr;  // nseg + 1
+    const int* rowSeg = nullptr;  // n
     const int* ptr = nullptr;
     const int* col = nullptr;
     const int16_t* coff = nullptr;
@@ -38,7 +30,7 @@ struct SegCg {
     const T* dinv = nullptr;
     const T* b = nullptr;
     T *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *t = nullptr;
-    double *partSp = nullptr, *partV0 = nullptr, *partV1 = nullptr;
+    double *rc0 = nullptr, *rc1 = nullptr;  // n each
     SegState* st = nullptr;
     const SegState* outer = nullptr;  // segments whose outer state is done take no part (refinement)
     int* ndone = nullptr;
@@ -49,9 +41,9 @@ struct SegRefine {
     const float* hi = nullptr;
     const float* lo = nullptr;
     const double* b = nullptr;
-    double* x = nullptr;    // FP64 solution
-    double* r = nullptr;    // FP64 residual
-    float* r32 = nullptr;   // inner right-hand side
+    double* x = nullptr;         // FP64 solution
+    double* r = nullptr;         // FP64 residual
+    float* r32 = nullptr;        // inner right-hand side
     const float* d32 = nullptr;  // inner solution (correction)
     SegState* st = nullptr;      // outer state: relres of b - A x, refinements in iters
     int* ndone = nullptr;

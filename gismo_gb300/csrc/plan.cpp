@@ -563,85 +563,103 @@ static void geoEvalHost(const HostPatch& P, const double* xi, double* x) {
             }
 }
 
+// values of one Dirichlet side at its boundary dofs (sideDofs order); `par`: OpenMP inside the side
+static std::vector<double> sideValues(const ProblemDesc& pd, size_t si, bool par) {
+    const int dim = pd.dim;
+    const HostPatch& P = pd.patches[pd.dsides[si]];
+    const int side = pd.dsides[si + 1];
+    const int dir = (side - 1) / 2, parity = (side - 1) % 2;
+    int odirs[2], no = 0;
+    for (int k = 0; k < dim; ++k) if (k != dir) odirs[no++] = k;
+    std::vector<double> gv[2];
+    int npts = 1;
+    for (int o = 0; o < no; ++o) { gv[o] = P.b[odirs[o]].greville(); npts *= int(gv[o].size()); }
+    const double fixv = parity ? P.b[dir].t.back() : P.b[dir].t.front();
+    const FieldParams& F = pd.fieldsOf(pd.dsides[si]);
+    std::vector<double> f(npts);
+#pragma omp parallel for schedule(static) if (par)
+    for (int i = 0; i < npts; ++i) {
+        double xi[3] = {0, 0, 0}, x[3];
+        int r = i;
+        for (int o = 0; o < no; ++o) {
+            const int c = r % int(gv[o].size());
+            r /= int(gv[o].size());
+            xi[odirs[o]] = gv[o][c];
+        }
+        xi[dir] = fixv;
+        geoEvalHost(P, xi, x);
+        double kap, ff, u;
+        evalFields(F, x, kap, ff, u);
+        f[i] = u;
+    }
+    // tensor collocation solve, one direction at a time (LU with partial pivoting). The
+    // collocation matrix is banded (p sub- and super-diagonals); with pivoting inside the band the
+    // factors stay within w = 3(p+1) of the diagonal, so the loops skip only exact zeros.
+    int stride = 1;
+    for (int o = 0; o < no; ++o) {
+        const Basis1D& B = P.b[odirs[o]];
+        const int n = B.n();
+        const int w = 3 * (B.p + 1);
+        std::vector<double> M(size_t(n) * n, 0.0), buf(2 * (B.p + 1));
+        for (int a = 0; a < n; ++a) {
+            const double u = gv[o][a];
+            const int s = B.span(u);
+            B.eval(s, u, buf.data());
+            for (int r = 0; r <= B.p; ++r) M[size_t(a) * n + (s - B.p + r)] = buf[r];
+        }
+        std::vector<int> piv(n);
+        for (int k = 0; k < n; ++k) {
+            int pm = k;
+            for (int i = k + 1; i < std::min(n, k + B.p + 2); ++i)
+                if (std::fabs(M[size_t(i) * n + k]) > std::fabs(M[size_t(pm) * n + k])) pm = i;
+            piv[k] = pm;
+            const int jlo = std::max(0, k - w), jhi = std::min(n, k + w + 1);
+            if (pm != k)
+                for (int j = jlo; j < jhi; ++j) std::swap(M[size_t(k) * n + j], M[size_t(pm) * n + j]);
+            const double dk = M[size_t(k) * n + k];
+            for (int i = k + 1; i < std::min(n, k + 2 * B.p + 2); ++i) {
+                const double l = M[size_t(i) * n + k] / dk;
+                if (l == 0.0) continue;
+                M[size_t(i) * n + k] = l;
+                for (int j = k + 1; j < jhi; ++j) M[size_t(i) * n + j] -= l * M[size_t(k) * n + j];
+            }
+        }
+        const int outer = npts / (n * stride);
+#pragma omp parallel for collapse(2) schedule(static) if (par)
+        for (int ob = 0; ob < outer; ++ob)
+            for (int ib = 0; ib < stride; ++ib) {
+                std::vector<double> col(n);
+                for (int a = 0; a < n; ++a) col[a] = f[size_t(ob) * n * stride + size_t(a) * stride + ib];
+                for (int k = 0; k < n; ++k) std::swap(col[k], col[piv[k]]);
+                for (int i = 0; i < n; ++i)
+                    for (int j = std::max(0, i - w); j < i; ++j) col[i] -= M[size_t(i) * n + j] * col[j];
+                for (int i = n - 1; i >= 0; --i) {
+                    for (int j = i + 1; j < std::min(n, i + w + 1); ++j) col[i] -= M[size_t(i) * n + j] * col[j];
+                    col[i] /= M[size_t(i) * n + i];
+                }
+                for (int a = 0; a < n; ++a) f[size_t(ob) * n * stride + size_t(a) * stride + ib] = col[a];
+            }
+        stride *= n;
+    }
+    return f;
+}
+
 void dirichletValues(const ProblemDesc& pd, const DofMap& map, std::vector<double>& ddof) {
     ddof.assign(map.boundarySize, 0.0);
-    const int dim = pd.dim;
+    const int nsides = int(pd.dsides.size() / 2);
+    // many sides (batches, multipatch): one side per thread; few sides: threads inside each side
+    const bool across = nsides >= 32;
+    std::vector<std::vector<double>> vals(nsides);
+#pragma omp parallel for schedule(dynamic, 4) if (across)
+    for (int k = 0; k < nsides; ++k) vals[k] = sideValues(pd, size_t(2 * k), !across);
+    // scatter in side order (a dof on two sides takes the later side's value)
     std::vector<int> bd;
-    for (size_t si = 0; si < pd.dsides.size(); si += 2) {
-        const HostPatch& P = pd.patches[pd.dsides[si]];
-        const int side = pd.dsides[si + 1];
-        const int dir = (side - 1) / 2, par = (side - 1) % 2;
-        int odirs[2], no = 0;
-        for (int k = 0; k < dim; ++k) if (k != dir) odirs[no++] = k;
-        std::vector<double> gv[2];
-        int npts = 1;
-        for (int o = 0; o < no; ++o) { gv[o] = P.b[odirs[o]].greville(); npts *= int(gv[o].size()); }
-        const double fixv = par ? P.b[dir].t.back() : P.b[dir].t.front();
-        std::vector<double> f(npts);
-#pragma omp parallel for schedule(static)
-        for (int i = 0; i < npts; ++i) {
-            double xi[3] = {0, 0, 0}, x[3];
-            int r = i;
-            for (int o = 0; o < no; ++o) {
-                const int c = r % int(gv[o].size());
-                r /= int(gv[o].size());
-                xi[odirs[o]] = gv[o][c];
-            }
-            xi[dir] = fixv;
-            geoEvalHost(P, xi, x);
-            double kap, ff, u;
-            evalFields(pd.fieldsOf(pd.dsides[si]), x, kap, ff, u);
-            f[i] = u;
-        }
-        // tensor collocation solve, one direction at a time (banded LU with partial pivoting)
-        int stride = 1;
-        for (int o = 0; o < no; ++o) {
-            const Basis1D& B = P.b[odirs[o]];
-            const int n = B.n();
-            std::vector<double> M(size_t(n) * n, 0.0), buf(2 * (B.p + 1));
-            for (int a = 0; a < n; ++a) {
-                const double u = gv[o][a];
-                const int s = B.span(u);
-                B.eval(s, u, buf.data());
-                for (int r = 0; r <= B.p; ++r) M[size_t(a) * n + (s - B.p + r)] = buf[r];
-            }
-            std::vector<int> piv(n);
-            for (int k = 0; k < n; ++k) {
-                int pm = k;
-                for (int i = k + 1; i < std::min(n, k + B.p + 2); ++i)
-                    if (std::fabs(M[size_t(i) * n + k]) > std::fabs(M[size_t(pm) * n + k])) pm = i;
-                piv[k] = pm;
-                if (pm != k)
-                    for (int j = 0; j < n; ++j) std::swap(M[size_t(k) * n + j], M[size_t(pm) * n + j]);
-                const double dk = M[size_t(k) * n + k];
-                for (int i = k + 1; i < std::min(n, k + 2 * B.p + 2); ++i) {
-                    const double l = M[size_t(i) * n + k] / dk;
-                    if (l == 0.0) continue;
-                    M[size_t(i) * n + k] = l;
-                    for (int j = k + 1; j < n; ++j) M[size_t(i) * n + j] -= l * M[size_t(k) * n + j];
-                }
-            }
-            const int outer = npts / (n * stride);
-#pragma omp parallel for collapse(2) schedule(static)
-            for (int ob = 0; ob < outer; ++ob)
-                for (int ib = 0; ib < stride; ++ib) {
-                    std::vector<double> col(n);
-                    for (int a = 0; a < n; ++a) col[a] = f[size_t(ob) * n * stride + size_t(a) * stride + ib];
-                    for (int k = 0; k < n; ++k) std::swap(col[k], col[piv[k]]);
-                    for (int i = 0; i < n; ++i)
-                        for (int j = 0; j < i; ++j) col[i] -= M[size_t(i) * n + j] * col[j];
-                    for (int i = n - 1; i >= 0; --i) {
-                        for (int j = i + 1; j < n; ++j) col[i] -= M[size_t(i) * n + j] * col[j];
-                        col[i] /= M[size_t(i) * n + i];
-                    }
-                    for (int a = 0; a < n; ++a) f[size_t(ob) * n * stride + size_t(a) * stride + ib] = col[a];
-                }
-            stride *= n;
-        }
-        sideDofs(P, side, bd);
+    for (int k = 0; k < nsides; ++k) {
+        const HostPatch& P = pd.patches[pd.dsides[2 * k]];
+        sideDofs(P, pd.dsides[2 * k + 1], bd);
         for (size_t l = 0; l < bd.size(); ++l) {
             const int gi = map.index[P.offset + bd[l]];
-            ddof[gi - map.freeSize] = f[l];
+            ddof[gi - map.freeSize] = vals[k][l];
         }
     }
 }

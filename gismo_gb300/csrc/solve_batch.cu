@@ -36,27 +36,16 @@ std::vector<int> segmentRows(const ProblemDesc& pd, const DofMap& map) {
 
 void Context::batchSetup() {
     const int nseg = int(segRow.size()) - 1;
-    auto table = [&](int rowsPerBlock, Tab& T, std::vector<int>& first) {
-        T.h.clear();
-        first.assign(nseg + 1, 0);
-        for (int j = 0; j < nseg; ++j) {
-            first[j] = int(T.h.size());
-            for (int b = 0; b < segRow[j + 1] - segRow[j]; b += rowsPerBlock) T.h.push_back({j, 0, b});
-        }
-        first[nseg] = int(T.h.size());
-        upload(arena, T.d, T.h, stream);
-    };
-    table(kBatchSpRows, tabSegSp, segSpH);
-    table(kBatchVecRows, tabSegV, segVH);
+    std::vector<int> rowSeg(pat.n);
+    for (int j = 0; j < nseg; ++j)
+        for (int r = segRow[j]; r < segRow[j + 1]; ++r) rowSeg[r] = j;
     upload(arena, dSegRow, segRow, stream);
-    upload(arena, dSegSp, segSpH, stream);
-    upload(arena, dSegV, segVH, stream);
-    allocN(arena, dSegPartSp, std::max<long long>(1, (long long)tabSegSp.h.size()));
-    allocN(arena, dSegPartV0, std::max<long long>(1, (long long)tabSegV.h.size()));
-    allocN(arena, dSegPartV1, std::max<long long>(1, (long long)tabSegV.h.size()));
+    upload(arena, dRowSeg, rowSeg, stream);
+    allocN(arena, dSegRc0, std::max(1, pat.n));
+    allocN(arena, dSegRc1, std::max(1, pat.n));
     allocN(arena, dSegSt, nseg);
     allocN(arena, dSegOuter, nseg);
-    allocN(arena, dSegDone, 2);
+    allocN(arena, dSegDone, 2);  // [inner done, outer done]
 }
 
 // iterations in chunks of 16 under one captured graph (per precision, once per context) until
@@ -103,18 +92,12 @@ void Context::solveBatch(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
         B.n = pat.n;
         B.nseg = nseg;
         B.segRow = dSegRow;
-        B.tabSp = tabSegSp.d;
-        B.segSp = dSegSp;
-        B.nSp = int(tabSegSp.h.size());
-        B.tabV = tabSegV.d;
-        B.segV = dSegV;
-        B.nV = int(tabSegV.h.size());
+        B.rowSeg = dRowSeg;
         B.ptr = dPtr;
         B.col = dCol;
         B.coff = dColOff;
-        B.partSp = dSegPartSp;
-        B.partV0 = dSegPartV0;
-        B.partV1 = dSegPartV1;
+        B.rc0 = dSegRc0;
+        B.rc1 = dSegRc1;
         B.st = dSegSt;
         B.ndone = dSegDone;
     };
