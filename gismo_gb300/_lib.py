@@ -14,7 +14,8 @@ EXPORTS = [
     "gsgpu_assemble", "gsgpu_sizes", "gsgpu_matrix_csr", "gsgpu_rhs", "gsgpu_fixed_dofs", "gsgpu_dof_map",
     "gsgpu_solve", "gsgpu_l2_error", "gsgpu_min_jacobian", "gsgpu_assemble_times", "gsgpu_stream",
     "gsgpu_set_profiling", "gsgpu_spmv_stats", "gsgpu_cg_jacobi_noalloc", "gsgpu_set_batch", "gsgpu_batch_info",
-    "gsgpu_batch_l2_error",
+    "gsgpu_batch_l2_error", "gsgpu_server_create", "gsgpu_server_submit", "gsgpu_server_wait",
+    "gsgpu_server_last_error", "gsgpu_server_destroy",
 ]
 
 OK, ERR_INVALID, ERR_CUDA, ERR_BUDGET, ERR_NOT_CONVERGED, ERR_JACOBIAN, ERR_STATE, ERR_TIMEOUT = range(8)
@@ -47,6 +48,12 @@ class SolverOpts(C.Structure):
 
 class SolveInfo(C.Structure):
     _fields_ = [("iterations", C.c_int), ("relres", C.c_double), ("refinements", C.c_int), ("t_solve_ms", C.c_double)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("nfree", C.c_int), ("iterations", C.c_int), ("relres", C.c_double),
+                ("t_submit", C.c_double), ("t_start", C.c_double), ("t_done", C.c_double), ("batch_size", C.c_int),
+                ("batch_id", C.c_longlong), ("est_bytes", C.c_double)]
 
 
 class GsGpuError(RuntimeError):
@@ -83,6 +90,12 @@ def lib() -> C.CDLL:
         L.gsgpu_set_batch.argtypes = [vp, C.c_int, vp]
         L.gsgpu_batch_info.argtypes = [vp, vp, vp, vp]
         L.gsgpu_batch_l2_error.argtypes = [vp, vp]
+        L.gsgpu_server_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.c_double, C.c_int, C.c_int]
+        L.gsgpu_server_submit.argtypes = [vp, C.POINTER(Problem), C.c_double, C.POINTER(C.c_longlong)]
+        L.gsgpu_server_wait.argtypes = [vp, C.c_longlong, vp, C.c_int, C.POINTER(RequestInfo)]
+        L.gsgpu_server_last_error.argtypes = [vp]
+        L.gsgpu_server_last_error.restype = C.c_char_p
+        L.gsgpu_server_destroy.argtypes = [vp]
         L.gsgpu_min_jacobian.argtypes = [vp, C.POINTER(C.c_double)]
         L.gsgpu_assemble_times.argtypes = [vp, vp]
         L.gsgpu_stream.argtypes = [vp, C.POINTER(vp)]

@@ -238,3 +238,54 @@ class GpuPoissonBatch(GpuPoissonAssembler):
         out = np.zeros(len(self.problems), np.float64)
         self._check(self.L.gsgpu_batch_l2_error(self.h, out.ctypes.data))
         return out
+
+
+class GpuPoissonServer:
+    """Request server with continuous batching (include/gsgpu.h gsgpu_server_*): submit() queues a
+    copy of a single-patch problem and returns at once; result() blocks until it is solved. Worker
+    slots batch the queued requests of one dimension under a device-memory budget."""
+
+    def __init__(self, device: int = 0, slots: int = 4, budget_gb: float = 120.0, max_batch: int = 64,
+                 precision: str = "mixed"):
+        self.L = _lib.lib()
+        self.h = C.c_void_p()
+        prec = _lib.PREC_FP64 if precision == "fp64" else _lib.PREC_MIXED
+        rc = self.L.gsgpu_server_create(C.byref(self.h), device, slots, budget_gb * 1e9, max_batch, prec)
+        if rc != _lib.OK:
+            raise GsGpuError(rc, "could not create the server")
+        self._sizes = {}
+
+    def submit(self, prob, tol: float = 1e-8) -> int:
+        pk = PackedProblem(prob)
+        rid = C.c_longlong()
+        rc = self.L.gsgpu_server_submit(self.h, C.byref(pk.struct), tol, C.byref(rid))
+        if rc != _lib.OK:
+            raise GsGpuError(rc, self.L.gsgpu_server_last_error(self.h).decode())
+        n = 1
+        for pt in prob.patches:
+            for k in range(prob.dim):
+                n *= len(pt.knots[k]) - pt.degree[k] - 1
+        self._sizes[rid.value] = n
+        return rid.value
+
+    def result(self, rid: int):
+        """(x, info) of request rid; info['status'] is the request's status code."""
+        cap = self._sizes.pop(rid, 0)
+        x = np.empty(cap, np.float64)
+        info = _lib.RequestInfo()
+        rc = self.L.gsgpu_server_wait(self.h, rid, x.ctypes.data, cap, C.byref(info))
+        d = {f: getattr(info, f) for f, _ in _lib.RequestInfo._fields_}
+        if rc not in (_lib.OK, _lib.ERR_NOT_CONVERGED, _lib.ERR_BUDGET):
+            raise GsGpuError(rc, self.L.gsgpu_server_last_error(self.h).decode())
+        return x[:info.nfree], d
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.gsgpu_server_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

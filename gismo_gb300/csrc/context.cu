@@ -826,6 +826,32 @@ int gsgpu_set_batch(gsgpu_context* ctx, int count, const gsgpu_problem* problems
     });
 }
 
+}  // extern "C"
+
+int gsgpu::setBatchDescs(gsgpu_context* ctx, std::vector<gsgpu::ProblemDesc>& items) {
+    return guarded(ctx, [&] {
+        gsgpu::ProblemDesc pd;
+        gsgpu::batchFromDescs(items, pd);
+        if (ctx->c.device >= 0) {
+            ctx->c.dropGraphs();
+            ctx->c.arena.releaseAll();
+        }
+        ctx->c = gsgpu::Context::reset(std::move(ctx->c));
+        ctx->c.pd = std::move(pd);
+        ctx->c.hasProblem = true;
+        ctx->c.batch = true;
+    });
+}
+
+void gsgpu::releaseDevice(gsgpu_context* ctx) {
+    if (!ctx || ctx->c.device < 0) return;
+    cudaSetDevice(ctx->c.device);
+    ctx->c.freeAssembly();
+    ctx->c.refreshed = ctx->c.assembled = ctx->c.solved = false;
+}
+
+extern "C" {
+
 int gsgpu_batch_info(gsgpu_context* ctx, int* offsets, int* iterations, double* relres) {
     return guarded(ctx, [&] {
         auto& c = ctx->c;

@@ -94,6 +94,10 @@ void coefsToSoa(const DevPatch* P, const BlkEnt* tab, long long nblk, const doub
 
 // free-dof row offsets of the problems of a batch (one patch per problem)
 std::vector<int> segmentRows(const ProblemDesc& pd, const DofMap& map);
+// gsgpu_set_batch from validated descriptions (consumed); the request server's entry
+int setBatchDescs(gsgpu_context* ctx, std::vector<ProblemDesc>& items);
+// free every device buffer of the context (it keeps its stream and problem)
+void releaseDevice(gsgpu_context* ctx);
 
 struct Context {
     int device = -1;

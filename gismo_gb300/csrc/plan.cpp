@@ -736,14 +736,12 @@ void problemFromC(const void* ptr, ProblemDesc& pd) {
     pd.quB = pr->quB;
 }
 
-void batchFromC(int count, const void* ptr, ProblemDesc& pd) {
-    const gsgpu_problem* pr = static_cast<const gsgpu_problem*>(ptr);
-    if (!pr || count < 1) throw std::invalid_argument("batch: count must be >= 1");
+void batchFromDescs(std::vector<ProblemDesc>& items, ProblemDesc& pd) {
+    if (items.empty()) throw std::invalid_argument("batch: count must be >= 1");
     pd = ProblemDesc();
     int off = 0;
-    for (int j = 0; j < count; ++j) {
-        ProblemDesc one;
-        problemFromC(&pr[j], one);
+    for (size_t j = 0; j < items.size(); ++j) {
+        ProblemDesc& one = items[j];
         if (one.patches.size() != 1 || !one.ifaces.empty())
             throw std::invalid_argument("batch: every problem must be a single patch without interfaces");
         if (j == 0) {
@@ -755,16 +753,24 @@ void batchFromC(int count, const void* ptr, ProblemDesc& pd) {
             throw std::invalid_argument("batch: dimension and quadrature rule must agree across problems");
         }
         HostPatch P = std::move(one.patches[0]);
-        P.field = j;
+        P.field = int(j);
         P.offset = off;
         off += P.ndofs;
         pd.patches.push_back(std::move(P));
         for (size_t i = 0; i < one.dsides.size(); i += 2) {
-            pd.dsides.push_back(j);
+            pd.dsides.push_back(int(j));
             pd.dsides.push_back(one.dsides[i + 1]);
         }
         pd.pfields.push_back(one.fields);
     }
+}
+
+void batchFromC(int count, const void* ptr, ProblemDesc& pd) {
+    const gsgpu_problem* pr = static_cast<const gsgpu_problem*>(ptr);
+    if (!pr || count < 1) throw std::invalid_argument("batch: count must be >= 1");
+    std::vector<ProblemDesc> items(static_cast<size_t>(count));
+    for (int j = 0; j < count; ++j) problemFromC(&pr[j], items[size_t(j)]);
+    batchFromDescs(items, pd);
 }
 
 void blockTable(const std::vector<long long>& work, int block, std::vector<BlkEnt>& tab) {

@@ -72,6 +72,8 @@ void problemFromC(const void* gsgpu_problem_ptr, ProblemDesc& pd);
 // a batch of independent single-patch problems as one ProblemDesc (patch j = problem j, with its
 // own field set); quA/quB and the dimension must agree
 void batchFromC(int count, const void* gsgpu_problem_array, ProblemDesc& pd);
+// the same from validated descriptions (consumed)
+void batchFromDescs(std::vector<ProblemDesc>& items, ProblemDesc& pd);
 
 // symbolic CSR + gather maps
 struct Pattern {

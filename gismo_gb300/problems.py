@@ -397,9 +397,9 @@ def cube_grid(n: int = 8, n_elem: int = 16, p: int = 2, seed: int = 3, amp: floa
     return prob
 
 
-def serving_requests(count: int, rate: float, seed: int = 11, check: bool = False):
-    """Poisson-process arrivals at ``rate`` req/s; 60 % 2D (16..256 elements/dir), 40 % 3D
-    (8..48 elements/dir), degree in {2,3,4}; geometry and kappa as in the other configs.
+def serving_requests(count: int, rate: float, seed: int = 11, check: bool = False, n2d=(16, 256), n3d=(8, 48)):
+    """Poisson-process arrivals at ``rate`` req/s; 60 % 2D (``n2d`` elements/dir, log-uniform), 40 % 3D
+    (``n3d`` elements/dir), degree in {2,3,4}; geometry and kappa as in the other configs.
     Returns a list of (arrival_time_s, Problem)."""
     rng = np.random.default_rng(seed)
     t = 0.0
@@ -408,10 +408,10 @@ def serving_requests(count: int, rate: float, seed: int = 11, check: bool = Fals
         t += rng.exponential(1.0 / rate)
         p = int(rng.integers(2, 5))
         if rng.uniform() < 0.6:
-            ne = int(round(math.exp(rng.uniform(math.log(16), math.log(256)))))
+            ne = int(round(math.exp(rng.uniform(math.log(n2d[0]), math.log(n2d[1])))))
             prob = displaced_single_patch(2, (ne, ne), (p, p), seed * 7919 + i, 0.05, check=check)
         else:
-            ne = int(round(math.exp(rng.uniform(math.log(8), math.log(48)))))
+            ne = int(round(math.exp(rng.uniform(math.log(n3d[0]), math.log(n3d[1])))))
             prob = displaced_single_patch(3, (ne,) * 3, (p,) * 3, seed * 7919 + i, 0.04, check=check)
         prob.tol = 1e-8
         out.append((t, prob))

@@ -148,6 +148,41 @@ int gsgpu_batch_info(gsgpu_context* ctx, int* offsets, int* iterations, double* 
 /* per problem: gsField::distanceL2 of the last solution (count values) */
 int gsgpu_batch_l2_error(gsgpu_context* ctx, double* err);
 
+/* Request server (continuous batching). No counterpart in the reference, which has no serving
+ * layer: a caller there runs one gsPoissonAssembler + gsConjugateGradient per request. Requests
+ * (single-patch problems, each copied at submission) are queued in arrival order. Each of `slots`
+ * worker threads owns a context and a CUDA stream; when it is free it takes the queue head and every
+ * later queued request of the same dimension and tolerance, in arrival order, up to `max_batch`
+ * requests and while their estimated device memory fits in what is left of `budget_bytes`, and
+ * assembles and solves them as one batch (gsgpu_set_batch) in `precision`. Requests that arrive
+ * while batches run join the next batch a slot forms; batches of different slots overlap on the
+ * device. A request's result does not depend on the other requests of its batch (every problem of a
+ * batch keeps its own CG scalars and stopping test). A request whose estimate exceeds the whole
+ * budget fails with GSGPU_ERR_BUDGET. Times are seconds since the server was created. */
+typedef struct gsgpu_server gsgpu_server;
+typedef struct {
+    int status;       /* GSGPU_OK or the request's error code */
+    int nfree;        /* free dofs (length of the solution) */
+    int iterations;   /* CG iterations (mixed: inner FP32 iterations summed over the refinements) */
+    double relres;    /* ||b - A x|| / ||b|| of the returned solution (FP64) */
+    double t_submit, t_start, t_done;
+    int batch_size;   /* requests solved by the same launches */
+    long long batch_id;
+    double est_bytes; /* device-memory estimate the admission used */
+} gsgpu_request_info;
+int gsgpu_server_create(gsgpu_server** srv, int device, int slots, double budget_bytes, int max_batch,
+                        int precision);
+/* queue a copy of a single-patch problem; *id identifies it in gsgpu_server_wait */
+int gsgpu_server_submit(gsgpu_server* srv, const gsgpu_problem* prob, double tol, long long* id);
+/* block until request `id` is done; x (capacity doubles, may be NULL) receives the solution. The
+ * request is forgotten afterwards. Returns the request's status (GSGPU_ERR_INVALID for an unknown
+ * id or a too small x). */
+int gsgpu_server_wait(gsgpu_server* srv, long long id, double* x, int capacity, gsgpu_request_info* info);
+/* message of the last failed request taken by gsgpu_server_wait */
+const char* gsgpu_server_last_error(const gsgpu_server* srv);
+/* finishes the queued requests, then stops the workers and frees everything */
+int gsgpu_server_destroy(gsgpu_server* srv);
+
 /* Utilities with no counterpart in the reference. */
 /* the CUDA stream (cudaStream_t) all device work of the context is issued on */
 int gsgpu_stream(gsgpu_context* ctx, void** stream);
