@@ -52,6 +52,10 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="volume", choices=["volume", "batch", "multigrid", "serving"],
+                    help="volume: the headline configuration; the others are in gismo_gb300/bench_workloads.py")
+    ap.add_argument("--mg-damping", type=float, default=0.5)
+    ap.add_argument("--requests", type=int, default=200)
     return ap.parse_args()
 
 
@@ -207,6 +211,12 @@ def run_reference(args):
 
 def main():
     args = parse()
+    if args.workload != "volume" and args.impl == "ours":
+        from gismo_gb300 import bench_workloads as BW
+        import __graft_entry__ as g
+        g.build()
+        fn = {"batch": BW.run_batch, "multigrid": BW.run_multigrid, "serving": BW.run_serving}[args.workload]
+        return fn(args, lambda: ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))))
     if args.impl == "reference":
         return run_reference(args)
     ws, rank, local = dist_env()

@@ -53,7 +53,8 @@ class SolveInfo(C.Structure):
 class RequestInfo(C.Structure):
     _fields_ = [("status", C.c_int), ("nfree", C.c_int), ("iterations", C.c_int), ("relres", C.c_double),
                 ("t_submit", C.c_double), ("t_start", C.c_double), ("t_done", C.c_double), ("batch_size", C.c_int),
-                ("batch_id", C.c_longlong), ("est_bytes", C.c_double)]
+                ("batch_id", C.c_longlong), ("est_bytes", C.c_double), ("ms_setup", C.c_double),
+                ("ms_assemble", C.c_double), ("ms_solve", C.c_double)]
 
 
 class GsGpuError(RuntimeError):

@@ -119,13 +119,16 @@ void Context::refresh() {
     }
     // diagonal slot of every row (Jacobi)
     diag.assign(pat.n, -1);
+    int nodiag = 0;
+#pragma omp parallel for schedule(static) reduction(+ : nodiag)
     for (int r = 0; r < pat.n; ++r) {
         const int* b = pat.col.data() + pat.ptr[r];
         const int* e = pat.col.data() + pat.ptr[r + 1];
         const int* f = std::lower_bound(b, e, r);
-        if (f == e || *f != r) throw std::runtime_error("pattern has no diagonal entry");
-        diag[r] = pat.ptr[r] + int(f - b);
+        if (f == e || *f != r) ++nodiag;
+        else diag[r] = pat.ptr[r] + int(f - b);
     }
+    if (nodiag) throw std::runtime_error("pattern has no diagonal entry");
     upload(arena, dPatches, L.dev, stream);
     {
         std::vector<dev::FieldConst<double>> fc64;
@@ -179,14 +182,16 @@ void Context::refresh() {
     if (batch) batchSetup();
     {
         // banded patterns (single patches) store columns as 16-bit offsets from the row
-        bool fits = true;
-        for (int r = 0; r < pat.n && fits; ++r)
+        int far = 0;
+#pragma omp parallel for schedule(static) reduction(+ : far)
+        for (int r = 0; r < pat.n; ++r)
             for (int k = pat.ptr[r]; k < pat.ptr[r + 1]; ++k)
-                if (pat.col[k] - r > 32767 || pat.col[k] - r < -32768) { fits = false; break; }
+                if (pat.col[k] - r > 32767 || pat.col[k] - r < -32768) ++far;
         arena.release(dColOff);
         dColOff = nullptr;
-        if (fits && !pat.col.empty()) {
-            std::vector<int16_t> off(pat.col.size());
+        if (far == 0 && !pat.col.empty()) {
+            bigvec<int16_t> off(pat.col.size());
+#pragma omp parallel for schedule(static)
             for (int r = 0; r < pat.n; ++r)
                 for (int k = pat.ptr[r]; k < pat.ptr[r + 1]; ++k) off[k] = int16_t(pat.col[k] - r);
             upload(arena, dColOff, off, stream);

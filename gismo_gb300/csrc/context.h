@@ -48,8 +48,8 @@ struct Tab {
     BlkEnt* d = nullptr;
 };
 
-template <typename T>
-inline void upload(DeviceArena& A, T*& dptr, const std::vector<T>& h, cudaStream_t s) {
+template <typename T, typename Alloc>
+inline void upload(DeviceArena& A, T*& dptr, const std::vector<T, Alloc>& h, cudaStream_t s) {
     A.release(dptr);
     dptr = static_cast<T*>(A.alloc(h.size() * sizeof(T)));
     if (!h.empty()) GSGPU_CUDA_TRY(cudaMemcpyAsync(dptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));

@@ -403,10 +403,152 @@ void rowEntries(const ProblemDesc& pd, const DofMap& map, const Layout& L, const
 }
 }  // namespace
 
+// Problems without interfaces (single patches, batches of independent patches): every free row has
+// one pre-image, and a patch's free dofs are numbered in its local lexicographic order, so a row's
+// columns come out ascending from its neighbour box with no sorting and no multi-source slots. The
+// neighbour set per direction is the support-sharing range the generic path tests pair by pair, and
+// the loop order (and so the lift order) is the same. Returns false (generic path) if an assumption
+// does not hold.
+static bool buildPatternSingle(const ProblemDesc& pd, const DofMap& map, const Layout& L, Pattern& pat) {
+    const int n = map.freeSize;
+    const int d = pd.dim;
+    const size_t np = pd.patches.size();
+    std::vector<int> rowPatch(n, -1), rowLoc(n, -1);
+    for (size_t pi = 0; pi < np; ++pi) {
+        const HostPatch& P = pd.patches[pi];
+        for (int i = 0; i < P.ndofs; ++i) {
+            const int J = map.index[P.offset + i];
+            if (J >= n) continue;
+            if (rowPatch[J] >= 0) return false;
+            rowPatch[J] = int(pi);
+            rowLoc[J] = i;
+        }
+    }
+    // support-sharing neighbour range [jlo, jhi] of every function, per patch and direction
+    std::vector<std::vector<int>> jlo(np * 3), jhi(np * 3);
+    for (size_t pi = 0; pi < np; ++pi) {
+        const HostPatch& P = pd.patches[pi];
+        const DevPatch& D = L.dev[pi];
+        for (int a = 0; a < d; ++a) {
+            const int* elo = L.ibuf.data() + D.doff[a];
+            const int* ehi = elo + D.n[a];
+            std::vector<int>& lo = jlo[pi * 3 + a];
+            std::vector<int>& hi = jhi[pi * 3 + a];
+            lo.assign(P.nd[a], 0);
+            hi.assign(P.nd[a], -1);
+            for (int i = 0; i < P.nd[a]; ++i) {
+                int first = -1, last = -2;
+                for (int j = std::max(0, i - D.p[a]); j <= std::min(P.nd[a] - 1, i + D.p[a]); ++j) {
+                    const bool share = std::max(elo[i], elo[j]) <= std::min(ehi[i], ehi[j]);
+                    if (!share) continue;
+                    if (first < 0) first = j;
+                    else if (j != last + 1) return false;  // not a contiguous range
+                    last = j;
+                }
+                lo[i] = first;
+                hi[i] = last;
+            }
+        }
+    }
+    auto box = [&](int I, int c[3], int lo[3], int hi[3]) {
+        const int pi = rowPatch[I];
+        const HostPatch& P = pd.patches[pi];
+        int r = rowLoc[I];
+        for (int a = 0; a < 3; ++a) {
+            if (a < d) {
+                c[a] = r % P.nd[a];
+                r /= P.nd[a];
+                lo[a] = jlo[size_t(pi) * 3 + a][c[a]];
+                hi[a] = jhi[size_t(pi) * 3 + a][c[a]];
+            } else {
+                c[a] = lo[a] = hi[a] = 0;
+            }
+        }
+    };
+    std::vector<long long> nslot(n + 1, 0), nlift(n + 1, 0);
+#pragma omp parallel for schedule(dynamic, 512)
+    for (int I = 0; I < n; ++I) {
+        const HostPatch& P = pd.patches[rowPatch[I]];
+        int c[3], lo[3], hi[3];
+        box(I, c, lo, hi);
+        long long ns = 0, nl = 0;
+        for (int z = lo[2]; z <= hi[2]; ++z)
+            for (int y = lo[1]; y <= hi[1]; ++y)
+                for (int x = lo[0]; x <= hi[0]; ++x) {
+                    const int lj = x + P.nd[0] * (y + (d == 3 ? P.nd[1] * z : 0));
+                    if (map.index[P.offset + lj] < n) ++ns;
+                    else ++nl;
+                }
+        nslot[I + 1] = ns;
+        nlift[I + 1] = nl;
+    }
+    for (int i = 0; i < n; ++i) {
+        nslot[i + 1] += nslot[i];
+        nlift[i + 1] += nlift[i];
+    }
+    if (nslot[n] >= (1LL << 31)) throw std::invalid_argument("more than 2^31 non-zeros");
+    pat.ptr.resize(n + 1);
+    for (int i = 0; i <= n; ++i) pat.ptr[i] = int(nslot[i]);
+    pat.col.resize(nslot[n]);
+    pat.src.resize(nslot[n]);
+    pat.fptr.resize(n + 1);
+    pat.fband.resize(nlift[n]);
+    pat.fbidx.resize(nlift[n]);
+    for (int i = 0; i <= n; ++i) pat.fptr[i] = uint32_t(nlift[i]);
+    int ordered = 1;
+#pragma omp parallel for schedule(dynamic, 512) reduction(& : ordered)
+    for (int I = 0; I < n; ++I) {
+        const int pi = rowPatch[I];
+        const HostPatch& P = pd.patches[pi];
+        const DevPatch& D = L.dev[pi];
+        int c[3], lo[3], hi[3];
+        box(I, c, lo, hi);
+        const long long n0W = (long long)D.n[0] * D.W[0], n1W = (long long)D.n[1] * D.W[1];
+        long long s = nslot[I], f = nlift[I];
+        int prev = -1;
+        for (int z = lo[2]; z <= hi[2]; ++z)
+            for (int y = lo[1]; y <= hi[1]; ++y)
+                for (int x = lo[0]; x <= hi[0]; ++x) {
+                    const int lj = x + P.nd[0] * (y + (d == 3 ? P.nd[1] * z : 0));
+                    const int J = map.index[P.offset + lj];
+                    long long b = (long long)c[0] * D.W[0] + (x - c[0] + D.p[0]);
+                    b += ((long long)c[1] * D.W[1] + (y - c[1] + D.p[1])) * n0W;
+                    if (d == 3) b += ((long long)c[2] * D.W[2] + (z - c[2] + D.p[2])) * n0W * n1W;
+                    b += D.band_off;
+                    if (J < n) {
+                        if (J <= prev) ordered = 0;
+                        prev = J;
+                        pat.col[s] = J;
+                        pat.src[s] = uint32_t(b);
+                        ++s;
+                    } else {
+                        pat.fband[f] = uint32_t(b);
+                        pat.fbidx[f] = uint32_t(J - n);
+                        ++f;
+                    }
+                }
+    }
+    if (!ordered) return false;
+    pat.ovf_ptr.assign(1, 0);
+    pat.lptr.resize(n + 1);
+    for (int i = 0; i <= n; ++i) pat.lptr[i] = uint32_t(i);
+    pat.lidx.resize(n);
+    for (int I = 0; I < n; ++I) pat.lidx[I] = uint32_t(L.dev[rowPatch[I]].lvec_off + rowLoc[I]);
+    return true;
+}
+
 void buildPattern(const ProblemDesc& pd, const DofMap& map, const Layout& L, Pattern& pat, int nthreads) {
     const int n = map.freeSize;
     pat = Pattern();
     pat.n = n;
+    if (pd.ifaces.empty()) {
+#ifdef _OPENMP
+        if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+        if (buildPatternSingle(pd, map, L, pat)) return;
+        pat = Pattern();
+        pat.n = n;
+    }
     // pre-images of every free global dof
     std::vector<int> preptr(n + 1, 0), preloc, prepatch;
     for (size_t pi = 0; pi < pd.patches.size(); ++pi) {

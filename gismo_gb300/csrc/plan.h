@@ -6,6 +6,8 @@
 
 #include <cstdint>
 #include <string>
+#include <memory>
+#include <utility>
 #include <vector>
 
 #include "gsgpu_internal.h"
@@ -75,13 +77,36 @@ void batchFromC(int count, const void* gsgpu_problem_array, ProblemDesc& pd);
 // the same from validated descriptions (consumed)
 void batchFromDescs(std::vector<ProblemDesc>& items, ProblemDesc& pd);
 
+// allocator whose resize() leaves new elements uninitialised: the large pattern arrays are filled by
+// parallel loops, which then also do the first touch of their pages
+template <class T>
+struct NoInitAlloc : std::allocator<T> {
+    template <class U>
+    struct rebind {
+        using other = NoInitAlloc<U>;
+    };
+    NoInitAlloc() = default;
+    template <class U>
+    NoInitAlloc(const NoInitAlloc<U>&) noexcept {}
+    template <class U>
+    void construct(U* p) noexcept {
+        ::new (static_cast<void*>(p)) U;
+    }
+    template <class U, class... Args>
+    void construct(U* p, Args&&... a) {
+        ::new (static_cast<void*>(p)) U(std::forward<Args>(a)...);
+    }
+};
+template <class T>
+using bigvec = std::vector<T, NoInitAlloc<T>>;
+
 // symbolic CSR + gather maps
 struct Pattern {
     int n = 0;
     std::vector<int> ptr;           // n+1 (int32: the reference's index_t)
-    std::vector<int> col;           // nnz
+    bigvec<int> col;                // nnz
     // per CSR slot: band entry (global band offset) or (kMulti | index into the overflow lists)
-    std::vector<uint32_t> src;
+    bigvec<uint32_t> src;
     std::vector<uint32_t> ovf_ptr;  // overflow list pointers (slots with several sources)
     std::vector<uint32_t> ovf_idx;
     // per free row: load-vector sources (global load-vector offsets)

@@ -17,6 +17,10 @@
 #include <thread>
 #include <vector>
 
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
 #include "../../include/gsgpu.h"
 #include "context.h"
 #include "plan.h"
@@ -55,7 +59,7 @@ double estimateBytes(const ProblemDesc& pd) {
 }  // namespace
 
 struct Server {
-    int device = 0, maxBatch = 64, precision = GSGPU_PREC_MIXED;
+    int device = 0, maxBatch = 64, precision = GSGPU_PREC_MIXED, nslots = 1;
     double budget = 0.0, reserved = 0.0;
     std::mutex m;
     std::condition_variable cvWork, cvDone;
@@ -111,9 +115,16 @@ void Server::run(gsgpu_context* ctx, std::vector<Request*>& batch) {
     std::vector<ProblemDesc> items;
     items.reserve(nb);
     for (Request* r : batch) items.push_back(std::move(r->pd));
+    auto clock = [] { return std::chrono::steady_clock::now(); };
+    auto ms = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+        return std::chrono::duration<double, std::milli>(b - a).count();
+    };
+    const auto t0 = clock();
     int rc = setBatchDescs(ctx, items);
     if (rc == GSGPU_OK) rc = gsgpu_refresh(ctx);
+    const auto t1 = clock();
     if (rc == GSGPU_OK) rc = gsgpu_assemble(ctx, precision);
+    const auto t2 = clock();
     std::vector<double> x;
     std::vector<int> off(nb + 1, 0), its(nb, 0);
     std::vector<double> rr(nb, 0.0);
@@ -133,10 +144,14 @@ void Server::run(gsgpu_context* ctx, std::vector<Request*>& batch) {
         if (rc == GSGPU_ERR_NOT_CONVERGED) rc = GSGPU_OK;  // judged per request below
         if (rc == GSGPU_OK) rc = gsgpu_batch_info(ctx, off.data(), its.data(), rr.data());
     }
+    const auto t3 = clock();
     const std::string msg = rc == GSGPU_OK ? std::string() : std::string(gsgpu_last_error(ctx));
     for (size_t j = 0; j < nb; ++j) {
         Request* r = batch[j];
         r->info.batch_size = int(nb);
+        r->info.ms_setup = ms(t0, t1);
+        r->info.ms_assemble = ms(t1, t2);
+        r->info.ms_solve = ms(t2, t3);
         if (rc != GSGPU_OK) {
             r->info.status = rc;
             r->err = msg;
@@ -153,6 +168,10 @@ void Server::run(gsgpu_context* ctx, std::vector<Request*>& batch) {
 }
 
 void Server::work() {
+#ifdef _OPENMP
+    // the slots' host set-up runs concurrently: each gets an equal share of the host threads
+    omp_set_num_threads(std::max(1, omp_get_num_procs() / std::max(1, nslots)));
+#endif
     gsgpu_context* ctx = nullptr;
     const int crc = gsgpu_create(&ctx, device);
     for (;;) {
@@ -214,6 +233,7 @@ int gsgpu_server_create(gsgpu_server** out, int device, int slots, double budget
     p->s.budget = budget_bytes;
     p->s.maxBatch = max_batch;
     p->s.precision = precision;
+    p->s.nslots = slots;
     for (int i = 0; i < slots; ++i) p->s.workers.emplace_back([p] { p->s.work(); });
     *out = p;
     return GSGPU_OK;

@@ -169,6 +169,7 @@ typedef struct {
     int batch_size;   /* requests solved by the same launches */
     long long batch_id;
     double est_bytes; /* device-memory estimate the admission used */
+    double ms_setup, ms_assemble, ms_solve;  /* wall time of the batch's refresh, assemble and solve */
 } gsgpu_request_info;
 int gsgpu_server_create(gsgpu_server** srv, int device, int slots, double budget_bytes, int max_batch,
                         int precision);
