@@ -87,9 +87,12 @@ void Context::buildTables() {
         mk(tabSt[1], [](const DevPatch& D) { return dev::stageWork<32>(D); });
         mk(tabSt[2], [](const DevPatch& D) { return dev::stageWork<33>(D); });
         for (int P = 1; P <= 4; ++P) {
-            mk(tabRow[0][P], [P](const DevPatch& D) { return D.p[0] == P ? dev::stageRowWork<31>(D) : 0LL; });
-            mk(tabRow[1][P], [P](const DevPatch& D) { return D.p[1] == P ? dev::stageRowWork<32>(D) : 0LL; });
-            mk(tabRow[2][P], [P](const DevPatch& D) { return D.p[2] == P ? dev::stageRowWork<33>(D) : 0LL; });
+            mk(tabRow[0][P], [P](const DevPatch& D) { return D.p[0] == P ? dev::stageInteriorWork<31>(D) : 0LL; });
+            mk(tabRow[1][P], [P](const DevPatch& D) { return D.p[1] == P ? dev::stageInteriorWork<32>(D) : 0LL; });
+            mk(tabRow[2][P], [P](const DevPatch& D) { return D.p[2] == P ? dev::stageInteriorWork<33>(D) : 0LL; });
+            mk(tabRowB[0][P], [P](const DevPatch& D) { return D.p[0] == P ? dev::stageBoundaryWork<31>(D) : 0LL; });
+            mk(tabRowB[1][P], [P](const DevPatch& D) { return D.p[1] == P ? dev::stageBoundaryWork<32>(D) : 0LL; });
+            mk(tabRowB[2][P], [P](const DevPatch& D) { return D.p[2] == P ? dev::stageBoundaryWork<33>(D) : 0LL; });
         }
         mk(tabLd[0], [](const DevPatch& D) { return dev::loadWork<31>(D); });
         mk(tabLd[1], [](const DevPatch& D) { return dev::loadWork<32>(D); });
@@ -98,8 +101,10 @@ void Context::buildTables() {
         mk(tabSt[0], [](const DevPatch& D) { return dev::stageWork<21>(D); });
         mk(tabSt[1], [](const DevPatch& D) { return dev::stageWork<22>(D); });
         for (int P = 1; P <= 4; ++P) {
-            mk(tabRow[0][P], [P](const DevPatch& D) { return D.p[0] == P ? dev::stageRowWork<21>(D) : 0LL; });
-            mk(tabRow[1][P], [P](const DevPatch& D) { return D.p[1] == P ? dev::stageRowWork<22>(D) : 0LL; });
+            mk(tabRow[0][P], [P](const DevPatch& D) { return D.p[0] == P ? dev::stageInteriorWork<21>(D) : 0LL; });
+            mk(tabRow[1][P], [P](const DevPatch& D) { return D.p[1] == P ? dev::stageInteriorWork<22>(D) : 0LL; });
+            mk(tabRowB[0][P], [P](const DevPatch& D) { return D.p[0] == P ? dev::stageBoundaryWork<21>(D) : 0LL; });
+            mk(tabRowB[1][P], [P](const DevPatch& D) { return D.p[1] == P ? dev::stageBoundaryWork<22>(D) : 0LL; });
         }
         mk(tabLd[0], [](const DevPatch& D) { return dev::loadWork<21>(D); });
         mk(tabLd[1], [](const DevPatch& D) { return dev::loadWork<22>(D); });
@@ -303,33 +308,36 @@ void Context::assemble(int precision) {
         const bool nh2 = rowGroup2();
         for (int P = 1; P <= 4; ++P) {
             auto nb = [&](int st) { return (long long)tabRow[st][P].h.size(); };
+            auto nbB = [&](int st) { return (long long)tabRowB[st][P].h.size(); };
             if (pd.dim == 3 && nh2) {
-                launch::contractRowDF<31, 0, 2>(P, dPatches, tabRow[0][P].d, nb(0), cDf, sDf, dIbuf, pfDf, s);
-                launch::contractRowDF<31, 2, 2>(P, dPatches, tabRow[0][P].d, nb(0), cDf, sDf, dIbuf, pfDf, s);
-                launch::contractRowDF<31, 4, 2>(P, dPatches, tabRow[0][P].d, nb(0), cDf, sDf, dIbuf, pfDf, s);
-                launch::contractRowDF<31, 6, 2>(P, dPatches, tabRow[0][P].d, nb(0), cDf, sDf, dIbuf, pfDf, s);
+                launch::contractRowDF<31, 0, 2>(P, dPatches, tabRow[0][P].d, nb(0), tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
+                launch::contractRowDF<31, 2, 2>(P, dPatches, tabRow[0][P].d, nb(0), tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
+                launch::contractRowDF<31, 4, 2>(P, dPatches, tabRow[0][P].d, nb(0), tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
+                launch::contractRowDF<31, 6, 2>(P, dPatches, tabRow[0][P].d, nb(0), tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
             } else if (pd.dim == 3) {
-                launch::contractRowDF<31, 0, 4>(P, dPatches, tabRow[0][P].d, nb(0), cDf, sDf, dIbuf, pfDf, s);
-                launch::contractRowDF<31, 4, 4>(P, dPatches, tabRow[0][P].d, nb(0), cDf, sDf, dIbuf, pfDf, s);
+                launch::contractRowDF<31, 0, 4>(P, dPatches, tabRow[0][P].d, nb(0), tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
+                launch::contractRowDF<31, 4, 4>(P, dPatches, tabRow[0][P].d, nb(0), tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
             } else {
-                launch::contractRowDF<21, 0, 4>(P, dPatches, tabRow[0][P].d, nb(0), cDf, sDf, dIbuf, pfDf, s);
+                launch::contractRowDF<21, 0, 4>(P, dPatches, tabRow[0][P].d, nb(0), tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
             }
         }
         for (int P = 1; P <= 4; ++P) {
             auto nb = [&](int st) { return (long long)tabRow[st][P].h.size(); };
+            auto nbB = [&](int st) { return (long long)tabRowB[st][P].h.size(); };
             if (pd.dim == 3 && nh2) {
-                launch::contractRowDF<32, 0, 2>(P, dPatches, tabRow[1][P].d, nb(1), sDf, uDf, dIbuf, pfDf, s);
-                launch::contractRowDF<32, 2, 2>(P, dPatches, tabRow[1][P].d, nb(1), sDf, uDf, dIbuf, pfDf, s);
+                launch::contractRowDF<32, 0, 2>(P, dPatches, tabRow[1][P].d, nb(1), tabRowB[1][P].d, nbB(1), sDf, uDf, dIbuf, pfDf, s);
+                launch::contractRowDF<32, 2, 2>(P, dPatches, tabRow[1][P].d, nb(1), tabRowB[1][P].d, nbB(1), sDf, uDf, dIbuf, pfDf, s);
             } else if (pd.dim == 3) {
-                launch::contractRowDF<32, 0, 4>(P, dPatches, tabRow[1][P].d, nb(1), sDf, uDf, dIbuf, pfDf, s);
+                launch::contractRowDF<32, 0, 4>(P, dPatches, tabRow[1][P].d, nb(1), tabRowB[1][P].d, nbB(1), sDf, uDf, dIbuf, pfDf, s);
             } else {
-                launch::contractRowDF<22, 0, 1>(P, dPatches, tabRow[1][P].d, nb(1), sDf, bandDf, dIbuf, pfDf, s);
+                launch::contractRowDF<22, 0, 1>(P, dPatches, tabRow[1][P].d, nb(1), tabRowB[1][P].d, nbB(1), sDf, bandDf, dIbuf, pfDf, s);
             }
         }
         if (pd.dim == 3)
             for (int P = 1; P <= 4; ++P)
-                launch::contractRowDF<33, 0, 1>(P, dPatches, tabRow[2][P].d, (long long)tabRow[2][P].h.size(), uDf,
-                                                bandDf, dIbuf, pfDf, s);
+                launch::contractRowDF<33, 0, 1>(P, dPatches, tabRow[2][P].d, (long long)tabRow[2][P].h.size(),
+                                                tabRowB[2][P].d, (long long)tabRowB[2][P].h.size(), uDf, bandDf, dIbuf,
+                                                pfDf, s);
     } else if (pd.dim == 3) {
         launch::contract<double, 31>(dPatches, tabSt[0].d, (long long)tabSt[0].h.size(), dFieldC, dS, dIbuf, dPf, s);
         launch::contract<double, 32>(dPatches, tabSt[1].d, (long long)tabSt[1].h.size(), dS, dU, dIbuf, dPf, s);

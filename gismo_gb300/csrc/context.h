@@ -139,7 +139,8 @@ struct Context {
     float *dR32 = nullptr, *dZ32 = nullptr, *dP32 = nullptr, *dT32 = nullptr, *dDx32 = nullptr, *dXhi = nullptr,
           *dXlo = nullptr;
     Tab tabPf, tabCoef, tabGeo1, tabGeo2, tabPoint, tabSt[3], tabLd[3];
-    Tab tabRow[3][5];  // [stage][degree along the stage axis]
+    Tab tabRow[3][5];  // [stage][degree along the stage axis]: interior rows of simple axes
+    Tab tabRowB[3][5]; // the remaining rows
 
     // device buffers (solve)
     int solveN = -1;

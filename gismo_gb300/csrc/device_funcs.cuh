@@ -627,6 +627,90 @@ GS_HD void contractRowDF(const DevPatch& D, long long item, const df32* __restri
         for (int h = 0; h < NH; ++h) op[(H0 + h) * G.out_fs + w * G.inner] = acc[w][h].result();
 }
 
+// rows of the stage axis with the fixed support shape (D.simple): p <= i <= n-1-p; the others are
+// the boundary rows (all rows when the axis is not simple)
+// (single-output stages keep the general kernel for every row: their accumulators are few, and
+// the unrolled form only raises register pressure there)
+template <int KIND>
+GS_HD int interiorRows(const DevPatch& D) {
+    const int ax = Stage<KIND>::AX;
+    const int m = D.n[ax] - 2 * D.p[ax];
+    return Stage<KIND>::NOUT > 1 && D.simple[ax] && m > 0 ? m : 0;
+}
+template <int KIND>
+GS_HD long long stageInteriorWork(const DevPatch& D) {
+    const StageGeom g = stageGeom<KIND>(D);
+    return g.outer * interiorRows<KIND>(D) * g.inner;
+}
+template <int KIND>
+GS_HD long long stageBoundaryWork(const DevPatch& D) {
+    const StageGeom g = stageGeom<KIND>(D);
+    return g.outer * (D.n[Stage<KIND>::AX] - interiorRows<KIND>(D)) * g.inner;
+}
+// boundary item -> row-blocked item (rows 0..p-1 and n-p..n-1, or all rows)
+template <int KIND>
+GS_HD long long boundaryItem(const DevPatch& D, long long item) {
+    const StageGeom g = stageGeom<KIND>(D);
+    const int ax = Stage<KIND>::AX;
+    const int m = interiorRows<KIND>(D), nb = D.n[ax] - m;
+    const long long c = item % g.inner;
+    const long long r = item / g.inner;
+    const int ib = int(r % nb);
+    const long long o = r / nb;
+    const int i = (m > 0 && ib >= D.p[ax]) ? ib + m : ib;
+    return (o * D.n[ax] + i) * g.inner + c;
+}
+
+// interior rows: function i = p + (row index) has support elements i-p..i with first[e] = e, so
+// element k of the support contributes its local function t to band offset k + t; the element
+// and quadrature loops unroll and accumulate straight into the band accumulators
+template <int KIND, int P, int H0, int NH>
+GS_HD void contractRowDFInterior(const DevPatch& D, long long item, const df32* __restrict__ in,
+                                 df32* __restrict__ out, const df32* __restrict__ pf) {
+    using S = Stage<KIND>;
+    constexpr int P1 = P + 1, W = 2 * P + 1, Q = P + 1;
+    const int ax = S::AX;
+    const StageGeom G = stageGeom<KIND>(D);
+    const int n = D.n[ax], Qa = D.Q[ax], E = D.E[ax];
+    const int m = n - 2 * P;
+    const long long c = item % G.inner;
+    long long r = item / G.inner;
+    const int i = P + int(r % m);
+    const long long o = r / m;
+    Dot2 acc[W][NH];
+    const long long tstride = (long long)E * Q * P1 * P1;
+    const df32* pfa = pf + D.pfoff[ax];
+#pragma unroll
+    for (int k = 0; k <= P; ++k) {
+        const int e = i - P + k;  // local function of i on element e: si = P - k
+#pragma unroll
+        for (int rr = 0; rr < Q; ++rr) {
+            const int g = e * Q + rr;
+            df32 x[S::NIN];
+            const df32* ip = in + G.in_base + (o * Qa + g) * G.inner + c;
+#pragma unroll
+            for (int f = 0; f < S::NIN; ++f) x[f] = ip[f * G.in_fs];
+            const df32* prow = pfa + ((long long)g * P1 + (P - k)) * P1;
+#pragma unroll
+            for (int t = 0; t < P1; ++t) {
+                df32 pv[4];
+#pragma unroll
+                for (int tau = 0; tau < 4; ++tau) pv[tau] = prow[tau * tstride + t];
+#pragma unroll
+                for (int kk = 0; kk < S::NT; ++kk) {
+                    const Term tm = S::term(kk);
+                    if (tm.h >= H0 && tm.h < H0 + NH) acc[k + t][tm.h - H0].mac(pv[tm.tau], x[tm.f]);
+                }
+            }
+        }
+    }
+    df32* op = out + G.out_base + (o * n + i) * W * G.inner + c;
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+#pragma unroll
+        for (int h = 0; h < NH; ++h) op[(H0 + h) * G.out_fs + w * G.inner] = acc[w][h].result();
+}
+
 // degree dispatch of the row-blocked contraction (uniform per patch)
 template <int KIND, int H0, int NH>
 GS_HD void contractRowDFp(const DevPatch& D, long long item, const df32* __restrict__ in, df32* __restrict__ out,

@@ -23,6 +23,10 @@ struct DevPatch {
     int dim;
     int field_id;  // index of the patch's closed-form field constants (batches of independent problems)
     int p[3], n[3], E[3], q[3], Q[3], W[3];
+    // per axis: element e's first active function is e, function i's support is elements
+    // max(0, i-p)..min(E-1, i) (simple interior knots) and q = p + 1: the rows p..n-1-p then have
+    // a fixed support shape (the unrolled interior contraction)
+    int simple[3];
     int gp[3], gn[3];
     long long ngeo;   // geometry control points
     long long nq;     // quadrature points (Q0*Q1*Q2)

@@ -35,9 +35,10 @@ void contractDF(const DevPatch* P, const BlkEnt* tab, long long nblk, const df32
                 const df32* pf, cudaStream_t s);
 // degree-P specialisation over the patches whose degree along the stage axis is P
 // (degrees 1..4; the context checks the range)
+// interior rows (unrolled fixed-shape kernel, tabInt) and the remaining rows (tabBnd)
 template <int KIND, int H0, int NH>
-void contractRowDF(int P, const DevPatch* Pd, const BlkEnt* tab, long long nblk, const df32* in, df32* out,
-                   const int* ibuf, const df32* pf, cudaStream_t s);
+void contractRowDF(int P, const DevPatch* Pd, const BlkEnt* tabInt, long long nInt, const BlkEnt* tabBnd,
+                   long long nBnd, const df32* in, df32* out, const int* ibuf, const df32* pf, cudaStream_t s);
 template <int KIND, typename Tin>
 void loadContract(const DevPatch* P, const BlkEnt* tab, long long nblk, const Tin* in, double* out,
                   const double* basis, const int* ibuf, cudaStream_t s);

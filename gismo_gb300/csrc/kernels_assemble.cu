@@ -119,16 +119,32 @@ __global__ void __launch_bounds__(kBlock) k_contract_df(const DevPatch* __restri
     dev::contractItemDF<KIND>(D, item, in, out, ibuf, pf);
 }
 
+// interior rows of simple axes (fixed support shape, unrolled); two CTAs per SM
 template <int KIND, int DEG, int H0, int NH>
-__global__ void __launch_bounds__(kBlock) k_contract_row_df(const DevPatch* __restrict__ P,
-                                                            const BlkEnt* __restrict__ tab,
-                                                            const df32* __restrict__ in, df32* __restrict__ out,
-                                                            const int* __restrict__ ibuf,
-                                                            const df32* __restrict__ pf) {
+__global__ void __launch_bounds__(kBlock, 2) k_contract_row_df_int(const DevPatch* __restrict__ P,
+                                                                   const BlkEnt* __restrict__ tab,
+                                                                   const df32* __restrict__ in,
+                                                                   df32* __restrict__ out,
+                                                                   const df32* __restrict__ pf) {
     const BlkEnt be = tab[blockIdx.x];
     const DevPatch& D = P[be.patch];
     const long long item = be.base + threadIdx.x;
-    if (item >= dev::stageRowWork<KIND>(D)) return;
+    if (item >= dev::stageInteriorWork<KIND>(D)) return;
+    dev::contractRowDFInterior<KIND, DEG, H0, NH>(D, item, in, out, pf);
+}
+
+// the remaining (boundary) rows with the general element loop
+template <int KIND, int DEG, int H0, int NH>
+__global__ void __launch_bounds__(kBlock) k_contract_row_df_bnd(const DevPatch* __restrict__ P,
+                                                                const BlkEnt* __restrict__ tab,
+                                                                const df32* __restrict__ in, df32* __restrict__ out,
+                                                                const int* __restrict__ ibuf,
+                                                                const df32* __restrict__ pf) {
+    const BlkEnt be = tab[blockIdx.x];
+    const DevPatch& D = P[be.patch];
+    const long long bitem = be.base + threadIdx.x;
+    if (bitem >= dev::stageBoundaryWork<KIND>(D)) return;
+    const long long item = dev::boundaryItem<KIND>(D, bitem);
     if (D.q[dev::Stage<KIND>::AX] == DEG + 1)
         dev::contractRowDF<KIND, DEG, H0, NH, DEG + 1>(D, item, in, out, ibuf, pf);
     else
@@ -247,19 +263,25 @@ template void contractDF<21>(const DevPatch*, const BlkEnt*, long long, const df
 template void contractDF<22>(const DevPatch*, const BlkEnt*, long long, const df32*, df32*, const int*, const df32*, cudaStream_t);
 
 template <int KIND, int H0, int NH>
-void contractRowDF(int P, const DevPatch* Pd, const BlkEnt* tab, long long nblk, const df32* in, df32* out,
-                   const int* ibuf, const df32* pf, cudaStream_t s) {
-    if (nblk <= 0) return;
+void contractRowDF(int P, const DevPatch* Pd, const BlkEnt* tabInt, long long nInt, const BlkEnt* tabBnd,
+                   long long nBnd, const df32* in, df32* out, const int* ibuf, const df32* pf, cudaStream_t s) {
+#define ROW_CASE(DEG)                                                                                              \
+    case DEG:                                                                                                      \
+        if (nInt > 0) k_contract_row_df_int<KIND, DEG, H0, NH><<<unsigned(nInt), kBlock, 0, s>>>(Pd, tabInt, in, out, pf); \
+        if (nBnd > 0) k_contract_row_df_bnd<KIND, DEG, H0, NH><<<unsigned(nBnd), kBlock, 0, s>>>(Pd, tabBnd, in, out, ibuf, pf); \
+        break;
     switch (P) {
-        case 1: k_contract_row_df<KIND, 1, H0, NH><<<unsigned(nblk), kBlock, 0, s>>>(Pd, tab, in, out, ibuf, pf); break;
-        case 2: k_contract_row_df<KIND, 2, H0, NH><<<unsigned(nblk), kBlock, 0, s>>>(Pd, tab, in, out, ibuf, pf); break;
-        case 3: k_contract_row_df<KIND, 3, H0, NH><<<unsigned(nblk), kBlock, 0, s>>>(Pd, tab, in, out, ibuf, pf); break;
-        case 4: k_contract_row_df<KIND, 4, H0, NH><<<unsigned(nblk), kBlock, 0, s>>>(Pd, tab, in, out, ibuf, pf); break;
+        ROW_CASE(1)
+        ROW_CASE(2)
+        ROW_CASE(3)
+        ROW_CASE(4)
         default: break;
     }
+#undef ROW_CASE
 }
-#define INST_ROW(K, H0, NH) \
-    template void contractRowDF<K, H0, NH>(int, const DevPatch*, const BlkEnt*, long long, const df32*, df32*, const int*, const df32*, cudaStream_t);
+#define INST_ROW(K, H0, NH)                                                                                      \
+    template void contractRowDF<K, H0, NH>(int, const DevPatch*, const BlkEnt*, long long, const BlkEnt*, long long, \
+                                           const df32*, df32*, const int*, const df32*, cudaStream_t);
 INST_ROW(31, 0, 4)
 INST_ROW(31, 4, 4)
 INST_ROW(32, 0, 4)

@@ -71,6 +71,7 @@ static void layoutOnGrid(const ProblemDesc& pdl, const ProblemDesc& fine, const 
         const HostPatch& PF = fine.patches[pi];
         const DevPatch& FD = FL.dev[pi];
         DevPatch D = FD;  // quadrature grid, fields and geometry extents of the finest level
+        for (int k = 0; k < 3; ++k) D.simple[k] = 0;  // coarse functions on fine elements: general shape
         D.ndof = 1;
         D.bandsize = 1;
         for (int k = 0; k < 3; ++k) {

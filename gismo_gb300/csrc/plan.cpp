@@ -306,6 +306,13 @@ void buildLayout(const ProblemDesc& pd, Layout& L) {
             }
             for (int i = 0; i < D.n[k]; ++i) L.ibuf.push_back(ehi[i]);
             io += 2LL * D.n[k];
+            {
+                bool simple = D.q[k] == B.p + 1 && D.n[k] == D.E[k] + B.p;
+                for (int e = 0; e < D.E[k] && simple; ++e) simple = B.elementSpan(e) - B.p == e;
+                for (int i = 0; i < D.n[k] && simple; ++i)
+                    simple = elo[i] == std::max(0, i - B.p) && ehi[i] == std::min(D.E[k] - 1, i);
+                D.simple[k] = simple ? 1 : 0;
+            }
             D.gqoff[k] = io;
             for (int g = 0; g < D.Q[k]; ++g) L.ibuf.push_back(L.gqspan[D.qoff[k] + g] - G.p);
             io += D.Q[k];
