@@ -655,6 +655,7 @@ void Context::solveMixed(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
     B.part0 = dPart0; B.part1 = dPart1; B.part2 = dPart2;
     B.st = dCg;
     B.val_hi = dValHi; B.val_lo = dValLo; B.dinv32 = dDinv32;
+    if (const char* e = std::getenv("GSGPU_MIXED_DELTA")) B.delta = std::atof(e);  // tuning override
     B.r32 = dR32; B.z32 = dZ32; B.p32 = dP32; B.t32 = dT32; B.dx32 = dDx32; B.xhi = dXhi; B.xlo = dXlo;
     const double tol = o.tol > 0 ? o.tol : 1e-10;
     const int maxit = o.max_iters > 0 ? o.max_iters : 1000;

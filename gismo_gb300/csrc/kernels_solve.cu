@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(kB) k_init(int n, const double* __restrict__ b
 
 __global__ void __launch_bounds__(kB) k_init_reduce(int nparts, const double* __restrict__ pbb,
                                                     const double* __restrict__ prz, CgState* __restrict__ st,
-                                                    double tol, int maxit) {
+                                                    double tol, int maxit, double delta) {
     const double bb = reducePartials(pbb, nparts);
     const double rz = reducePartials(prz, nparts);
     if (threadIdx.x == 0) {
@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(kB) k_init_reduce(int nparts, const double* __
         st->replaced = 0;
         st->restart = 0;
         st->last_true = 1.0;
-        st->delta = 1e-2;
+        st->delta = delta;
         // zero rhs: x = 0 is the solution; x0 = 0 gives ||r||/||b|| = 1 >= tol otherwise
         st->done = (bb == 0.0 || 1.0 < tol) ? 1 : (maxit <= 0 ? 2 : 0);
     }
@@ -464,7 +464,7 @@ void jacobiDiag(int n, const int* diag, const double* val, double damping, doubl
 void cgInit(const CgBuffers& B, double tol, int maxit, cudaStream_t s) {
     const int np = cgPartials(B.n);
     k_init<<<np, kB, 0, s>>>(B.n, B.b, B.x, B.r, B.z, B.p, B.dinv, B.part0, B.part1);
-    k_init_reduce<<<1, kB, 0, s>>>(np, B.part0, B.part1, B.st, tol, maxit);
+    k_init_reduce<<<1, kB, 0, s>>>(np, B.part0, B.part1, B.st, tol, maxit, B.delta);
 }
 
 // launch a row kernel template for the lanes-per-row and column-format choice of B
@@ -511,7 +511,7 @@ void jacobiDiag32(int n, const int* diag, const float* val_hi, float* dinv32, cu
 void mixedInit(const CgBuffers& B, double tol, int maxit, cudaStream_t s) {
     const int np = cgPartials(B.n);
     k_init_m<<<np, kB, 0, s>>>(B.n, B.b, B.x, B.r, B.dx32, B.r32, B.z32, B.p32, B.dinv32, B.part0, B.part1);
-    k_init_reduce<<<1, kB, 0, s>>>(np, B.part0, B.part1, B.st, tol, maxit);
+    k_init_reduce<<<1, kB, 0, s>>>(np, B.part0, B.part1, B.st, tol, maxit, B.delta);
 }
 
 void mixedSpmv(const CgBuffers& B, cudaStream_t s) {

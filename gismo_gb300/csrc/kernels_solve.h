@@ -24,6 +24,7 @@ struct CgState {
 struct CgBuffers {
     int n = 0;
     int lanes_per_row = 32;
+    double delta = 1e-2;  // mixed: residual replacement once the recursive residual dropped by this factor
     const int* ptr = nullptr;
     const int* col = nullptr;
     const int16_t* coff = nullptr;  // if set: column = row + coff[k] (banded patterns), col unused
