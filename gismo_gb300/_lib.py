@@ -15,7 +15,7 @@ EXPORTS = [
     "gsgpu_solve", "gsgpu_l2_error", "gsgpu_min_jacobian", "gsgpu_assemble_times", "gsgpu_stream",
     "gsgpu_set_profiling", "gsgpu_spmv_stats", "gsgpu_cg_jacobi_noalloc", "gsgpu_set_batch", "gsgpu_batch_info",
     "gsgpu_batch_l2_error", "gsgpu_server_create", "gsgpu_server_submit", "gsgpu_server_wait",
-    "gsgpu_server_last_error", "gsgpu_server_destroy",
+    "gsgpu_server_last_error", "gsgpu_server_destroy", "gsgpu_apply", "gsgpu_mg_apply",
 ]
 
 OK, ERR_INVALID, ERR_CUDA, ERR_BUDGET, ERR_NOT_CONVERGED, ERR_JACOBIAN, ERR_STATE, ERR_TIMEOUT = range(8)
@@ -97,6 +97,8 @@ def lib() -> C.CDLL:
         L.gsgpu_server_last_error.argtypes = [vp]
         L.gsgpu_server_last_error.restype = C.c_char_p
         L.gsgpu_server_destroy.argtypes = [vp]
+        L.gsgpu_apply.argtypes = [vp, vp, vp]
+        L.gsgpu_mg_apply.argtypes = [vp, C.POINTER(SolverOpts), vp, vp]
         L.gsgpu_min_jacobian.argtypes = [vp, C.POINTER(C.c_double)]
         L.gsgpu_assemble_times.argtypes = [vp, vp]
         L.gsgpu_stream.argtypes = [vp, C.POINTER(vp)]

@@ -146,6 +146,24 @@ class GpuPoissonAssembler:
         self._check(self.L.gsgpu_dof_map(self.h, out.ctypes.data))
         return out
 
+    def apply(self, x: np.ndarray) -> np.ndarray:
+        """gsMatrixOp::apply on the device: K x with the assembled FP64 matrix."""
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.empty_like(x)
+        self._check(self.L.gsgpu_apply(self.h, x.ctypes.data, y.ctypes.data))
+        return y
+
+    def mg_apply(self, r: np.ndarray, mg_levels: int = 4, mg_npre: int = 2, mg_npost: int = 2,
+                 mg_damping: float = 0.6) -> np.ndarray:
+        """gsMultiGridOp as a preconditioner: one FP64 V-cycle on r from a zero start."""
+        o = SolverOpts()
+        o.method, o.precision = _lib.SOLVER_CG_MG, _lib.PREC_FP64
+        o.mg_levels, o.mg_npre, o.mg_npost, o.mg_damping = mg_levels, mg_npre, mg_npost, mg_damping
+        r = np.ascontiguousarray(r, np.float64)
+        z = np.empty_like(r)
+        self._check(self.L.gsgpu_mg_apply(self.h, C.byref(o), r.ctypes.data, z.ctypes.data))
+        return z
+
     def l2_error(self) -> float:
         """gsField::distanceL2 of the last solution against the manufactured solution."""
         v = C.c_double()

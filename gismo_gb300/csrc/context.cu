@@ -391,6 +391,31 @@ void Context::assemble(int precision) {
     if (!(detMin > 0.0)) throw JacobianError("geometry map has det J <= 0 at a quadrature point");
 }
 
+// y = K x with the assembled FP64 matrix (the CG SpMV kernel); x, y on the host
+void Context::applyMatrix(const double* x, double* y) {
+    if (!assembled || assembledPrecision != kFP64) throw StateError("apply() needs assemble(GSGPU_PREC_FP64)");
+    ensureSolveBuffers();
+    cudaStream_t s = stream;
+    GSGPU_CUDA_TRY(cudaMemcpyAsync(dP, x, sizeof(double) * size_t(pat.n), cudaMemcpyHostToDevice, s));
+    GSGPU_CUDA_TRY(cudaMemsetAsync(dCg, 0, sizeof(CgState), s));  // a running state: the kernel is not skipped
+    CgBuffers B;
+    B.n = pat.n;
+    B.lanes_per_row = lanesPerRow(true);
+    B.ptr = dPtr;
+    B.col = dCol;
+    B.coff = dColOff;
+    B.val = dVal;
+    B.p = dP;
+    B.t = dT;
+    B.part2 = dPart2;
+    B.st = dCg;
+    launch::cgSpmv(B, s);
+    GSGPU_CUDA_TRY(cudaMemcpyAsync(y, dT, sizeof(double) * size_t(pat.n), cudaMemcpyDeviceToHost, s));
+    GSGPU_CUDA_TRY(cudaGetLastError());
+    GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    solved = false;  // the CG state was overwritten
+}
+
 // gsField::distanceL2 of the last solution: the geometry stages are re-run in FP64 (after a
 // mixed-precision assembly their buffers hold double-float values), then one quadrature kernel
 std::vector<double> Context::l2PerPatch() {
@@ -976,6 +1001,22 @@ int gsgpu_solve(gsgpu_context* ctx, const gsgpu_solver_opts* opts, double* x, gs
         return GSGPU_ERR_NOT_CONVERGED;
     }
     return rc;
+}
+
+int gsgpu_apply(gsgpu_context* ctx, const double* x, double* y) {
+    if (!x || !y) return GSGPU_ERR_INVALID;
+    return guarded(ctx, [&] {
+        if (ctx->c.batch) throw std::invalid_argument("apply() is not available for batches");
+        ctx->c.applyMatrix(x, y);
+    });
+}
+
+int gsgpu_mg_apply(gsgpu_context* ctx, const gsgpu_solver_opts* opts, const double* r, double* z) {
+    if (!opts || !r || !z) return GSGPU_ERR_INVALID;
+    return guarded(ctx, [&] {
+        if (ctx->c.batch) throw std::invalid_argument("mg_apply() is not available for batches");
+        ctx->c.mgApply(*opts, r, z);
+    });
 }
 
 int gsgpu_l2_error(gsgpu_context* ctx, double* err) {

@@ -181,6 +181,10 @@ struct Context {
     void segRun(const SegCg<T>& B, cudaGraphExec_t& exec, int maxit);
     template <typename T>
     void mgRun(const gsgpu_solver_opts& o, gsgpu_solve_info& info, bool mixed);
+    template <typename T>
+    void mgPrepare(const gsgpu_solver_opts& o, bool mixed, std::vector<MgLevelDev<T>>& lv, MgParams& prm);
+    void mgApply(const gsgpu_solver_opts& o, const double* r, double* z);
+    void applyMatrix(const double* x, double* y);
     // profiling of the solver's SpMV launches
     bool profiling = false;
     long long spmvLaunches = 0;

@@ -200,8 +200,10 @@ void Context::mgAssemble(bool mixed) {
     mgCoarseIters = 0;  // the coarse operator changed: size the coarse iteration cap again
 }
 
+// device views of the hierarchy (vectors allocated on first use), Jacobi diagonals and the
+// V-cycle parameters (the coarse iteration cap is sized once per assembly)
 template <typename T>
-void Context::mgRun(const gsgpu_solver_opts& o, gsgpu_solve_info& info, bool mixed) {
+void Context::mgPrepare(const gsgpu_solver_opts& o, bool mixed, std::vector<MgLevelDev<T>>& lv, MgParams& prm) {
     cudaStream_t s = stream;
     const int n = pat.n;
     const int nl = int(mgl.size()) + 1;
@@ -218,7 +220,7 @@ void Context::mgRun(const gsgpu_solver_opts& o, gsgpu_solve_info& info, bool mix
     if (!dMgCoarseSt) dMgCoarseSt = static_cast<CgState*>(arena.alloc(sizeof(CgState)));
     if (!dMgSt) dMgSt = static_cast<CgState*>(arena.alloc(sizeof(CgState)));
 
-    std::vector<MgLevelDev<T>> lv(nl);
+    lv.assign(nl, MgLevelDev<T>());
     {
         MgLevelDev<T>& A = lv[0];
         A.n = n;
@@ -268,7 +270,7 @@ void Context::mgRun(const gsgpu_solver_opts& o, gsgpu_solve_info& info, bool mix
     }
     for (const MgLevelDev<T>& A : lv) launch::mgDinv<T>(A, s);
 
-    MgParams prm;
+    prm = MgParams();
     prm.npre = o.mg_npre >= 0 ? o.mg_npre : 2;
     prm.npost = o.mg_npost >= 0 ? o.mg_npost : 2;
     prm.damping = o.mg_damping > 0 ? o.mg_damping : 0.6;
@@ -299,6 +301,17 @@ void Context::mgRun(const gsgpu_solver_opts& o, gsgpu_solve_info& info, bool mix
         mgCoarseTol = prm.coarse_tol;
     }
     prm.coarse_iters = mgCoarseIters;
+}
+
+template <typename T>
+void Context::mgRun(const gsgpu_solver_opts& o, gsgpu_solve_info& info, bool mixed) {
+    cudaStream_t s = stream;
+    const int n = pat.n;
+    const int nl = int(mgl.size()) + 1;
+    const int np = launch::mgPartials();
+    std::vector<MgLevelDev<T>> lv;
+    MgParams prm;
+    mgPrepare<T>(o, mixed, lv, prm);
 
     MgOuter O;
     O.n = n;
@@ -362,6 +375,25 @@ void Context::mgRun(const gsgpu_solver_opts& o, gsgpu_solve_info& info, bool mix
     info.relres = hs.relres;
     info.refinements = 0;
     lastConverged = hs.done == 1;
+}
+
+// one FP64 V-cycle z = MG(r) from a zero start (gsMultiGridOp as a preconditioner); r, z on the host
+void Context::mgApply(const gsgpu_solver_opts& o, const double* r, double* z) {
+    if (!assembled || assembledPrecision != kFP64) throw StateError("mg_apply() needs assemble(GSGPU_PREC_FP64)");
+    const int levels = o.mg_levels > 0 ? o.mg_levels : 4;
+    if (levels < 2) throw std::invalid_argument("multigrid needs at least 2 levels");
+    ensureSolveBuffers();
+    mgSetup(levels);
+    mgAssemble(false);
+    std::vector<MgLevelDev<double>> lv;
+    MgParams prm;
+    mgPrepare<double>(o, false, lv, prm);
+    cudaStream_t s = stream;
+    GSGPU_CUDA_TRY(cudaMemcpyAsync(lv[0].b, r, sizeof(double) * size_t(pat.n), cudaMemcpyHostToDevice, s));
+    launch::vcycle<double>(lv, 0, prm, nullptr, s);
+    GSGPU_CUDA_TRY(cudaMemcpyAsync(z, lv[0].x, sizeof(double) * size_t(pat.n), cudaMemcpyDeviceToHost, s));
+    GSGPU_CUDA_TRY(cudaGetLastError());
+    GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
 }
 
 void Context::solveMG(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {

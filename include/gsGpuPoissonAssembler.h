@@ -19,6 +19,8 @@
 #pragma once
 
 #include <gsAssembler/gsPoissonAssembler.h>
+#include <gsIO/gsOptionList.h>
+#include <gsSolver/gsLinearOperator.h>
 #include <gsNurbs/gsTensorBSpline.h>
 #include <gsNurbs/gsTensorBSplineBasis.h>
 
@@ -89,14 +91,55 @@ public:
     /// CG (+ Jacobi) on the device-resident system (gsConjugateGradient(matrix(), gsJacobiOp))
     int solve(gsMatrix<T>& x, double tol = 1e-10, int maxIter = 1000) {
         gsgpu_solver_opts o = {GSGPU_SOLVER_CG_JACOBI, GSGPU_PREC_FP64, tol, maxIter, 4, 2, 2, 0.6, 1e-4};
+        return run(o, x);
+    }
+
+    /// gsConjugateGradient(matrix(), gsJacobiOp | gsMultiGridOp).setOptions(opt).solve(rhs(), x) on
+    /// the device, with G+Smo's option names: "Tolerance", "MaxIterations" (gsIterativeSolver.h:92-99),
+    /// "Preconditioner" ("Jacobi" or "MultiGrid"), the multigrid's "Levels" (gsGridHierarchy),
+    /// "NumPreSmooth", "NumPostSmooth" (gsMultiGrid.hpp:299-328) and the smoother's "Damping"
+    /// (gsJacobiOp), plus "Precision" ("fp64" or "mixed": re-assembles the double-float operator on
+    /// the device; matrix() keeps the FP64 system). Returns the iteration count; error() gives the
+    /// final relative residual as gsIterativeSolver::error() does.
+    int solve(const gsOptionList& opt, gsMatrix<T>& x) {
+        gsgpu_solver_opts o = {};
+        o.method = opt.askString("Preconditioner", "Jacobi") == "MultiGrid" ? GSGPU_SOLVER_CG_MG : GSGPU_SOLVER_CG_JACOBI;
+        o.precision = opt.askString("Precision", "fp64") == "mixed" ? GSGPU_PREC_MIXED : GSGPU_PREC_FP64;
+        o.tol = opt.askReal("Tolerance", 1e-10);
+        o.max_iters = opt.askInt("MaxIterations", 1000);
+        o.mg_levels = opt.askInt("Levels", 4);
+        o.mg_npre = opt.askInt("NumPreSmooth", 2);
+        o.mg_npost = opt.askInt("NumPostSmooth", 2);
+        o.mg_damping = opt.askReal("Damping", 0.6);
+        o.inner_tol = 1e-4;
+        if (o.precision == GSGPU_PREC_MIXED) check(gsgpu_assemble(m_ctx, GSGPU_PREC_MIXED));
+        const int its = run(o, x);
+        if (o.precision == GSGPU_PREC_MIXED) check(gsgpu_assemble(m_ctx, GSGPU_PREC_FP64));
+        return its;
+    }
+
+    /// relative residual of the last solve (gsIterativeSolver::error())
+    double error() const { return m_error; }
+
+    /// gsField::distanceL2 of the last device solution against the manufactured solution
+    double distanceL2() const {
+        double e = 0.0;
+        check(gsgpu_l2_error(m_ctx, &e));
+        return e;
+    }
+
+    gsgpu_context* context() const { return m_ctx; }
+
+private:
+    int run(const gsgpu_solver_opts& o, gsMatrix<T>& x) {
         gsgpu_solve_info info;
         x.resize(this->numDofs(), 1);
         const int rc = gsgpu_solve(m_ctx, &o, x.data(), &info);
         if (rc != GSGPU_OK && rc != GSGPU_ERR_NOT_CONVERGED) check(rc);
+        m_error = info.relres;
         return info.iterations;
     }
 
-private:
     void check(int rc) const {
         if (rc != GSGPU_OK)
             throw std::runtime_error(std::string("gsgpu: ") + (m_ctx ? gsgpu_last_error(m_ctx) : "no context"));
@@ -172,9 +215,66 @@ private:
     }
 
     gsgpu_context* m_ctx = nullptr;
+    double m_error = 0.0;
     gsGpuFields m_fields;
     std::vector<int> m_degree, m_nknots, m_gdegree, m_gnknots, m_ifaces, m_dsides;
     std::vector<double> m_knots, m_gknots, m_coefs;
+};
+
+/// The assembled device matrix as a gsLinearOperator (gsMatrixOp semantics: x = K input, column
+/// by column), so G+Smo's own solvers can run on the GPU operator
+template <class T = real_t>
+class gsGpuMatrixOp : public gsLinearOperator<T> {
+public:
+    explicit gsGpuMatrixOp(const gsGpuPoissonAssembler<T>& A) : m_ctx(A.context()), m_n(A.numDofs()) {}
+    void apply(const gsMatrix<T>& input, gsMatrix<T>& x) const override {
+        x.resize(m_n, input.cols());
+        for (index_t c = 0; c < input.cols(); ++c) {
+            gsMatrix<T> in = input.col(c), out(m_n, 1);
+            if (gsgpu_apply(m_ctx, in.data(), out.data()) != GSGPU_OK)
+                throw std::runtime_error(std::string("gsgpu: ") + gsgpu_last_error(m_ctx));
+            x.col(c) = out;
+        }
+    }
+    index_t rows() const override { return m_n; }
+    index_t cols() const override { return m_n; }
+
+private:
+    gsgpu_context* m_ctx;
+    index_t m_n;
+};
+
+/// gsMultiGridOp as a preconditioner on the device (gsPreconditionerOp::apply: one V-cycle from a
+/// zero start, gsMultiGrid.hpp:147-201); setOptions takes "Levels", "NumPreSmooth",
+/// "NumPostSmooth" and "Damping"
+template <class T = real_t>
+class gsGpuMultiGridOp : public gsLinearOperator<T> {
+public:
+    explicit gsGpuMultiGridOp(const gsGpuPoissonAssembler<T>& A) : m_ctx(A.context()), m_n(A.numDofs()) {
+        m_opts = {GSGPU_SOLVER_CG_MG, GSGPU_PREC_FP64, 0.0, 0, 4, 2, 2, 0.6, 0.0};
+    }
+    void setOptions(const gsOptionList& opt) override {
+        m_opts.mg_levels = opt.askInt("Levels", m_opts.mg_levels);
+        m_opts.mg_npre = opt.askInt("NumPreSmooth", m_opts.mg_npre);
+        m_opts.mg_npost = opt.askInt("NumPostSmooth", m_opts.mg_npost);
+        m_opts.mg_damping = opt.askReal("Damping", m_opts.mg_damping);
+    }
+    void apply(const gsMatrix<T>& input, gsMatrix<T>& x) const override {
+        x.resize(m_n, input.cols());
+        for (index_t c = 0; c < input.cols(); ++c) {
+            gsMatrix<T> in = input.col(c), out(m_n, 1);
+            if (gsgpu_mg_apply(m_ctx, &m_opts, in.data(), out.data()) != GSGPU_OK)
+                throw std::runtime_error(std::string("gsgpu: ") + gsgpu_last_error(m_ctx));
+            x.col(c) = out;
+        }
+    }
+    index_t rows() const override { return m_n; }
+    index_t cols() const override { return m_n; }
+
+private:
+    gsgpu_context* m_ctx;
+    index_t m_n;
+    gsgpu_solver_opts m_opts;
 };
 
 }  // namespace gismo

@@ -129,6 +129,13 @@ int gsgpu_dof_map(gsgpu_context* ctx, int* index);
  * (gsIterativeSolver.h:114-125, gsConjugateGradient.hpp:19-84). x: host array of nfree values
  * (may be NULL to keep the solution on the device only). */
 int gsgpu_solve(gsgpu_context* ctx, const gsgpu_solver_opts* opts, double* x, gsgpu_solve_info* info);
+/* gsMatrixOp::apply (gsMatrixOp.h:74-75) on the device: y = K x with the assembled FP64 matrix
+ * (host arrays of nfree values), so that G+Smo's own solvers can run on the GPU operator */
+int gsgpu_apply(gsgpu_context* ctx, const double* x, double* y);
+/* gsMultiGridOp as a preconditioner (gsPreconditionerOp::apply, gsPreconditioner.h:79-84, and
+ * multiGridStep, gsMultiGrid.hpp:147-201): z = one FP64 V-cycle on r from a zero start, with the
+ * hierarchy and smoother options of opts (mg_levels, mg_npre, mg_npost, mg_damping) */
+int gsgpu_mg_apply(gsgpu_context* ctx, const gsgpu_solver_opts* opts, const double* r, double* z);
 /* gsField::distanceL2 of the last solution against u (gsField.hpp:23-41) */
 int gsgpu_l2_error(gsgpu_context* ctx, double* err);
 

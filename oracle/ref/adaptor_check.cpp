@@ -4,6 +4,7 @@
 #include <gsCore/gsMultiBasis.h>
 #include <gsCore/gsFunctionExpr.h>
 #include <gsNurbs/gsKnotVector.h>
+#include <gsSolver/gsConjugateGradient.h>
 #include "gsGpuPoissonAssembler.h"
 using namespace gismo;
 int main(int argc, char**) {
@@ -22,7 +23,25 @@ int main(int argc, char**) {
         A.assemble();
         gsMatrix<> x;
         A.solve(x);
-        return int(A.matrix().nonZeros() + x.rows());
+        gsOptionList opt;
+        opt.addString("Preconditioner", "", "MultiGrid");
+        opt.addInt("Levels", "", 3);
+        A.solve(opt, x);
+        // G+Smo's own CG on the device operator and V-cycle
+        gsGpuMatrixOp<> K(A);
+        gsGpuMultiGridOp<> M(A);
+        M.setOptions(opt);
+        gsMatrix<> y, z;
+        K.apply(x, y);
+        M.apply(y, z);
+        // the reference's own CG driven by the device operator and the device V-cycle
+        gsLinearOperator<>::Ptr Kp(new gsGpuMatrixOp<>(A)), Mp(new gsGpuMultiGridOp<>(A));
+        gsConjugateGradient<> cg(Kp, Mp);
+        cg.setTolerance(1e-8);
+        gsMatrix<> xs;
+        xs.setZero(A.numDofs(), 1);
+        cg.solve(A.rhs(), xs);
+        return int(A.matrix().nonZeros() + x.rows() + z.rows() + A.distanceL2() + A.error() + cg.iterations());
     }
     return 0;
 }
