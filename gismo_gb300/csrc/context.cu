@@ -116,12 +116,108 @@ void Context::refresh() {
     if (device >= 0) freeAssembly();
     buildDofMap(pd, map);
     buildLayout(pd, L);
-    buildPattern(pd, map, L, pat, 0);
+    // problems without interfaces get their pattern built on the device (no host non-zeros)
+    RowPlan rp;
+    devPattern = device >= 0 && std::getenv("GSGPU_HOST_PATTERN") == nullptr && rowPlanSingle(pd, map, L, rp);
+    if (devPattern) {
+        pat = Pattern();
+        pat.n = map.freeSize;
+    } else {
+        buildPattern(pd, map, L, pat, 0);
+        nnz = (long long)pat.col.size();
+    }
     if (batch) segRow = segmentRows(pd, map);
     if (device < 0) {  // host-only context: the plan, no device buffers
         refreshed = true;
         return;
     }
+    refreshUploads();
+    if (devPattern) patternOnDevice(rp);
+    else patternFromHost();
+    if (batch) batchSetup();
+    allocN(arena, dVal, nnz);
+    allocN(arena, dRhs, pat.n);
+    allocN(arena, dDdof, std::max(1, map.boundarySize));
+    allocN(arena, dDetKey, 1);
+    buildTables();
+    // the control points of the problem
+    std::vector<double> raw;
+    for (const HostPatch& P : pd.patches) raw.insert(raw.end(), P.coefs.begin(), P.coefs.end());
+    GSGPU_CUDA_TRY(cudaMemcpyAsync(dCoefRaw, raw.data(), raw.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
+    launch::coefsToSoa(dPatches, tabCoef.d, (long long)tabCoef.h.size(), dCoefRaw, dCoefs, stream);
+    GSGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+    refreshed = true;
+    assembled = false;
+    solved = false;
+}
+
+// sparsity pattern, gather maps and diagonal slots on the device from the row plan
+void Context::patternOnDevice(const RowPlan& rp) {
+    cudaStream_t s = stream;
+    const int n = pat.n;
+    int *dRowPatch = nullptr, *dRowLoc = nullptr, *dRng = nullptr, *dPoff = nullptr, *dFlags = nullptr;
+    long long *dRngOff = nullptr, *cnt0 = nullptr, *cnt1 = nullptr, *sums = nullptr;
+    std::vector<int> poff;
+    for (const HostPatch& P : pd.patches) poff.push_back(P.offset);
+    upload(arena, dRowPatch, rp.rowPatch, s);
+    upload(arena, dRowLoc, rp.rowLoc, s);
+    upload(arena, dRng, rp.rng.empty() ? std::vector<int>(1, 0) : rp.rng, s);
+    upload(arena, dRngOff, rp.rngOff, s);
+    upload(arena, dPoff, poff, s);
+    allocN(arena, cnt0, n + 1LL);
+    allocN(arena, cnt1, n + 1LL);
+    allocN(arena, sums, std::max(1LL, launch::scanScratch(n + 1LL)));
+    allocN(arena, dFlags, 2);
+    GSGPU_CUDA_TRY(cudaMemsetAsync(dFlags, 0, 2 * sizeof(int), s));
+    launch::RowPlanDev R;
+    R.n = n;
+    R.nfree = map.freeSize;
+    R.rowPatch = dRowPatch;
+    R.rowLoc = dRowLoc;
+    R.rng = dRng;
+    R.rngOff = dRngOff;
+    R.index = dIndex;
+    R.poff = dPoff;
+    launch::patternCount(dPatches, R, cnt0, cnt1, sums, s);
+    long long tot[2] = {0, 0};
+    GSGPU_CUDA_TRY(cudaMemcpyAsync(&tot[0], cnt0 + n, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    GSGPU_CUDA_TRY(cudaMemcpyAsync(&tot[1], cnt1 + n, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    if (tot[0] >= (1LL << 31)) throw std::invalid_argument("more than 2^31 non-zeros");
+    if (L.band >= (long long)Pattern::kMulti) throw std::invalid_argument("band too large for 31-bit band indexing");
+    nnz = tot[0];
+    allocN(arena, dPtr, n + 1LL);
+    allocN(arena, dCol, std::max(1LL, nnz));
+    allocN(arena, dSrc, std::max(1LL, nnz));
+    allocN(arena, dFptr, n + 1LL);
+    allocN(arena, dFband, std::max(1LL, tot[1]));
+    allocN(arena, dFbidx, std::max(1LL, tot[1]));
+    allocN(arena, dDiag, std::max(1, n));
+    allocN(arena, dLptr, n + 1LL);
+    allocN(arena, dLidx, std::max(1, n));
+    upload(arena, dOvfPtr, std::vector<uint32_t>(1, 0), s);
+    upload(arena, dOvfIdx, std::vector<uint32_t>(1, 0), s);
+    launch::patternFill(dPatches, R, cnt0, cnt1, dPtr, dCol, dSrc, dFptr, dFband, dFbidx, dDiag, dLptr, dLidx, dFlags,
+                        s);
+    int flags[2] = {0, 0};
+    GSGPU_CUDA_TRY(cudaMemcpyAsync(flags, dFlags, sizeof(flags), cudaMemcpyDeviceToHost, s));
+    GSGPU_CUDA_TRY(cudaGetLastError());
+    GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    if (flags[0]) throw std::runtime_error("device pattern: a row without its diagonal or with unordered columns");
+    arena.release(dColOff);
+    dColOff = nullptr;
+    if (flags[1] <= 32767 && nnz > 0) {  // banded patterns: 16-bit column offsets from the row
+        allocN(arena, dColOff, nnz);
+        launch::patternColOffsets(n, dPtr, dCol, dColOff, s);
+    }
+    GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    for (void* p : {(void*)dRowPatch, (void*)dRowLoc, (void*)dRng, (void*)dRngOff, (void*)dPoff, (void*)cnt0,
+                    (void*)cnt1, (void*)sums, (void*)dFlags})
+        arena.release(p);
+}
+
+// the host pattern: diagonal slots, uploads and 16-bit column offsets when they fit
+void Context::patternFromHost() {
     // diagonal slot of every row (Jacobi)
     diag.assign(pat.n, -1);
     int nodiag = 0;
@@ -134,6 +230,38 @@ void Context::refresh() {
         else diag[r] = pat.ptr[r] + int(f - b);
     }
     if (nodiag) throw std::runtime_error("pattern has no diagonal entry");
+    upload(arena, dPtr, pat.ptr, stream);
+    upload(arena, dCol, pat.col, stream);
+    upload(arena, dSrc, pat.src, stream);
+    upload(arena, dOvfPtr, pat.ovf_ptr.empty() ? std::vector<uint32_t>(1, 0) : pat.ovf_ptr, stream);
+    upload(arena, dOvfIdx, pat.ovf_idx.empty() ? std::vector<uint32_t>(1, 0) : pat.ovf_idx, stream);
+    upload(arena, dLptr, pat.lptr, stream);
+    upload(arena, dLidx, pat.lidx, stream);
+    upload(arena, dFptr, pat.fptr, stream);
+    upload(arena, dFband, pat.fband.empty() ? std::vector<uint32_t>(1, 0) : pat.fband, stream);
+    upload(arena, dFbidx, pat.fbidx.empty() ? std::vector<uint32_t>(1, 0) : pat.fbidx, stream);
+    upload(arena, dDiag, diag, stream);
+    {
+        // banded patterns (single patches) store columns as 16-bit offsets from the row
+        int far = 0;
+#pragma omp parallel for schedule(static) reduction(+ : far)
+        for (int r = 0; r < pat.n; ++r)
+            for (int k = pat.ptr[r]; k < pat.ptr[r + 1]; ++k)
+                if (pat.col[k] - r > 32767 || pat.col[k] - r < -32768) ++far;
+        arena.release(dColOff);
+        dColOff = nullptr;
+        if (far == 0 && !pat.col.empty()) {
+            bigvec<int16_t> off(pat.col.size());
+#pragma omp parallel for schedule(static)
+            for (int r = 0; r < pat.n; ++r)
+                for (int k = pat.ptr[r]; k < pat.ptr[r + 1]; ++k) off[k] = int16_t(pat.col[k] - r);
+            upload(arena, dColOff, off, stream);
+        }
+    }
+}
+
+// patch data, tables and the assembly buffers (everything but the pattern)
+void Context::refreshUploads() {
     upload(arena, dPatches, L.dev, stream);
     {
         std::vector<dev::FieldConst<double>> fc64;
@@ -172,50 +300,7 @@ void Context::refresh() {
     allocN(arena, dLv1, L.lv1);
     allocN(arena, dLv2, std::max(1LL, L.lv2));
     allocN(arena, dLvec, L.lvec);
-    upload(arena, dPtr, pat.ptr, stream);
-    upload(arena, dCol, pat.col, stream);
-    upload(arena, dSrc, pat.src, stream);
-    upload(arena, dOvfPtr, pat.ovf_ptr.empty() ? std::vector<uint32_t>(1, 0) : pat.ovf_ptr, stream);
-    upload(arena, dOvfIdx, pat.ovf_idx.empty() ? std::vector<uint32_t>(1, 0) : pat.ovf_idx, stream);
-    upload(arena, dLptr, pat.lptr, stream);
-    upload(arena, dLidx, pat.lidx, stream);
-    upload(arena, dFptr, pat.fptr, stream);
-    upload(arena, dFband, pat.fband.empty() ? std::vector<uint32_t>(1, 0) : pat.fband, stream);
-    upload(arena, dFbidx, pat.fbidx.empty() ? std::vector<uint32_t>(1, 0) : pat.fbidx, stream);
-    upload(arena, dDiag, diag, stream);
     upload(arena, dIndex, map.index, stream);
-    if (batch) batchSetup();
-    {
-        // banded patterns (single patches) store columns as 16-bit offsets from the row
-        int far = 0;
-#pragma omp parallel for schedule(static) reduction(+ : far)
-        for (int r = 0; r < pat.n; ++r)
-            for (int k = pat.ptr[r]; k < pat.ptr[r + 1]; ++k)
-                if (pat.col[k] - r > 32767 || pat.col[k] - r < -32768) ++far;
-        arena.release(dColOff);
-        dColOff = nullptr;
-        if (far == 0 && !pat.col.empty()) {
-            bigvec<int16_t> off(pat.col.size());
-#pragma omp parallel for schedule(static)
-            for (int r = 0; r < pat.n; ++r)
-                for (int k = pat.ptr[r]; k < pat.ptr[r + 1]; ++k) off[k] = int16_t(pat.col[k] - r);
-            upload(arena, dColOff, off, stream);
-        }
-    }
-    allocN(arena, dVal, (long long)pat.col.size());
-    allocN(arena, dRhs, pat.n);
-    allocN(arena, dDdof, std::max(1, map.boundarySize));
-    allocN(arena, dDetKey, 1);
-    buildTables();
-    // the control points of the problem
-    std::vector<double> raw;
-    for (const HostPatch& P : pd.patches) raw.insert(raw.end(), P.coefs.begin(), P.coefs.end());
-    GSGPU_CUDA_TRY(cudaMemcpyAsync(dCoefRaw, raw.data(), raw.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
-    launch::coefsToSoa(dPatches, tabCoef.d, (long long)tabCoef.h.size(), dCoefRaw, dCoefs, stream);
-    GSGPU_CUDA_TRY(cudaStreamSynchronize(stream));
-    refreshed = true;
-    assembled = false;
-    solved = false;
 }
 
 void Context::setCoefs(const double* coefs) {
@@ -371,10 +456,10 @@ void Context::assemble(int precision) {
     if (!ddof.empty())
         GSGPU_CUDA_TRY(cudaMemcpyAsync(dDdof, ddof.data(), ddof.size() * sizeof(double), cudaMemcpyHostToDevice, s));
     if (mixed) {
-        launch::gatherCsrDF((long long)pat.col.size(), dSrc, bandDf, dOvfPtr, dOvfIdx, dValHi, dValLo, s);
+        launch::gatherCsrDF(nnz, dSrc, bandDf, dOvfPtr, dOvfIdx, dValHi, dValLo, s);
         launch::rhsRows<df32>(pat.n, dLvec, dLptr, dLidx, bandDf, dFptr, dFband, dFbidx, dDdof, dRhs, s);
     } else {
-        launch::gatherCsr<double>((long long)pat.col.size(), dSrc, dBand, dOvfPtr, dOvfIdx, dVal, s);
+        launch::gatherCsr<double>(nnz, dSrc, dBand, dOvfPtr, dOvfIdx, dVal, s);
         launch::rhsRows<double>(pat.n, dLvec, dLptr, dLidx, dBand, dFptr, dFband, dFbidx, dDdof, dRhs, s);
     }
     GSGPU_CUDA_TRY(cudaEventRecord(ev[6], s));
@@ -528,7 +613,7 @@ int Context::lanesPerRow(bool fp64) const {
         const int v = std::atoi(e);
         if (v == 4 || v == 8 || v == 16 || v == 32) return v;
     }
-    const double avg = pat.n ? double(pat.col.size()) / pat.n : 1.0;
+    const double avg = pat.n ? double(nnz) / pat.n : 1.0;
     if (avg > 48) return fp64 ? 8 : 16;
     if (avg > 20) return fp64 ? 8 : 16;
     if (avg > 10) return 8;
@@ -582,7 +667,7 @@ void Context::solve(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
     const int maxit = o.max_iters > 0 ? o.max_iters : 1000;
     launch::cgInit(B, tol, maxit, s);
     CgState hs{};
-    spmvBytes = double(pat.col.size()) * (8 + (dColOff ? 2 : 4)) + double(pat.n + 1) * 4 + 2.0 * pat.n * 8;
+    spmvBytes = double(nnz) * (8 + (dColOff ? 2 : 4)) + double(pat.n + 1) * 4 + 2.0 * pat.n * 8;
     if (profiling) {
         // one iteration at a time, every SpMV bracketed by events (no graph)
         cudaEvent_t a, b;
@@ -644,7 +729,6 @@ void Context::solve(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
 void Context::ensureMixedBuffers() {
     if (dValHi) return;
     dropGraphs();
-    const long long nnz = (long long)pat.col.size();
     const int n = pat.n;
     allocN(arena, dCoefsDf, L.coefs);
     allocN(arena, dValHi, nnz);
@@ -686,7 +770,7 @@ void Context::solveMixed(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
     const int maxit = o.max_iters > 0 ? o.max_iters : 1000;
     launch::mixedInit(B, tol, maxit, s);
     CgState hs{};
-    spmvBytes = double(pat.col.size()) * (4 + (dColOff ? 2 : 4)) + double(pat.n + 1) * 4 + 2.0 * pat.n * 4;
+    spmvBytes = double(nnz) * (4 + (dColOff ? 2 : 4)) + double(pat.n + 1) * 4 + 2.0 * pat.n * 4;
     const int chunk = 16;
     if (profiling) {
         cudaEvent_t a, b;
@@ -933,7 +1017,7 @@ int gsgpu_sizes(gsgpu_context* ctx, int* nfree, long long* nnz, int* nfixed, int
     return guarded(ctx, [&] {
         if (!ctx->c.refreshed) throw gsgpu::StateError("sizes() before refresh()");
         if (nfree) *nfree = ctx->c.pat.n;
-        if (nnz) *nnz = (long long)ctx->c.pat.col.size();
+        if (nnz) *nnz = ctx->c.nnz;
         if (nfixed) *nfixed = ctx->c.map.boundarySize;
         if (nlocal) *nlocal = ctx->c.map.nlocal;
     });
@@ -944,16 +1028,24 @@ int gsgpu_matrix_csr(gsgpu_context* ctx, int* ptr, int* col, double* val) {
         auto& c = ctx->c;
         if (!c.refreshed) throw gsgpu::StateError("matrix() before refresh()");
         if (val && !c.assembled) throw gsgpu::StateError("matrix() values before assemble()");
-        if (ptr) std::copy(c.pat.ptr.begin(), c.pat.ptr.end(), ptr);
-        if (col) std::copy(c.pat.col.begin(), c.pat.col.end(), col);
+        if (c.devPattern) {  // the pattern lives on the device only
+            if (ptr)
+                GSGPU_CUDA_TRY(cudaMemcpyAsync(ptr, c.dPtr, size_t(c.pat.n + 1) * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+            if (col && c.nnz)
+                GSGPU_CUDA_TRY(cudaMemcpyAsync(col, c.dCol, size_t(c.nnz) * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+            GSGPU_CUDA_TRY(cudaStreamSynchronize(c.stream));
+        } else {
+            if (ptr) std::copy(c.pat.ptr.begin(), c.pat.ptr.end(), ptr);
+            if (col) std::copy(c.pat.col.begin(), c.pat.col.end(), col);
+        }
         if (val && c.assembledPrecision == gsgpu::kMixed) {  // the df32 operator as FP64 values hi + lo
-            std::vector<float> hi(c.pat.col.size()), lo(c.pat.col.size());
+            std::vector<float> hi(size_t(c.nnz)), lo(size_t(c.nnz));
             GSGPU_CUDA_TRY(cudaMemcpyAsync(hi.data(), c.dValHi, hi.size() * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
             GSGPU_CUDA_TRY(cudaMemcpyAsync(lo.data(), c.dValLo, lo.size() * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
             GSGPU_CUDA_TRY(cudaStreamSynchronize(c.stream));
             for (size_t k = 0; k < hi.size(); ++k) val[k] = double(hi[k]) + double(lo[k]);
         } else if (val) {
-            GSGPU_CUDA_TRY(cudaMemcpyAsync(val, c.dVal, c.pat.col.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            GSGPU_CUDA_TRY(cudaMemcpyAsync(val, c.dVal, size_t(c.nnz) * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
             GSGPU_CUDA_TRY(cudaStreamSynchronize(c.stream));
         }
     });

@@ -128,6 +128,8 @@ struct Context {
            *dLvec = nullptr;
     int *dPtr = nullptr, *dCol = nullptr, *dDiag = nullptr;
     int16_t* dColOff = nullptr;  // column - row, when every offset fits in 16 bits
+    long long nnz = 0;           // non-zeros of the CSR system
+    bool devPattern = false;     // pattern built on the device (no interfaces): no host col/src arrays
     uint32_t *dSrc = nullptr, *dOvfPtr = nullptr, *dOvfIdx = nullptr, *dLptr = nullptr, *dLidx = nullptr,
              *dFptr = nullptr, *dFband = nullptr, *dFbidx = nullptr;
     double *dVal = nullptr, *dRhs = nullptr, *dDdof = nullptr;
@@ -191,6 +193,9 @@ struct Context {
     double spmvMs = 0.0, spmvBytes = 0.0;
 
     void refresh();
+    void refreshUploads();
+    void patternOnDevice(const RowPlan& rp);
+    void patternFromHost();
     void setCoefs(const double* coefs);
     void assemble(int precision);
     void solve(const gsgpu_solver_opts& o, gsgpu_solve_info& info);

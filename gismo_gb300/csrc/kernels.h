@@ -61,6 +61,26 @@ void l2Partials(const DevPatch* P, const BlkEnt* tab, long long nblk, const dev:
                 const double* Y1, const double* Y2, const double* gtab, const int* ibuf, const double* wq,
                 const double* btab, const double* coef, double* part, cudaStream_t s);
 
+// sparsity pattern of a problem without interfaces on the device (pattern_dev.cu) from the host's
+// row plan (plan.h RowPlan): counts and exclusive scans (nslot, nlift: n+1 entries), then the fill
+struct RowPlanDev {
+    int n = 0, nfree = 0;
+    const int* rowPatch = nullptr;
+    const int* rowLoc = nullptr;
+    const int* rng = nullptr;
+    const long long* rngOff = nullptr;
+    const int* index = nullptr;  // dof map (patch-local -> global)
+    const int* poff = nullptr;   // first patch-local dof of each patch
+};
+long long scanScratch(long long n);
+void patternCount(const DevPatch* P, const RowPlanDev& R, long long* nslot, long long* nlift, long long* sums,
+                  cudaStream_t s);
+// flags[0]: a row without its diagonal or with unordered columns; flags[1]: largest |column - row|
+void patternFill(const DevPatch* P, const RowPlanDev& R, const long long* nslot, const long long* nlift, int* ptr,
+                 int* col, uint32_t* src, uint32_t* fptr, uint32_t* fband, uint32_t* fbidx, int* diag, uint32_t* lptr,
+                 uint32_t* lidx, int* flags, cudaStream_t s);
+void patternColOffsets(int n, const int* ptr, const int* col, int16_t* coff, cudaStream_t s);
+
 // order-preserving uint64 key of a double (for atomicMin over signed values)
 inline unsigned long long detKeyInit() { return ~0ULL; }
 double detKeyDecode(unsigned long long key);

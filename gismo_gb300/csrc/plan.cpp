@@ -410,39 +410,39 @@ void rowEntries(const ProblemDesc& pd, const DofMap& map, const Layout& L, const
 }
 }  // namespace
 
-// Problems without interfaces (single patches, batches of independent patches): every free row has
-// one pre-image, and a patch's free dofs are numbered in its local lexicographic order, so a row's
-// columns come out ascending from its neighbour box with no sorting and no multi-source slots. The
-// neighbour set per direction is the support-sharing range the generic path tests pair by pair, and
-// the loop order (and so the lift order) is the same. Returns false (generic path) if an assumption
-// does not hold.
-static bool buildPatternSingle(const ProblemDesc& pd, const DofMap& map, const Layout& L, Pattern& pat) {
+// rows of a problem without interfaces: pre-image of each free row and support-sharing neighbour
+// ranges per patch and direction (false if a free dof has two pre-images or a range is not
+// contiguous)
+bool rowPlanSingle(const ProblemDesc& pd, const DofMap& map, const Layout& L, RowPlan& rp) {
+    if (!pd.ifaces.empty()) return false;
     const int n = map.freeSize;
     const int d = pd.dim;
     const size_t np = pd.patches.size();
-    std::vector<int> rowPatch(n, -1), rowLoc(n, -1);
+    rp = RowPlan();
+    rp.rowPatch.assign(n, -1);
+    rp.rowLoc.assign(n, -1);
     for (size_t pi = 0; pi < np; ++pi) {
         const HostPatch& P = pd.patches[pi];
         for (int i = 0; i < P.ndofs; ++i) {
             const int J = map.index[P.offset + i];
             if (J >= n) continue;
-            if (rowPatch[J] >= 0) return false;
-            rowPatch[J] = int(pi);
-            rowLoc[J] = i;
+            if (rp.rowPatch[J] >= 0) return false;
+            rp.rowPatch[J] = int(pi);
+            rp.rowLoc[J] = i;
         }
     }
     // support-sharing neighbour range [jlo, jhi] of every function, per patch and direction
-    std::vector<std::vector<int>> jlo(np * 3), jhi(np * 3);
+    rp.rngOff.assign(np * 3, 0);
     for (size_t pi = 0; pi < np; ++pi) {
         const HostPatch& P = pd.patches[pi];
         const DevPatch& D = L.dev[pi];
-        for (int a = 0; a < d; ++a) {
+        for (int a = 0; a < 3; ++a) {
+            rp.rngOff[pi * 3 + a] = (long long)rp.rng.size();
+            if (a >= d) continue;
             const int* elo = L.ibuf.data() + D.doff[a];
             const int* ehi = elo + D.n[a];
-            std::vector<int>& lo = jlo[pi * 3 + a];
-            std::vector<int>& hi = jhi[pi * 3 + a];
-            lo.assign(P.nd[a], 0);
-            hi.assign(P.nd[a], -1);
+            const size_t base = rp.rng.size();
+            rp.rng.resize(base + 2 * size_t(P.nd[a]));
             for (int i = 0; i < P.nd[a]; ++i) {
                 int first = -1, last = -2;
                 for (int j = std::max(0, i - D.p[a]); j <= std::min(P.nd[a] - 1, i + D.p[a]); ++j) {
@@ -452,11 +452,27 @@ static bool buildPatternSingle(const ProblemDesc& pd, const DofMap& map, const L
                     else if (j != last + 1) return false;  // not a contiguous range
                     last = j;
                 }
-                lo[i] = first;
-                hi[i] = last;
+                rp.rng[base + i] = first;
+                rp.rng[base + P.nd[a] + i] = last;
             }
         }
     }
+    return true;
+}
+
+// Problems without interfaces (single patches, batches of independent patches): every free row has
+// one pre-image, and a patch's free dofs are numbered in its local lexicographic order, so a row's
+// columns come out ascending from its neighbour box with no sorting and no multi-source slots. The
+// neighbour set per direction is the support-sharing range the generic path tests pair by pair, and
+// the loop order (and so the lift order) is the same. Returns false (generic path) if an assumption
+// does not hold.
+static bool buildPatternSingle(const ProblemDesc& pd, const DofMap& map, const Layout& L, Pattern& pat) {
+    const int n = map.freeSize;
+    const int d = pd.dim;
+    RowPlan rp;
+    if (!rowPlanSingle(pd, map, L, rp)) return false;
+    const std::vector<int>& rowPatch = rp.rowPatch;
+    const std::vector<int>& rowLoc = rp.rowLoc;
     auto box = [&](int I, int c[3], int lo[3], int hi[3]) {
         const int pi = rowPatch[I];
         const HostPatch& P = pd.patches[pi];
@@ -465,8 +481,8 @@ static bool buildPatternSingle(const ProblemDesc& pd, const DofMap& map, const L
             if (a < d) {
                 c[a] = r % P.nd[a];
                 r /= P.nd[a];
-                lo[a] = jlo[size_t(pi) * 3 + a][c[a]];
-                hi[a] = jhi[size_t(pi) * 3 + a][c[a]];
+                lo[a] = rp.rng[rp.rngOff[size_t(pi) * 3 + a] + c[a]];
+                hi[a] = rp.rng[rp.rngOff[size_t(pi) * 3 + a] + P.nd[a] + c[a]];
             } else {
                 c[a] = lo[a] = hi[a] = 0;
             }

@@ -142,4 +142,14 @@ void gaussLegendre(int n, std::vector<double>& x, std::vector<double>& w);
 // block -> (patch, base) tables for batched kernels
 void blockTable(const std::vector<long long>& work, int block, std::vector<BlkEnt>& tab);
 
+// Rows of a problem without interfaces: the patch and patch-local index of each free row, and per
+// patch and direction the support-sharing neighbour range [jlo(i), jhi(i)] of every function
+// (jlo at rng[rngOff[3 patch + a] + i], jhi n_a entries later)
+struct RowPlan {
+    std::vector<int> rowPatch, rowLoc;
+    std::vector<int> rng;
+    std::vector<long long> rngOff;
+};
+bool rowPlanSingle(const ProblemDesc& pd, const DofMap& map, const Layout& L, RowPlan& rp);
+
 }  // namespace gsgpu

@@ -164,3 +164,28 @@ def test_l2_error_on_device(precision):
         l2 = o.l2_error(x)
         assert abs(A.l2_error() - l2) <= 1e-9 * l2, (A.l2_error(), l2)
         A.close()
+
+
+def test_device_pattern_equals_host_pattern(monkeypatch):
+    """Problems without interfaces build their pattern on the device: the CSR arrays, rhs and CG
+    solution are bitwise those of the host builder (GSGPU_HOST_PATTERN forces the host path)."""
+    from gismo_gb300.assembler import GpuPoissonAssembler, GpuPoissonBatch
+    cases = [lambda: GpuPoissonAssembler(P.displaced_single_patch(3, (5, 6, 7), (2, 3, 2), 8, 0.04), device=0),
+             lambda: GpuPoissonBatch(P.patch_batch(count=9, seed=4, nmin=4, nmax=20), device=0)]
+    for make in cases:
+        out = []
+        for host in (False, True):
+            if host:
+                monkeypatch.setenv("GSGPU_HOST_PATTERN", "1")
+            else:
+                monkeypatch.delenv("GSGPU_HOST_PATTERN", raising=False)
+            A = make()
+            A.assemble("fp64")
+            x, _ = A.solve(tol=1e-10)
+            x = np.concatenate(x) if isinstance(x, list) else x
+            out.append((A.csr(), A.rhs(), x))
+            A.close()
+        (pa, ca, va), ra, xa = out[0]
+        (pb, cb, vb), rb, xb = out[1]
+        assert np.array_equal(pa, pb) and np.array_equal(ca, cb) and np.array_equal(va, vb)
+        assert np.array_equal(ra, rb) and np.array_equal(xa, xb)
