@@ -42,7 +42,7 @@ class SolverOpts(C.Structure):
     _fields_ = [
         ("method", C.c_int), ("precision", C.c_int), ("tol", C.c_double), ("max_iters", C.c_int),
         ("mg_levels", C.c_int), ("mg_npre", C.c_int), ("mg_npost", C.c_int), ("mg_damping", C.c_double),
-        ("inner_tol", C.c_double),
+        ("inner_tol", C.c_double), ("mg_cycles", C.c_int), ("mg_cgc_damping", C.c_double),
     ]
 
 

@@ -154,11 +154,13 @@ class GpuPoissonAssembler:
         return y
 
     def mg_apply(self, r: np.ndarray, mg_levels: int = 4, mg_npre: int = 2, mg_npost: int = 2,
-                 mg_damping: float = 0.6) -> np.ndarray:
-        """gsMultiGridOp as a preconditioner: one FP64 V-cycle on r from a zero start."""
+                 mg_damping: float = 0.6, mg_cycles: int = 1, mg_cgc_damping: float = 1.0) -> np.ndarray:
+        """gsMultiGridOp as a preconditioner: one FP64 cycle (V for mg_cycles=1, W for 2) on r
+        from a zero start."""
         o = SolverOpts()
         o.method, o.precision = _lib.SOLVER_CG_MG, _lib.PREC_FP64
         o.mg_levels, o.mg_npre, o.mg_npost, o.mg_damping = mg_levels, mg_npre, mg_npost, mg_damping
+        o.mg_cycles, o.mg_cgc_damping = mg_cycles, mg_cgc_damping
         r = np.ascontiguousarray(r, np.float64)
         z = np.empty_like(r)
         self._check(self.L.gsgpu_mg_apply(self.h, C.byref(o), r.ctypes.data, z.ctypes.data))
@@ -196,12 +198,13 @@ class GpuPoissonAssembler:
     # ---- gsConjugateGradient ----
     def solve(self, tol: float = 1e-10, max_iters: int = 1000, method: str = "jacobi", precision: str = "fp64",
               mg_levels: int = 4, mg_npre: int = 2, mg_npost: int = 2, mg_damping: float = 0.6,
-              inner_tol: float = 1e-4, download: bool = True):
+              inner_tol: float = 1e-4, download: bool = True, mg_cycles: int = 1, mg_cgc_damping: float = 1.0):
         o = SolverOpts()
         o.method = _lib.SOLVER_CG_JACOBI if method == "jacobi" else _lib.SOLVER_CG_MG
         o.precision = _lib.PREC_FP64 if precision == "fp64" else _lib.PREC_MIXED
         o.tol, o.max_iters = tol, max_iters
         o.mg_levels, o.mg_npre, o.mg_npost, o.mg_damping = mg_levels, mg_npre, mg_npost, mg_damping
+        o.mg_cycles, o.mg_cgc_damping = mg_cycles, mg_cgc_damping
         o.inner_tol = inner_tol
         info = SolveInfo()
         x = np.empty(self.sizes()[0], np.float64) if download else None

@@ -80,11 +80,12 @@ struct MgLevelBuf {
 
 // what a captured multigrid solver graph depends on
 struct MgGraphKey {
-    int mixed = -1, levels = 0, npre = 0, npost = 0, coarse_iters = 0;
-    double damping = 0.0, coarse_tol = 0.0;
+    int mixed = -1, levels = 0, npre = 0, npost = 0, coarse_iters = 0, cycles = 0;
+    double damping = 0.0, coarse_tol = 0.0, cgc = 0.0;
     bool operator==(const MgGraphKey& o) const {
         return mixed == o.mixed && levels == o.levels && npre == o.npre && npost == o.npost &&
-               coarse_iters == o.coarse_iters && damping == o.damping && coarse_tol == o.coarse_tol;
+               coarse_iters == o.coarse_iters && cycles == o.cycles && damping == o.damping &&
+               coarse_tol == o.coarse_tol && cgc == o.cgc;
     }
 };
 

@@ -141,6 +141,21 @@ struct Dot2 {
         twoSum(s, p, s, t);
         c = fadd(c, fadd(t, e));
     }
+    // += a * b for an FP32 factor b
+    DF_HD void mac(df32 a, float b) {
+        float p, e;
+        twoProd(a.hi, b, p, e);
+        e = ffma(a.lo, b, e);
+        float t;
+        twoSum(s, p, s, t);
+        c = fadd(c, fadd(t, e));
+    }
+    // += a
+    DF_HD void add(df32 a) {
+        float t;
+        twoSum(s, a.hi, s, t);
+        c = fadd(c, fadd(t, a.lo));
+    }
     DF_HD void add(const Dot2& o) {
         float t;
         twoSum(s, o.s, s, t);
@@ -152,6 +167,25 @@ struct Dot2 {
         return df32(h, l);
     }
 };
+
+// a*b + sgn*c*d with one rounding step: both products exact by TwoProduct, their cross terms and
+// the error of the FP32 sum collected in one FP32 correction (the two-term case of Dot2); error
+// about 2^-47 (|ab| + |cd|)
+DF_HD df32 dot2Terms(df32 a, df32 b, df32 c, df32 d, float sgn) {
+    float p1, e1, p2, e2;
+    twoProd(a.hi, b.hi, p1, e1);
+    e1 = ffma(a.hi, b.lo, e1);
+    e1 = ffma(a.lo, b.hi, e1);
+    const float ch = fmul(sgn, c.hi), cl = fmul(sgn, c.lo);
+    twoProd(ch, d.hi, p2, e2);
+    e2 = ffma(ch, d.lo, e2);
+    e2 = ffma(cl, d.hi, e2);
+    float sh, t;
+    twoSum(p1, p2, sh, t);
+    const float lo = fadd(fadd(e1, e2), t);
+    fastTwoSum(sh, lo, sh, t);
+    return df32(sh, t);
+}
 
 // -------------------------------------------------------------------------------------------
 // constants as df32 (hi + lo of the double value)
@@ -188,12 +222,13 @@ DF_HD void sincospiDf(df32 x, df32& s, df32& c) {
                             2.8114572543455206e-15,
                             1.5619206968586225e-16,
                             8.2206352466243295e-18};
-    // sin(a) = a sum_{j=0..9} (-1)^j a^(2j) / (2j+1)!,  cos(a) = sum_{j=0..9} (-1)^j a^(2j) / (2j)!
-    // (|a| <= pi/4: the first omitted terms are below 1e-19 relative)
-    df32 sp(-inv[19]);
-    for (int j = 8; j >= 0; --j) sp = df32((j % 2 ? -1.0 : 1.0) * inv[2 * j + 1]) + a2 * sp;
-    df32 cp(-inv[18]);
-    for (int j = 8; j >= 0; --j) cp = df32((j % 2 ? -1.0 : 1.0) * inv[2 * j]) + a2 * cp;
+    // sin(a) = a sum_{j=0..7} (-1)^j a^(2j) / (2j+1)!,  cos(a) = sum_{j=0..8} (-1)^j a^(2j) / (2j)!
+    // |a| <= pi/4, so the first omitted terms are below (pi/4)^16/17!/0.90 < 7e-17 of sin(a) and
+    // (pi/4)^18/18! < 3e-18 of cos(a) >= 0.707, both under the df32 unit 2^-48 = 3.6e-15
+    df32 sp(-inv[15]);
+    for (int j = 6; j >= 0; --j) sp = df32((j % 2 ? -1.0 : 1.0) * inv[2 * j + 1]) + a2 * sp;
+    df32 cp(inv[16]);
+    for (int j = 7; j >= 0; --j) cp = df32((j % 2 ? -1.0 : 1.0) * inv[2 * j]) + a2 * cp;
     const df32 sa = a * sp, ca = cp;
     const int q = ((int)n) & 3;
     if (q == 0) { s = sa; c = ca; }
@@ -207,11 +242,12 @@ DF_HD df32 expDf(df32 y) {
     const float k = rintf(y.hi * 1.44269504088896341f);
     df32 r = y - dfLn2() * k;
     r = df32(fmul(r.hi, 0.0625f), fmul(r.lo, 0.0625f));
-    const double inv[10] = {1.0, 1.0, 0.5, 1.6666666666666666e-01, 4.1666666666666664e-02, 8.3333333333333332e-03,
-                            1.3888888888888889e-03, 1.9841269841269841e-04, 2.4801587301587302e-05,
-                            2.7557319223985893e-06};
-    df32 e(inv[9]);
-    for (int j = 8; j >= 0; --j) e = df32(inv[j]) + r * e;
+    // degree 7: |r/16| <= ln2/32, so the first omitted term (ln2/32)^8/8! < 1.3e-18, and below
+    // 2.1e-17 after the 4 squarings
+    const double inv[8] = {1.0, 1.0, 0.5, 1.6666666666666666e-01, 4.1666666666666664e-02, 8.3333333333333332e-03,
+                           1.3888888888888889e-03, 1.9841269841269841e-04};
+    df32 e(inv[7]);
+    for (int j = 6; j >= 0; --j) e = df32(inv[j]) + r * e;
     for (int j = 0; j < 4; ++j) e = e * e;
     return ldexpDf(e, int(k));
 }

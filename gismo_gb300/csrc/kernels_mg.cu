@@ -12,6 +12,7 @@
 // with no sequential triangular solves. The outer CG uses the Polak-Ribiere beta
 // (r_k - r_{k-1}).z_k / r_{k-1}.z_{k-1}, which stays a CG for a fixed preconditioner and is robust
 // when the coarse solve leaves a small inexactness.
+#include <algorithm>
 #include <cstdint>
 
 #include "kernels_mg.h"
@@ -112,10 +113,11 @@ __global__ void __launch_bounds__(kB) k_resid_mg(int n, const int* __restrict__ 
 template <typename T, int LPR>
 __global__ void __launch_bounds__(kB) k_transfer(int n, const int* __restrict__ ptr, const int* __restrict__ col,
                                                  const T* __restrict__ val, const T* __restrict__ x,
-                                                 T* __restrict__ y, int sub, const CgState* __restrict__ outer) {
+                                                 T* __restrict__ y, int sub, T scale,
+                                                 const CgState* __restrict__ outer) {
     if (stopped(outer, nullptr)) return;
     rowLoop<T, LPR, false>(n, ptr, col, nullptr, [&](int k) { return val[k]; }, x, [&](int row, T ax) {
-        if (sub) y[row] -= ax;
+        if (sub) y[row] -= scale * ax;
         else y[row] = ax;
     });
 }
@@ -428,8 +430,12 @@ void coarseIters(const MgLevelDev<T>& L, int k, const CgState* outer, cudaStream
     }
 }
 
+// gsMultiGridOp::multiGridStep (gsMultiGrid.hpp:147-201) with r = A x - b and x -= cgc P e; the
+// coarse correction e starts at zero and runs prm.cycles cycles, one on the coarsest level, whose
+// Jacobi-PCG solve overwrites its x as the reference's direct coarse solver does
 template <typename T>
-void vcycle(const std::vector<MgLevelDev<T>>& lv, int l, const MgParams& prm, const CgState* outer, cudaStream_t s) {
+void vcycle(const std::vector<MgLevelDev<T>>& lv, int l, const MgParams& prm, const CgState* outer, cudaStream_t s,
+            bool zero) {
     const MgLevelDev<T>& L = lv[l];
     const int nrb = rowBlocks(L.n, L.lpr);
     const int nb = blocksFor(L.n);
@@ -444,16 +450,17 @@ void vcycle(const std::vector<MgLevelDev<T>>& lv, int l, const MgParams& prm, co
     T* nxt = L.z;
     for (int k = 0; k < prm.npre; ++k) {
         MG_ROW_DISPATCH(k_jacobi, T, L, nrb, L.n, L.ptr, L.col, L.coff, L.val, L.dinv, w, L.b, cur, nxt,
-                        k == 0 ? 1 : 0, outer);
+                        k == 0 && zero ? 1 : 0, outer);
         T* tmp = cur; cur = nxt; nxt = tmp;
     }
-    if (prm.npre == 0)  // x = 0
+    if (prm.npre == 0 && zero)  // x = 0
         k_jacobi<T, 4, false><<<nb, kB, 0, s>>>(L.n, L.ptr, L.col, L.coff, L.val, L.dinv, T(0), L.b, cur, cur, 1, outer);
     MG_ROW_DISPATCH(k_resid_mg, T, L, nrb, L.n, L.ptr, L.col, L.coff, L.val, cur, L.b, L.r, outer);
     const MgLevelDev<T>& C = lv[l + 1];
-    k_transfer<T, 16><<<rowBlocks(C.n, 16), kB, 0, s>>>(C.n, C.Rptr, C.Rcol, C.Rval, L.r, C.b, 0, outer);
-    vcycle<T>(lv, l + 1, prm, outer, s);
-    k_transfer<T, 8><<<rowBlocks(L.n, 8), kB, 0, s>>>(L.n, C.Pptr, C.Pcol, C.Pval, C.x, cur, 1, outer);
+    k_transfer<T, 16><<<rowBlocks(C.n, 16), kB, 0, s>>>(C.n, C.Rptr, C.Rcol, C.Rval, L.r, C.b, 0, T(1), outer);
+    const int nc = l + 2 == (int)lv.size() ? 1 : std::max(1, prm.cycles);
+    for (int c = 0; c < nc; ++c) vcycle<T>(lv, l + 1, prm, outer, s, c == 0);
+    k_transfer<T, 8><<<rowBlocks(L.n, 8), kB, 0, s>>>(L.n, C.Pptr, C.Pcol, C.Pval, C.x, cur, 1, T(prm.cgc), outer);
     for (int k = 0; k < prm.npost; ++k) {
         MG_ROW_DISPATCH(k_jacobi, T, L, nrb, L.n, L.ptr, L.col, L.coff, L.val, L.dinv, w, L.b, cur, nxt, 0, outer);
         T* tmp = cur; cur = nxt; nxt = tmp;
@@ -517,8 +524,10 @@ template void coarseStart<double>(const MgLevelDev<double>&, double, const CgSta
 template void coarseStart<float>(const MgLevelDev<float>&, double, const CgState*, cudaStream_t);
 template void coarseIters<double>(const MgLevelDev<double>&, int, const CgState*, cudaStream_t);
 template void coarseIters<float>(const MgLevelDev<float>&, int, const CgState*, cudaStream_t);
-template void vcycle<double>(const std::vector<MgLevelDev<double>>&, int, const MgParams&, const CgState*, cudaStream_t);
-template void vcycle<float>(const std::vector<MgLevelDev<float>>&, int, const MgParams&, const CgState*, cudaStream_t);
+template void vcycle<double>(const std::vector<MgLevelDev<double>>&, int, const MgParams&, const CgState*, cudaStream_t,
+                             bool);
+template void vcycle<float>(const std::vector<MgLevelDev<float>>&, int, const MgParams&, const CgState*, cudaStream_t,
+                            bool);
 template void mgPcgPrecond<double>(const MgOuter&, const std::vector<MgLevelDev<double>>&, const MgParams&, cudaStream_t);
 template void mgPcgPrecond<float>(const MgOuter&, const std::vector<MgLevelDev<float>>&, const MgParams&, cudaStream_t);
 

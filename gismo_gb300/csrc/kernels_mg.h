@@ -32,7 +32,9 @@ struct MgLevelDev {
 
 struct MgParams {
     int npre = 2, npost = 2;
-    double damping = 0.6;
+    double damping = 0.6;  // damped Jacobi smoother
+    int cycles = 1;        // coarse-correction cycles on every level but the coarsest (1 = V, 2 = W)
+    double cgc = 1.0;      // damping of the coarse-grid correction
     int coarse_iters = 100;  // cap of the coarsest-level Jacobi-PCG
     double coarse_tol = 1e-10;
 };
@@ -65,9 +67,11 @@ template <typename T>
 void coarseStart(const MgLevelDev<T>& L, double tol, const CgState* outer, cudaStream_t s);
 template <typename T>
 void coarseIters(const MgLevelDev<T>& L, int k, const CgState* outer, cudaStream_t s);
-// levels[l].x = V-cycle(levels[l].b) from a zero start; kernels skip once outer->done is set
+// one cycle on levels[l].b: from a zero start (zero) or from levels[l].x, result in levels[l].x;
+// kernels skip once outer->done is set
 template <typename T>
-void vcycle(const std::vector<MgLevelDev<T>>& levels, int l, const MgParams& prm, const CgState* outer, cudaStream_t s);
+void vcycle(const std::vector<MgLevelDev<T>>& levels, int l, const MgParams& prm, const CgState* outer, cudaStream_t s,
+            bool zero = true);
 void mgPcgStart(const MgOuter& O, double tol, int maxit, cudaStream_t s);
 // preconditioned direction: z is the V-cycle result of level 0 (precision T)
 template <typename T>

@@ -274,6 +274,12 @@ void Context::mgPrepare(const gsgpu_solver_opts& o, bool mixed, std::vector<MgLe
     prm.npre = o.mg_npre >= 0 ? o.mg_npre : 2;
     prm.npost = o.mg_npost >= 0 ? o.mg_npost : 2;
     prm.damping = o.mg_damping > 0 ? o.mg_damping : 0.6;
+    prm.cycles = o.mg_cycles > 0 ? o.mg_cycles : 1;
+    prm.cgc = o.mg_cgc_damping > 0 ? o.mg_cgc_damping : 1.0;
+    // launches per cycle grow as cycles^(levels - 2); keep the captured graph bounded
+    double visits = 1, total = 1;
+    for (size_t l = 1; l + 1 < lv.size(); ++l) total += (visits *= prm.cycles);
+    if (total > 4096) throw std::invalid_argument("NumCycles: too many coarse-level visits per cycle");
     prm.coarse_tol = envOr("GSGPU_MG_COARSE_TOL", mixed ? 1e-5 : 1e-10);
     if (mgCoarseIters == 0 || mgCoarseTol != prm.coarse_tol) {
         // size the coarse iteration cap: iterations of the coarsest Jacobi-PCG on a seeded random
@@ -349,6 +355,8 @@ void Context::mgRun(const gsgpu_solver_opts& o, gsgpu_solve_info& info, bool mix
     key.npost = prm.npost;
     key.coarse_iters = prm.coarse_iters;
     key.damping = prm.damping;
+    key.cycles = prm.cycles;
+    key.cgc = prm.cgc;
     key.coarse_tol = prm.coarse_tol;
     if (!gexecMg || !(gexecMgKey == key)) {
         if (gexecMg) cudaGraphExecDestroy(gexecMg);

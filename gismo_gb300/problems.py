@@ -141,6 +141,8 @@ class Problem:
     mg_npre: int = 2
     mg_npost: int = 2
     mg_damping: float = 0.6
+    mg_cycles: int = 1            # gsMultiGridOp "NumCycles" (1 = V-cycle, 2 = W-cycle)
+    mg_cgc_damping: float = 1.0   # gsMultiGridOp "CoarseGridCorrectionDamping"
     name: str = ""
 
     # ---- closed forms (numpy, used by the generator's checks and by the host tests) ----
@@ -452,6 +454,8 @@ def write_spec(prob: Problem, path: str) -> None:
     lines.append(f"quad {fmt(prob.quA)} {prob.quB}")
     lines.append(f"solver {prob.solver} {fmt(prob.tol)} {prob.maxit}")
     lines.append(f"mg {prob.mg_levels} {prob.mg_npre} {prob.mg_npost} {fmt(prob.mg_damping)}")
+    if prob.mg_cycles != 1 or prob.mg_cgc_damping != 1.0:
+        lines.append(f"mgcycle {prob.mg_cycles} {fmt(prob.mg_cgc_damping)}")
     lines.append("end")
     with open(path, "w") as fh:
         fh.write("\n".join(lines) + "\n")

@@ -90,15 +90,15 @@ public:
 
     /// CG (+ Jacobi) on the device-resident system (gsConjugateGradient(matrix(), gsJacobiOp))
     int solve(gsMatrix<T>& x, double tol = 1e-10, int maxIter = 1000) {
-        gsgpu_solver_opts o = {GSGPU_SOLVER_CG_JACOBI, GSGPU_PREC_FP64, tol, maxIter, 4, 2, 2, 0.6, 1e-4};
+        gsgpu_solver_opts o = {GSGPU_SOLVER_CG_JACOBI, GSGPU_PREC_FP64, tol, maxIter, 4, 2, 2, 0.6, 1e-4, 1, 1.0};
         return run(o, x);
     }
 
     /// gsConjugateGradient(matrix(), gsJacobiOp | gsMultiGridOp).setOptions(opt).solve(rhs(), x) on
     /// the device, with G+Smo's option names: "Tolerance", "MaxIterations" (gsIterativeSolver.h:92-99),
     /// "Preconditioner" ("Jacobi" or "MultiGrid"), the multigrid's "Levels" (gsGridHierarchy),
-    /// "NumPreSmooth", "NumPostSmooth" (gsMultiGrid.hpp:299-328) and the smoother's "Damping"
-    /// (gsJacobiOp), plus "Precision" ("fp64" or "mixed": re-assembles the double-float operator on
+    /// "NumPreSmooth", "NumPostSmooth", "NumCycles", "CoarseGridCorrectionDamping"
+    /// (gsMultiGrid.hpp:299-328) and the smoother's "Damping" (gsJacobiOp), plus "Precision" ("fp64" or "mixed": re-assembles the double-float operator on
     /// the device; matrix() keeps the FP64 system). Returns the iteration count; error() gives the
     /// final relative residual as gsIterativeSolver::error() does.
     int solve(const gsOptionList& opt, gsMatrix<T>& x) {
@@ -111,6 +111,8 @@ public:
         o.mg_npre = opt.askInt("NumPreSmooth", 2);
         o.mg_npost = opt.askInt("NumPostSmooth", 2);
         o.mg_damping = opt.askReal("Damping", 0.6);
+        o.mg_cycles = opt.askInt("NumCycles", 1);
+        o.mg_cgc_damping = opt.askReal("CoarseGridCorrectionDamping", 1.0);
         o.inner_tol = 1e-4;
         if (o.precision == GSGPU_PREC_MIXED) check(gsgpu_assemble(m_ctx, GSGPU_PREC_MIXED));
         const int its = run(o, x);
@@ -244,20 +246,23 @@ private:
     index_t m_n;
 };
 
-/// gsMultiGridOp as a preconditioner on the device (gsPreconditionerOp::apply: one V-cycle from a
+/// gsMultiGridOp as a preconditioner on the device (gsPreconditionerOp::apply: one cycle from a
 /// zero start, gsMultiGrid.hpp:147-201); setOptions takes "Levels", "NumPreSmooth",
-/// "NumPostSmooth" and "Damping"
+/// "NumPostSmooth", "NumCycles", "CoarseGridCorrectionDamping" and "Damping". "SymmSmooth" needs
+/// no setting: the damped Jacobi step is its own transpose, so step and stepT coincide
 template <class T = real_t>
 class gsGpuMultiGridOp : public gsLinearOperator<T> {
 public:
     explicit gsGpuMultiGridOp(const gsGpuPoissonAssembler<T>& A) : m_ctx(A.context()), m_n(A.numDofs()) {
-        m_opts = {GSGPU_SOLVER_CG_MG, GSGPU_PREC_FP64, 0.0, 0, 4, 2, 2, 0.6, 0.0};
+        m_opts = {GSGPU_SOLVER_CG_MG, GSGPU_PREC_FP64, 0.0, 0, 4, 2, 2, 0.6, 0.0, 1, 1.0};
     }
     void setOptions(const gsOptionList& opt) override {
         m_opts.mg_levels = opt.askInt("Levels", m_opts.mg_levels);
         m_opts.mg_npre = opt.askInt("NumPreSmooth", m_opts.mg_npre);
         m_opts.mg_npost = opt.askInt("NumPostSmooth", m_opts.mg_npost);
         m_opts.mg_damping = opt.askReal("Damping", m_opts.mg_damping);
+        m_opts.mg_cycles = opt.askInt("NumCycles", m_opts.mg_cycles);
+        m_opts.mg_cgc_damping = opt.askReal("CoarseGridCorrectionDamping", m_opts.mg_cgc_damping);
     }
     void apply(const gsMatrix<T>& input, gsMatrix<T>& x) const override {
         x.resize(m_n, input.cols());

@@ -81,6 +81,8 @@ typedef struct {
     int mg_npre, mg_npost; /* "NumPreSmooth", "NumPostSmooth" */
     double mg_damping;     /* damping of the Jacobi smoother */
     double inner_tol;      /* mixed precision: FP32 inner reduction per refinement step */
+    int mg_cycles;         /* "NumCycles": 1 = V-cycle, 2 = W-cycle (0: 1) */
+    double mg_cgc_damping; /* "CoarseGridCorrectionDamping" (0: 1) */
 } gsgpu_solver_opts;
 
 typedef struct {
@@ -133,8 +135,9 @@ int gsgpu_solve(gsgpu_context* ctx, const gsgpu_solver_opts* opts, double* x, gs
  * (host arrays of nfree values), so that G+Smo's own solvers can run on the GPU operator */
 int gsgpu_apply(gsgpu_context* ctx, const double* x, double* y);
 /* gsMultiGridOp as a preconditioner (gsPreconditionerOp::apply, gsPreconditioner.h:79-84, and
- * multiGridStep, gsMultiGrid.hpp:147-201): z = one FP64 V-cycle on r from a zero start, with the
- * hierarchy and smoother options of opts (mg_levels, mg_npre, mg_npost, mg_damping) */
+ * multiGridStep, gsMultiGrid.hpp:147-201): z = one FP64 cycle on r from a zero start, with the
+ * hierarchy, smoother and cycle options of opts (mg_levels, mg_npre, mg_npost, mg_damping,
+ * mg_cycles, mg_cgc_damping) */
 int gsgpu_mg_apply(gsgpu_context* ctx, const gsgpu_solver_opts* opts, const double* r, double* z);
 /* gsField::distanceL2 of the last solution against u (gsField.hpp:23-41) */
 int gsgpu_l2_error(gsgpu_context* ctx, double* err);

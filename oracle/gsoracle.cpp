@@ -835,8 +835,8 @@ struct Oracle {
         return std::sqrt(acc);
     }
 
-    double solveMG(double tol, int maxit, int levels, int npre, int npost, double damping, double* x, int& iters,
-                   double& relres);
+    double solveMG(double tol, int maxit, int levels, int npre, int npost, double damping, int cycles, double cgc,
+                   double* x, int& iters, double& relres);
 };
 
 }  // namespace
@@ -920,8 +920,8 @@ struct Level {
 
 }  // namespace
 
-double Oracle::solveMG(double tol, int maxit, int levels, int npre, int npost, double damping, double* x,
-                       int& iters, double& relres) {
+double Oracle::solveMG(double tol, int maxit, int levels, int npre, int npost, double damping, int cycles,
+                       double cgc, double* x, int& iters, double& relres) {
     auto t0 = std::chrono::steady_clock::now();
     // build the level structures (finest = this)
     std::vector<Oracle*> lv;
@@ -1082,7 +1082,10 @@ double Oracle::solveMG(double tol, int maxit, int levels, int npre, int npost, d
             for (int k = As[l].ptr[r]; k < As[l].ptr[r + 1]; ++k)
                 if (As[l].idx[k] == r) Dinv[l][r] = 1.0 / As[l].val[k];
     }
-    // V-cycle (gsMultiGridOp::multiGridStep, gsMultiGrid.hpp:147-201): x -> x + MG(b - A x)
+    // one cycle (gsMultiGridOp::multiGridStep, gsMultiGrid.hpp:147-201) from the x passed in: the
+    // coarse correction starts at zero and is cycled `cycles` times on every level but the
+    // coarsest (NumCycles, 1 = V-cycle, 2 = W-cycle; gsMultiGrid.h:328-333), then enters x scaled
+    // by the coarse-grid correction damping
     std::function<void(int, const double*, double*)> vcycle = [&](int l, const double* b, double* xl) {
         const Csr& M = As[l];
         const int n = M.n;
@@ -1111,11 +1114,12 @@ double Oracle::solveMG(double tol, int maxit, int levels, int npre, int npost, d
         std::vector<double> rc(R.cols, 0.0), ec(R.cols, 0.0);
         for (int i = 0; i < R.rows; ++i)
             for (int m = R.ptr[i]; m < R.ptr[i + 1]; ++m) rc[R.idx[m]] += R.val[m] * r[i];
-        vcycle(l + 1, rc.data(), ec.data());
+        const int nc = l + 2 == L ? 1 : cycles;
+        for (int c = 0; c < nc; ++c) vcycle(l + 1, rc.data(), ec.data());
         for (int i = 0; i < R.rows; ++i) {
             double s = 0;
             for (int m = R.ptr[i]; m < R.ptr[i + 1]; ++m) s += R.val[m] * ec[R.idx[m]];
-            xl[i] -= s;
+            xl[i] -= cgc * s;
         }
         for (int s = 0; s < npost; ++s) smooth();
     };
@@ -1174,9 +1178,10 @@ void orc_ddof(void* h, double* out) {
 double orc_solve_cg(void* h, double tol, int maxit, double* x, int* iters, double* relres) {
     return static_cast<Oracle*>(h)->solveCG(tol, maxit, x, *iters, *relres);
 }
-double orc_solve_mg(void* h, double tol, int maxit, int levels, int npre, int npost, double damping, double* x,
-                    int* iters, double* relres) {
-    return static_cast<Oracle*>(h)->solveMG(tol, maxit, levels, npre, npost, damping, x, *iters, *relres);
+double orc_solve_mg(void* h, double tol, int maxit, int levels, int npre, int npost, double damping, int cycles,
+                    double cgc, double* x, int* iters, double* relres) {
+    return static_cast<Oracle*>(h)->solveMG(tol, maxit, levels, npre, npost, damping, cycles, cgc, x, *iters,
+                                            *relres);
 }
 double orc_l2_error(void* h, const double* x) { return static_cast<Oracle*>(h)->l2error(x); }
 void orc_gauss(int n, double* nodes, double* weights) {

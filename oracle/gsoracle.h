@@ -53,9 +53,10 @@ void orc_rhs(void* h, double* out);
 void orc_ddof(void* h, double* out);
 /* gsConjugateGradient + gsJacobiOp (damping 1): returns elapsed seconds */
 double orc_solve_cg(void* h, double tol, int maxit, double* x, int* iters, double* relres);
-/* CG preconditioned by gsMultiGridOp V-cycle with damped Jacobi smoothing */
+/* CG preconditioned by gsMultiGridOp with damped Jacobi smoothing; cycles = NumCycles (1 = V, 2 = W),
+ * cgc = CoarseGridCorrectionDamping */
 double orc_solve_mg(void* h, double tol, int maxit, int levels, int npre, int npost, double damping,
-                    double* x, int* iters, double* relres);
+                    int cycles, double cgc, double* x, int* iters, double* relres);
 double orc_l2_error(void* h, const double* x);
 /* Gauss-Legendre rule on [-1,1] (ascending nodes) */
 void orc_gauss(int n, double* nodes, double* weights);

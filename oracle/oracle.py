@@ -53,8 +53,8 @@ def _lib():
     lib.orc_solve_cg.restype = C.c_double
     lib.orc_solve_cg.argtypes = [vp, C.c_double, C.c_int, C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)]
     lib.orc_solve_mg.restype = C.c_double
-    lib.orc_solve_mg.argtypes = [vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_void_p,
-                                 C.POINTER(C.c_int), C.POINTER(C.c_double)]
+    lib.orc_solve_mg.argtypes = [vp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int,
+                                 C.c_double, C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)]
     lib.orc_l2_error.restype = C.c_double
     lib.orc_l2_error.argtypes = [vp, C.c_void_p]
     lib.orc_gauss.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
@@ -158,10 +158,11 @@ class OracleProblem:
         t = lib().orc_solve_cg(self.h, tol, maxit, x.ctypes.data, C.byref(it), C.byref(rr))
         return x, it.value, rr.value, t
 
-    def solve_mg(self, tol=1e-8, maxit=1000, levels=4, npre=2, npost=2, damping=0.6):
+    def solve_mg(self, tol=1e-8, maxit=1000, levels=4, npre=2, npost=2, damping=0.6, cycles=1, cgc_damping=1.0):
         x = np.zeros(self.sizes()[0])
         it, rr = C.c_int(), C.c_double()
-        t = lib().orc_solve_mg(self.h, tol, maxit, levels, npre, npost, damping, x.ctypes.data, C.byref(it), C.byref(rr))
+        t = lib().orc_solve_mg(self.h, tol, maxit, levels, npre, npost, damping, cycles, cgc_damping, x.ctypes.data,
+                               C.byref(it), C.byref(rr))
         return x, it.value, rr.value, t
 
     def l2_error(self, x):

@@ -66,6 +66,8 @@ struct Spec {
     int maxit = 1000;
     int levels = 4, npre = 2, npost = 2;
     double damping = 0.6;
+    int cycles = 1;
+    double cgc = 1.0;
 };
 
 Spec readSpec(const std::string& path) {
@@ -99,6 +101,7 @@ Spec readSpec(const std::string& path) {
         else if (tok == "quad") in >> s.quA >> s.quB;
         else if (tok == "solver") in >> s.solver >> s.tol >> s.maxit;
         else if (tok == "mg") in >> s.levels >> s.npre >> s.npost >> s.damping;
+        else if (tok == "mgcycle") in >> s.cycles >> s.cgc;
         else if (tok == "end") break;
         else { std::cerr << "bad token " << tok << "\n"; std::exit(2); }
     }
@@ -290,6 +293,8 @@ int main(int argc, char** argv) {
             gsOptionList mgopt;
             mgopt.addInt("NumPreSmooth", "", s.npre);
             mgopt.addInt("NumPostSmooth", "", s.npost);
+            mgopt.addInt("NumCycles", "", s.cycles);
+            mgopt.addReal("CoarseGridCorrectionDamping", "", s.cgc);
             mg->setOptions(mgopt);
             mg->setCoarseSolver(makeSparseCholeskySolver(mg->matrix(0)));
             for (index_t i = 1; i < mg->numLevels(); ++i) {

@@ -43,6 +43,11 @@ def cases():
     pr.mg_levels = 3
     pr.tol = 1e-8
     out["cubegrid2_p2_n4_mg"] = pr
+    pr = P.displaced_single_patch(2, (32, 24), (2, 2), 9, 0.05, ufreq=2)
+    pr.solver = "mg"
+    pr.mg_levels, pr.mg_cycles, pr.mg_cgc_damping = 4, 2, 0.8  # W-cycle, damped coarse correction
+    pr.tol = 1e-8
+    out["disp2d_p2_32x24_mgw"] = pr
     pr = P.cube_grid(n=2, n_elem=4, p=2, seed=3, kappa_modes=8)
     pr.solver = "cg"
     pr.tol = 1e-8

@@ -31,12 +31,13 @@ def _assembler(prob):
 def _mg(A, prob, tol, precision="fp64", levels=None):
     return A.solve(tol=tol, max_iters=500, method="mg", precision=precision,
                    mg_levels=levels or prob.mg_levels, mg_npre=prob.mg_npre, mg_npost=prob.mg_npost,
-                   mg_damping=prob.mg_damping)
+                   mg_damping=prob.mg_damping, mg_cycles=prob.mg_cycles, mg_cgc_damping=prob.mg_cgc_damping)
 
 
-def test_mg_matches_reference_fixture():
+@pytest.mark.parametrize("name", ["cubegrid2_p2_n4_mg", "disp2d_p2_32x24_mgw"])
+def test_mg_matches_reference_fixture(name):
+    """V-cycle (3D, 3 levels) and W-cycle with coarse-correction damping 0.8 (2D, 4 levels)."""
     from oracle import oracle as O
-    name = "cubegrid2_p2_n4_mg"
     g = load_golden(name)
     prob = golden_problem(name)
     A = _assembler(prob)
@@ -81,6 +82,47 @@ def test_mg_matches_oracle(case):
     b = A.rhs()
     assert np.linalg.norm(b - K @ x) <= 1.01e-8 * np.linalg.norm(b)
     assert abs(o.l2_error(x) - o.l2_error(xo)) <= 5e-4 * o.l2_error(xo)
+    A.close()
+
+
+@pytest.mark.parametrize("case", ["cubegrid3_p2_n4", "disp2d_p3_48x40"])
+@pytest.mark.parametrize("cycles,cgc", [(2, 1.0), (1, 0.7), (2, 0.85)])
+def test_mg_cycles_match_oracle(case, cycles, cgc):
+    """NumCycles (W-cycle) and CoarseGridCorrectionDamping against the oracle's multiGridStep."""
+    from oracle import oracle as O
+    make, levels = CASES[case]
+    prob = make()
+    o = O.OracleProblem(prob)
+    o.assemble()
+    xo, it, _, _ = o.solve_mg(1e-8, 500, levels, 2, 2, 0.6, cycles, cgc)
+    A = _assembler(prob)
+    A.assemble()
+    x, info = A.solve(tol=1e-8, max_iters=500, method="mg", mg_levels=levels, mg_cycles=cycles,
+                      mg_cgc_damping=cgc)
+    assert info["converged"], info
+    assert abs(info["iterations"] - it) <= 1, (info, it)
+    b = A.rhs()
+    assert np.linalg.norm(b - A.matrix() @ x) <= 1.01e-8 * np.linalg.norm(b)
+    assert np.linalg.norm(x - xo) <= 1e-6 * np.linalg.norm(xo)
+    # the mixed form of the same cycle
+    A.assemble("mixed")
+    xm, im = A.solve(tol=1e-8, max_iters=500, method="mg", precision="mixed", mg_levels=levels,
+                     mg_cycles=cycles, mg_cgc_damping=cgc)
+    assert im["converged"] and im["iterations"] <= info["iterations"] + 2, (im, info)
+    assert np.linalg.norm(xm - xo) <= 1e-6 * np.linalg.norm(xo)
+    A.close()
+
+
+def test_mg_cycle_limit_is_an_error():
+    """A cycle count whose coarse visits explode is refused, not captured."""
+    from gismo_gb300._lib import GsGpuError
+    prob = P.displaced_single_patch(2, (48, 40), (3, 3), 7, 0.05, ufreq=2)
+    A = _assembler(prob)
+    A.assemble()
+    with pytest.raises(GsGpuError):
+        A.solve(tol=1e-8, method="mg", mg_levels=4, mg_cycles=100)
+    x, info = A.solve(tol=1e-8, method="mg", mg_levels=4)
+    assert info["converged"]
     A.close()
 
 

@@ -80,3 +80,16 @@ def test_vcycle_is_symmetric_positive(assembled):
     z1, z2 = A.mg_apply(r1, mg_levels=3), A.mg_apply(r2, mg_levels=3)
     assert abs(r2 @ z1 - r1 @ z2) <= 1e-7 * abs(r1 @ z2)
     assert r1 @ z1 > 0 and r2 @ z2 > 0
+
+
+def test_wcycle_is_symmetric_positive(assembled):
+    A = assembled
+    rng = np.random.default_rng(9)
+    n = A.sizes()[0]
+    r1, r2 = rng.standard_normal(n), rng.standard_normal(n)
+    kw = dict(mg_levels=3, mg_cycles=2, mg_cgc_damping=0.9)
+    z1, z2 = A.mg_apply(r1, **kw), A.mg_apply(r2, **kw)
+    assert abs(r2 @ z1 - r1 @ z2) <= 1e-7 * abs(r1 @ z2)
+    assert r1 @ z1 > 0 and r2 @ z2 > 0
+    # a W-cycle is a different operator from the V-cycle
+    assert np.linalg.norm(z1 - A.mg_apply(r1, mg_levels=3)) > 1e-6 * np.linalg.norm(z1)

@@ -42,7 +42,8 @@ def test_oracle_matches_reference(path):
     if len(g["ddof"]):
         assert np.abs(o.ddof() - g["ddof"]).max() <= 1e-12 * max(1.0, np.abs(g["ddof"]).max())
     if prob.solver == "mg":
-        x, it, rr, _ = o.solve_mg(prob.tol, prob.maxit, prob.mg_levels, prob.mg_npre, prob.mg_npost, prob.mg_damping)
+        x, it, rr, _ = o.solve_mg(prob.tol, prob.maxit, prob.mg_levels, prob.mg_npre, prob.mg_npost, prob.mg_damping,
+                                  prob.mg_cycles, prob.mg_cgc_damping)
     else:
         x, it, rr, _ = o.solve_cg(prob.tol, prob.maxit)
     # the element-loop scatter order varies between OpenMP runs (as in the reference), which moves
