@@ -129,6 +129,10 @@ struct Context {
            *dLvec = nullptr;
     int *dPtr = nullptr, *dCol = nullptr, *dDiag = nullptr;
     int16_t* dColOff = nullptr;  // column - row, when every offset fits in 16 bits
+    uint8_t* dBoxFlag = nullptr; // box rows of the SpMVs (CgBuffers::box), or none
+    int* dBoxOff = nullptr;
+    int nBox = 0;
+    long long nBoxRows = 0;
     long long nnz = 0;           // non-zeros of the CSR system
     bool devPattern = false;     // pattern built on the device (no interfaces): no host col/src arrays
     uint32_t *dSrc = nullptr, *dOvfPtr = nullptr, *dOvfIdx = nullptr, *dLptr = nullptr, *dLidx = nullptr,
@@ -197,6 +201,11 @@ struct Context {
     void refreshUploads();
     void patternOnDevice(const RowPlan& rp);
     void patternFromHost();
+    void findBoxRows();
+    // SpMV bytes the box rows do not read (their column offsets) less the flags they do read
+    double boxSavedBytes() const {
+        return nBox ? double(nBoxRows) * nBox * (dColOff ? 2 : 4) - double(pat.n) : 0.0;
+    }
     void setCoefs(const double* coefs);
     void assemble(int precision);
     void solve(const gsgpu_solver_opts& o, gsgpu_solve_info& info);

@@ -15,6 +15,7 @@ namespace {
 
 constexpr int kB = 256;
 constexpr int kUnroll = 4;  // independent (value, column) -> x load chains per lane in the SpMV loops
+constexpr int kUnrollBox = 8;  // box rows: the columns come from shared memory, only values from HBM
 
 __device__ __forceinline__ double warpSum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -102,24 +103,38 @@ __device__ __forceinline__ double reducePartials(const double* part, int n) {
     return s;
 }
 
+// the block's copy of the box-row offset table (BOX kernels)
+template <bool BOX>
+__device__ __forceinline__ void stageBox(int* sbox, const int* __restrict__ off, int nbox) {
+    if (!BOX) return;
+    for (int j = threadIdx.x; j < nbox; j += blockDim.x) sbox[j] = off[j];
+    __syncthreads();
+}
+
 // t = A p (LPR lanes per row, grid-stride over row groups) and block partial sums of p.t
-template <int LPR, bool REL>
+template <int LPR, bool REL, bool BOX>
 __global__ void __launch_bounds__(kB) k_spmv_dot(int n, const int* __restrict__ ptr, const int* __restrict__ col,
-                                                 const int16_t* __restrict__ coff,
+                                                 const int16_t* __restrict__ coff, const uint8_t* __restrict__ box,
+                                                 const int* __restrict__ boxOff, int nbox,
                                                  const double* __restrict__ val, const double* __restrict__ p,
                                                  double* __restrict__ t, double* __restrict__ part,
                                                  const CgState* __restrict__ st) {
     if (st->done) return;
+    __shared__ int sbox[BOX ? launch::kMaxBox : 1];
+    stageBox<BOX>(sbox, boxOff, nbox);
     const int rowsPerBlock = kB / LPR;
     const int lane = threadIdx.x % LPR;
     double contrib = 0.0;
     for (int base = blockIdx.x * rowsPerBlock; base < n; base += gridDim.x * rowsPerBlock) {
         const int row = base + threadIdx.x / LPR;
         double s = 0.0;
-        if (row < n)
-            dev::rowMac<LPR, kUnroll, REL>(
-                row, ptr[row], ptr[row + 1], lane, col, coff, [&](int k) { return val[k]; },
-                [&](int c) { return p[c]; }, [&](double v, double x) { s += v * x; });
+        if (row < n) {
+            auto fv = [&](int k) { return val[k]; };
+            auto fx = [&](int c) { return p[c]; };
+            auto fm = [&](double v, double x) { s += v * x; };
+            if (BOX && box[row]) dev::rowMacBox<LPR, kUnroll>(row, ptr[row], ptr[row + 1], lane, sbox, fv, fx, fm);
+            else dev::rowMac<LPR, kUnroll, REL>(row, ptr[row], ptr[row + 1], lane, col, coff, fv, fx, fm);
+        }
         // every lane of the warp takes part in the shuffles (rows past n contribute 0)
         for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (row < n && lane == 0) {
@@ -239,23 +254,30 @@ __global__ void __launch_bounds__(kB) k_dinv(int n, const int* __restrict__ diag
 // FP64 iterate, so the stopping test is on the true FP64-accurate residual (iterative refinement
 // with the Krylov direction kept across replacements). Dot products accumulate in FP64.
 
-template <int LPR, bool REL>
+template <int LPR, bool REL, bool BOX>
 __global__ void __launch_bounds__(kB) k_spmv32_dot(int n, const int* __restrict__ ptr, const int* __restrict__ col,
-                                                   const int16_t* __restrict__ coff,
+                                                   const int16_t* __restrict__ coff, const uint8_t* __restrict__ box,
+                                                   const int* __restrict__ boxOff, int nbox,
                                                    const float* __restrict__ val, const float* __restrict__ p,
                                                    float* __restrict__ t, double* __restrict__ part,
                                                    const CgState* __restrict__ st) {
     if (st->done || st->pause) return;
+    __shared__ int sbox[BOX ? launch::kMaxBox : 1];
+    stageBox<BOX>(sbox, boxOff, nbox);
     const int rowsPerBlock = kB / LPR;
     const int lane = threadIdx.x % LPR;
     double contrib = 0.0;
     for (int base = blockIdx.x * rowsPerBlock; base < n; base += gridDim.x * rowsPerBlock) {
         const int row = base + threadIdx.x / LPR;
         float s = 0.f;
-        if (row < n)
-            dev::rowMac<LPR, kUnroll, REL>(
-                row, ptr[row], ptr[row + 1], lane, col, coff, [&](int k) { return val[k]; },
-                [&](int c) { return p[c]; }, [&](float v, float x) { s = fmaf(v, x, s); });
+        if (row < n) {
+            auto fv = [&](int k) { return val[k]; };
+            auto fx = [&](int c) { return p[c]; };
+            auto fm = [&](float v, float x) { s = fmaf(v, x, s); };
+            if (BOX && box[row])
+                dev::rowMacBox<LPR, kUnrollBox>(row, ptr[row], ptr[row + 1], lane, sbox, fv, fx, fm);
+            else dev::rowMac<LPR, kUnroll, REL>(row, ptr[row], ptr[row + 1], lane, col, coff, fv, fx, fm);
+        }
         for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (row < n && lane == 0) {
             t[row] = s;
@@ -446,6 +468,25 @@ __global__ void __launch_bounds__(kB) k_dinv32(int n, const int* __restrict__ di
 
 inline unsigned g1(long long n) { return unsigned((n + kB - 1) / kB); }
 
+// one warp per row: box[row] = 1 iff the row has nbox slots with columns row + off[j]
+__global__ void __launch_bounds__(kB) k_box_flags(int n, const int* __restrict__ ptr, const int* __restrict__ col,
+                                                  const int* __restrict__ off, int nbox, uint8_t* __restrict__ box,
+                                                  unsigned long long* __restrict__ count) {
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= n) return;  // whole warps
+    const int row = int(warp);
+    const int kb = ptr[row];
+    bool ok = ptr[row + 1] - kb == nbox;
+    if (ok)
+        for (int j = lane; j < nbox; j += 32) ok = ok && col[kb + j] == row + off[j];
+    ok = __all_sync(0xffffffffu, ok);
+    if (lane == 0) {
+        box[row] = ok ? 1 : 0;
+        if (ok) atomicAdd(count, 1ULL);
+    }
+}
+
 }  // namespace
 
 namespace launch {
@@ -479,9 +520,32 @@ void cgInit(const CgBuffers& B, double tol, int maxit, cudaStream_t s) {
         }                                                                                                      \
     } while (0)
 
+// kernels with the box-row template flag: <LPR, REL, BOX>
+#define GSGPU_BOX_ROW(KERNEL, L, NB, ...)                                                               \
+    do {                                                                                                \
+        const bool rel = B.coff != nullptr;                                                             \
+        if (B.box) {                                                                                    \
+            if (rel) KERNEL<L, true, true><<<NB, kB, 0, s>>>(__VA_ARGS__);                              \
+            else KERNEL<L, false, true><<<NB, kB, 0, s>>>(__VA_ARGS__);                                 \
+        } else {                                                                                        \
+            if (rel) KERNEL<L, true, false><<<NB, kB, 0, s>>>(__VA_ARGS__);                             \
+            else KERNEL<L, false, false><<<NB, kB, 0, s>>>(__VA_ARGS__);                                \
+        }                                                                                               \
+    } while (0)
+#define GSGPU_BOX_DISPATCH(KERNEL, NB, ...)                                                             \
+    do {                                                                                                \
+        switch (B.lanes_per_row) {                                                                      \
+            case 4: GSGPU_BOX_ROW(KERNEL, 4, NB, __VA_ARGS__); break;                                   \
+            case 8: GSGPU_BOX_ROW(KERNEL, 8, NB, __VA_ARGS__); break;                                   \
+            case 16: GSGPU_BOX_ROW(KERNEL, 16, NB, __VA_ARGS__); break;                                 \
+            default: GSGPU_BOX_ROW(KERNEL, 32, NB, __VA_ARGS__); break;                                 \
+        }                                                                                               \
+    } while (0)
+
 void cgSpmv(const CgBuffers& B, cudaStream_t s) {
     const int nb = spmvPartials(B.n, B.lanes_per_row);
-    GSGPU_ROW_DISPATCH(k_spmv_dot, nb, B.n, B.ptr, B.col, B.coff, B.val, B.p, B.t, B.part2, B.st);
+    GSGPU_BOX_DISPATCH(k_spmv_dot, nb, B.n, B.ptr, B.col, B.coff, B.box, B.box_off, B.nbox, B.val, B.p, B.t, B.part2,
+                       B.st);
 }
 
 void cgRest(const CgBuffers& B, cudaStream_t s) {
@@ -496,6 +560,13 @@ void cgRest(const CgBuffers& B, cudaStream_t s) {
 void cgIteration(const CgBuffers& B, cudaStream_t s) {
     cgSpmv(B, s);
     cgRest(B, s);
+}
+
+void boxFlags(int n, const int* ptr, const int* col, const int* off, int nbox, uint8_t* box,
+              unsigned long long* count, cudaStream_t s) {
+    if (n <= 0) return;
+    const long long threads = 32LL * n;
+    k_box_flags<<<unsigned((threads + kB - 1) / kB), kB, 0, s>>>(n, ptr, col, off, nbox, box, count);
 }
 
 int spmvPartials(int n, int lanes_per_row) {
@@ -516,7 +587,8 @@ void mixedInit(const CgBuffers& B, double tol, int maxit, cudaStream_t s) {
 
 void mixedSpmv(const CgBuffers& B, cudaStream_t s) {
     const int nb = spmvPartials(B.n, B.lanes_per_row);
-    GSGPU_ROW_DISPATCH(k_spmv32_dot, nb, B.n, B.ptr, B.col, B.coff, B.val_hi, B.p32, B.t32, B.part2, B.st);
+    GSGPU_BOX_DISPATCH(k_spmv32_dot, nb, B.n, B.ptr, B.col, B.coff, B.box, B.box_off, B.nbox, B.val_hi, B.p32, B.t32,
+                       B.part2, B.st);
 }
 
 void mixedRest(const CgBuffers& B, cudaStream_t s) {

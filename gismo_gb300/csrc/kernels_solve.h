@@ -28,6 +28,11 @@ struct CgBuffers {
     const int* ptr = nullptr;
     const int* col = nullptr;
     const int16_t* coff = nullptr;  // if set: column = row + coff[k] (banded patterns), col unused
+    // box rows: rows with box[row] = 1 have columns row + box_off[0..nbox) (the full neighbour box of
+    // an interior basis function); their column offsets come from a shared table in the SpMV
+    const uint8_t* box = nullptr;
+    const int* box_off = nullptr;
+    int nbox = 0;
     const double* val = nullptr;
     const double* b = nullptr;
     const double* dinv = nullptr;
@@ -50,7 +55,13 @@ void cgInit(const CgBuffers& B, double tol, int maxit, cudaStream_t s);
 void cgIteration(const CgBuffers& B, cudaStream_t s);
 void cgSpmv(const CgBuffers& B, cudaStream_t s);
 void cgRest(const CgBuffers& B, cudaStream_t s);
-constexpr int kMaxSpmvBlocks = 1024;  // SpMV grids are capped (grid-stride over rows): partials <= this
+// SpMV grids are capped (grid-stride over rows): partials <= this; 8 resident 256-thread blocks on
+// each of GB300's 152 SMs, so every SM holds the same number of blocks
+constexpr int kMaxSpmvBlocks = 152 * 8;
+constexpr int kMaxBox = 1024;  // largest box-row offset table (the (2p+1)^3 box of p <= 4)
+// box[row] = 1 iff row has exactly nbox slots with columns row + off[j]; *count = number of such rows
+void boxFlags(int n, const int* ptr, const int* col, const int* off, int nbox, uint8_t* box,
+              unsigned long long* count, cudaStream_t s);
 // mixed precision (FP32 inner iteration, FP64-accurate residual replacement)
 void jacobiDiag32(int n, const int* diag, const float* val_hi, float* dinv32, cudaStream_t s);
 void mixedInit(const CgBuffers& B, double tol, int maxit, cudaStream_t s);

@@ -40,5 +40,28 @@ __device__ __forceinline__ void rowMac(int row, int kb, int ke, int lane, const 
     for (; k < ke; k += LPR) fm(fv(k), fx(csrCol<REL>(row, k, col, coff)));
 }
 
+// a row whose columns are row + box[j], j = k - kb: the same slots, loads and accumulation order
+// as rowMac, with the column offsets read from a shared-memory table instead of HBM
+template <int LPR, int U, class FV, class FX, class FM>
+__device__ __forceinline__ void rowMacBox(int row, int kb, int ke, int lane, const int* box, FV fv, FX fx, FM fm) {
+    const int len = ke - kb;
+    int j = lane;
+    for (; j + (U - 1) * LPR < len; j += U * LPR) {
+        decltype(fv(0)) v[U];
+        int c[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            v[u] = fv(kb + j + u * LPR);
+            c[u] = row + box[j + u * LPR];
+        }
+        decltype(fx(0)) xv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) xv[u] = fx(c[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u) fm(v[u], xv[u]);
+    }
+    for (; j < len; j += LPR) fm(fv(kb + j), fx(row + box[j]));
+}
+
 }  // namespace dev
 }  // namespace gsgpu
