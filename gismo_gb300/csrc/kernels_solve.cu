@@ -6,6 +6,8 @@
 // Iteration (gsConjugateGradient::step, src/gsSolver/gsConjugateGradient.hpp:54-84):
 //   t = A p; alpha = rho / (p.t); x += alpha p; r -= alpha t; stop if ||r||/||b|| < tol;
 //   z = D^-1 r; beta = (r.z)/rho; p = z + beta p.
+#include <algorithm>
+
 #include "df32.cuh"
 #include "kernels_solve.h"
 #include "spmv_row.cuh"
@@ -15,7 +17,13 @@ namespace {
 
 constexpr int kB = 256;
 constexpr int kUnroll = 4;  // independent (value, column) -> x load chains per lane in the SpMV loops
-constexpr int kUnrollBox = 8;  // box rows: the columns come from shared memory, only values from HBM
+// FP32 SpMV steps (predicated, no serial tail): 8 loads in flight per lane for CSR rows, 11 for
+// box rows (a 7x7x7 box row of 343 slots in two steps of 16 lanes)
+constexpr int kUnrollP = 8;
+constexpr int kUnrollBox = 11;
+constexpr int kSpmv32BlocksPerSm = 6;  // 40 registers a thread for those load chains
+// the FP64 SpMV keeps rowMac (4-load steps and a scalar tail): the predicated form measured
+// slower there (C2: 74.6 vs 70.1 ms per FP64 step), the FP64 FMA rate limits it
 
 __device__ __forceinline__ double warpSum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -255,7 +263,7 @@ __global__ void __launch_bounds__(kB) k_dinv(int n, const int* __restrict__ diag
 // with the Krylov direction kept across replacements). Dot products accumulate in FP64.
 
 template <int LPR, bool REL, bool BOX>
-__global__ void __launch_bounds__(kB) k_spmv32_dot(int n, const int* __restrict__ ptr, const int* __restrict__ col,
+__global__ void __launch_bounds__(kB, kSpmv32BlocksPerSm) k_spmv32_dot(int n, const int* __restrict__ ptr, const int* __restrict__ col,
                                                    const int16_t* __restrict__ coff, const uint8_t* __restrict__ box,
                                                    const int* __restrict__ boxOff, int nbox,
                                                    const float* __restrict__ val, const float* __restrict__ p,
@@ -275,8 +283,8 @@ __global__ void __launch_bounds__(kB) k_spmv32_dot(int n, const int* __restrict_
             auto fx = [&](int c) { return p[c]; };
             auto fm = [&](float v, float x) { s = fmaf(v, x, s); };
             if (BOX && box[row])
-                dev::rowMacBox<LPR, kUnrollBox>(row, ptr[row], ptr[row + 1], lane, sbox, fv, fx, fm);
-            else dev::rowMac<LPR, kUnroll, REL>(row, ptr[row], ptr[row + 1], lane, col, coff, fv, fx, fm);
+                dev::rowMacBoxP<LPR, kUnrollBox>(row, ptr[row], ptr[row + 1], lane, sbox, fv, fx, fm);
+            else dev::rowMacP<LPR, kUnrollP, REL>(row, ptr[row], ptr[row + 1], lane, col, coff, fv, fx, fm);
         }
         for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (row < n && lane == 0) {
@@ -585,15 +593,20 @@ void mixedInit(const CgBuffers& B, double tol, int maxit, cudaStream_t s) {
     k_init_reduce<<<1, kB, 0, s>>>(np, B.part0, B.part1, B.st, tol, maxit, B.delta);
 }
 
+// FP32 SpMV grid: kSpmv32BlocksPerSm resident blocks on every SM
+int spmv32Partials(int n, int lanes_per_row) {
+    return std::min(spmvPartials(n, lanes_per_row), 152 * kSpmv32BlocksPerSm);
+}
+
 void mixedSpmv(const CgBuffers& B, cudaStream_t s) {
-    const int nb = spmvPartials(B.n, B.lanes_per_row);
+    const int nb = spmv32Partials(B.n, B.lanes_per_row);
     GSGPU_BOX_DISPATCH(k_spmv32_dot, nb, B.n, B.ptr, B.col, B.coff, B.box, B.box_off, B.nbox, B.val_hi, B.p32, B.t32,
                        B.part2, B.st);
 }
 
 void mixedRest(const CgBuffers& B, cudaStream_t s) {
     const int np = cgPartials(B.n);
-    const int nb = spmvPartials(B.n, B.lanes_per_row);
+    const int nb = spmv32Partials(B.n, B.lanes_per_row);
     k_alpha_m<<<1, kB, 0, s>>>(nb, B.part2, B.st);
     k_update32<<<np, kB, 0, s>>>(B.n, B.dx32, B.r32, B.z32, B.p32, B.t32, B.dinv32, B.part0, B.part1, B.st);
     k_beta_m<<<1, kB, 0, s>>>(np, B.part0, B.part1, B.st);

@@ -63,5 +63,53 @@ __device__ __forceinline__ void rowMacBox(int row, int kb, int ke, int lane, con
     for (; j < len; j += LPR) fm(fv(kb + j), fx(row + box[j]));
 }
 
+// rowMac without a serial tail: every step issues all U loads, slots past the row end predicated
+// off (value 0, column row), so a row takes ceil(len / (U LPR)) steps with U loads in flight each.
+// A masked slot adds fma(0, x, s) = s, so the sums equal rowMac's bit for bit.
+template <int LPR, int U, bool REL, class FV, class FX, class FM>
+__device__ __forceinline__ void rowMacP(int row, int kb, int ke, int lane, const int* __restrict__ col,
+                                        const int16_t* __restrict__ coff, FV fv, FX fx, FM fm) {
+    using V = decltype(fv(0));
+    for (int k = kb + lane; k < ke; k += U * LPR) {
+        V v[U];
+        int c[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int kk = k + u * LPR;
+            const bool ok = kk < ke;
+            v[u] = ok ? fv(kk) : V(0);
+            c[u] = ok ? csrCol<REL>(row, kk, col, coff) : row;
+        }
+        decltype(fx(0)) xv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) xv[u] = fx(c[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u) fm(v[u], xv[u]);
+    }
+}
+
+// rowMacBox with predicated steps (see rowMacP)
+template <int LPR, int U, class FV, class FX, class FM>
+__device__ __forceinline__ void rowMacBoxP(int row, int kb, int ke, int lane, const int* box, FV fv, FX fx, FM fm) {
+    using V = decltype(fv(0));
+    const int len = ke - kb;
+    for (int j = lane; j < len; j += U * LPR) {
+        V v[U];
+        int c[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int jj = j + u * LPR;
+            const bool ok = jj < len;
+            v[u] = ok ? fv(kb + jj) : V(0);
+            c[u] = ok ? row + box[jj] : row;
+        }
+        decltype(fx(0)) xv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) xv[u] = fx(c[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u) fm(v[u], xv[u]);
+    }
+}
+
 }  // namespace dev
 }  // namespace gsgpu
