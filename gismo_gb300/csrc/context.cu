@@ -88,6 +88,8 @@ void Context::buildTables() {
         mk(tabSt[2], [](const DevPatch& D) { return dev::stageWork<33>(D); });
         for (int P = 1; P <= 4; ++P) {
             mk(tabRow[0][P], [P](const DevPatch& D) { return D.p[0] == P ? dev::stageInteriorWork<31>(D) : 0LL; });
+            mk(tabTile31[P],
+               [P](const DevPatch& D) { return D.p[0] == P ? dev::stage31Tiles(D) * launch::kBlock : 0LL; });
             mk(tabRow[1][P], [P](const DevPatch& D) { return D.p[1] == P ? dev::stageInteriorWork<32>(D) : 0LL; });
             mk(tabRow[2][P], [P](const DevPatch& D) { return D.p[2] == P ? dev::stageInteriorWork<33>(D) : 0LL; });
             mk(tabRowB[0][P], [P](const DevPatch& D) { return D.p[0] == P ? dev::stageBoundaryWork<31>(D) : 0LL; });
@@ -466,8 +468,14 @@ void Context::assemble(int precision) {
                 launch::contractRowDF<31, 4, 2>(P, dPatches, tabRow[0][P].d, nb(0), tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
                 launch::contractRowDF<31, 6, 2>(P, dPatches, tabRow[0][P].d, nb(0), tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
             } else if (pd.dim == 3) {
-                launch::contractRowDF<31, 0, 4>(P, dPatches, tabRow[0][P].d, nb(0), tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
-                launch::contractRowDF<31, 4, 4>(P, dPatches, tabRow[0][P].d, nb(0), tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
+                // interior rows: shared-memory tiles where the degree allows them (they cover the same
+                // patches as tabRow[0][P]), else the unrolled row kernel
+                const bool tiled = dev::tiledStage31(P) && std::getenv("GSGPU_NO_TILE31") == nullptr;
+                const long long ni = tiled ? 0 : nb(0);
+                if (tiled)
+                    launch::stage31Tile(P, dPatches, tabTile31[P].d, (long long)tabTile31[P].h.size(), cDf, sDf, pfDf, s);
+                launch::contractRowDF<31, 0, 4>(P, dPatches, tabRow[0][P].d, ni, tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
+                launch::contractRowDF<31, 4, 4>(P, dPatches, tabRow[0][P].d, ni, tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
             } else {
                 launch::contractRowDF<21, 0, 4>(P, dPatches, tabRow[0][P].d, nb(0), tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
             }

@@ -148,6 +148,7 @@ struct Context {
     Tab tabPf, tabCoef, tabGeo1, tabGeo2, tabPoint, tabSt[3], tabLd[3];
     Tab tabRow[3][5];  // [stage][degree along the stage axis]: interior rows of simple axes
     Tab tabRowB[3][5]; // the remaining rows
+    Tab tabTile31[5];  // 3D stage 1 interior rows in shared-memory tiles (degrees 2, 3)
 
     // device buffers (solve)
     int solveN = -1;

@@ -746,6 +746,29 @@ GS_HD void contractRowDFInterior(const DevPatch& D, long long item, const df32* 
         for (int h = 0; h < NH; ++h) op[(H0 + h) * G.out_fs + w * G.inner] = acc[w][h].result();
 }
 
+// 3D stage 1 for the interior rows of a simple axis 0, in tiles of kTileLines lines (o) by
+// kTileRows consecutive rows (i) per block, one launch per output half (h 0-3, h 4-7); degrees 2
+// and 3, other degrees keep contractRowDFInterior
+constexpr int kTileLines = 8, kTileRows = 32;
+GS_HD bool tiledStage31(int P) { return P == 2 || P == 3; }
+GS_HD long long stage31Tiles(const DevPatch& D) {
+    const int m = interiorRows<31>(D);
+    if (D.dim != 3 || m == 0 || !tiledStage31(D.p[0])) return 0;
+    const StageGeom g = stageGeom<31>(D);
+    return (g.outer + kTileLines - 1) / kTileLines * ((m + kTileRows - 1) / kTileRows);
+}
+// the stage-1 terms of outputs H0..H0+3 read a contiguous range of input fields and of pair
+// factor types (Stage<31>::term): h 0-3 fields 0-2, types 1-3; h 4-7 fields 2-5, types 0-1
+GS_HD constexpr int tileField0(int H0) { return H0 == 0 ? 0 : 2; }
+GS_HD constexpr int tileNField(int H0) { return H0 == 0 ? 3 : 4; }
+GS_HD constexpr int tileTau0(int H0) { return H0 == 0 ? 1 : 0; }
+GS_HD constexpr int tileNTau(int H0) { return H0 == 0 ? 3 : 2; }
+// shared memory of a tile: pair factors [si][rr][t][tau][ee] and fields [f][rr][line][ee],
+// ee = element - first element of the tile
+GS_HD constexpr int tileElems(int P) { return kTileRows + P; }
+GS_HD constexpr int tilePfCount(int P, int H0) { return (P + 1) * (P + 1) * (P + 1) * tileNTau(H0) * tileElems(P); }
+GS_HD constexpr int tileFieldCount(int P, int H0) { return tileNField(H0) * (P + 1) * kTileLines * tileElems(P); }
+
 // degree dispatch of the row-blocked contraction (uniform per patch)
 template <int KIND, int H0, int NH>
 GS_HD void contractRowDFp(const DevPatch& D, long long item, const df32* __restrict__ in, df32* __restrict__ out,

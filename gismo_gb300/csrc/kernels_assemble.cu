@@ -133,6 +133,98 @@ __global__ void __launch_bounds__(kBlock, 2) k_contract_row_df_int(const DevPatc
     dev::contractRowDFInterior<KIND, DEG, H0, NH>(D, item, in, out, pf);
 }
 
+// 3D stage 1 (axis 0) interior rows, tiled (dev::stage31Tiles), outputs H0..H0+3: the block
+// stages the pair factors of its elements and the coefficient fields of its lines that those
+// outputs use in shared memory, laid out so that the 32 rows of a warp read consecutive words,
+// then each thread forms the outputs of its row. The products and the Dot2 order per output are
+// those of contractRowDFInterior<31>, so the results are the same bit for bit; what changes is
+// where the operands come from (shared memory instead of strided L1 traffic).
+template <int P, int H0>
+__global__ void __launch_bounds__(dev::kTileLines * dev::kTileRows, 2)
+    k_stage31_tile(const DevPatch* __restrict__ Pd, const BlkEnt* __restrict__ tab, const df32* __restrict__ in,
+                   df32* __restrict__ out, const df32* __restrict__ pf) {
+    using S = dev::Stage<31>;
+    constexpr int P1 = P + 1, Q = P + 1, W = 2 * P + 1, LB = dev::kTileLines, RB = dev::kTileRows;
+    constexpr int NE = dev::tileElems(P);
+    constexpr int F0 = dev::tileField0(H0), NF = dev::tileNField(H0);
+    constexpr int T0 = dev::tileTau0(H0), NTAU = dev::tileNTau(H0);
+    extern __shared__ df32 smem[];
+    df32* sPF = smem;
+    df32* sX = smem + dev::tilePfCount(P, H0);
+    const BlkEnt be = tab[blockIdx.x];
+    const DevPatch& D = Pd[be.patch];
+    const dev::StageGeom G = dev::stageGeom<31>(D);
+    const int n = D.n[0], E = D.E[0], Qa = D.Q[0];
+    const int m = n - 2 * P;
+    const int nseg = (m + RB - 1) / RB;
+    const long long tile = be.base / kBlock;
+    const long long o0 = tile / nseg * LB;
+    const int seg = int(tile % nseg);
+    const int i0 = P + seg * RB;
+    const int e0 = i0 - P;
+    const int ne = min(NE, E - e0);
+    const int nl = int(min((long long)LB, G.outer - o0));
+    // pair factors of elements e0 .. e0+ne-1, types T0 .. T0+NTAU-1 (contiguous per type)
+    const long long tstride = (long long)E * Q * P1 * P1;
+    const df32* pfa = pf + D.pfoff[0] + T0 * tstride + (long long)e0 * Q * P1 * P1;
+    const int per = ne * Q * P1 * P1;
+    for (int idx = threadIdx.x; idx < NTAU * per; idx += blockDim.x) {
+        const int tau = idx / per;
+        const int j = idx - tau * per;
+        int r = j;
+        const int t = r % P1;
+        r /= P1;
+        const int si = r % P1;
+        r /= P1;
+        const int rr = r % Q;
+        const int ee = r / Q;
+        sPF[(((si * Q + rr) * P1 + t) * NTAU + tau) * NE + ee] = pfa[tau * tstride + j];
+    }
+    // fields F0 .. F0+NF-1 of the tile's lines at the points of those elements
+    const int perl = ne * Q;
+    for (int idx = threadIdx.x; idx < NF * nl * perl; idx += blockDim.x) {
+        const int f = idx / (nl * perl);
+        int r = idx - f * nl * perl;
+        const int l = r / perl;
+        r -= l * perl;
+        const int rr = r % Q;
+        const int ee = r / Q;
+        sX[((f * Q + rr) * LB + l) * NE + ee] =
+            in[G.in_base + (F0 + f) * G.in_fs + (o0 + l) * Qa + (long long)e0 * Q + r];
+    }
+    __syncthreads();
+    const int l = threadIdx.x / RB, rw = threadIdx.x % RB;
+    const int i = i0 + rw;
+    if (l >= nl || i >= n - P) return;
+    const df32* sx = sX + l * NE + rw;
+    const df32* spf = sPF + rw;
+    Dot2 acc[W][4];
+#pragma unroll
+    for (int k = 0; k <= P; ++k) {
+#pragma unroll
+        for (int rr = 0; rr < Q; ++rr) {
+            df32 x[NF];
+#pragma unroll
+            for (int f = 0; f < NF; ++f) x[f] = sx[(f * Q + rr) * LB * NE + k];
+            const df32* prow = spf + ((P - k) * Q + rr) * P1 * NTAU * NE + k;
+#pragma unroll
+            for (int t = 0; t < P1; ++t) {
+#pragma unroll
+                for (int kk = 0; kk < S::NT; ++kk) {
+                    const dev::Term tm = S::term(kk);
+                    if (tm.h >= H0 && tm.h < H0 + 4)
+                        acc[k + t][tm.h - H0].mac(prow[(t * NTAU + tm.tau - T0) * NE], x[tm.f - F0]);
+                }
+            }
+        }
+    }
+    df32* op = out + G.out_base + ((o0 + l) * n + i) * W;
+#pragma unroll
+    for (int w = 0; w < W; ++w)
+#pragma unroll
+        for (int h = 0; h < 4; ++h) op[(H0 + h) * G.out_fs + w] = acc[w][h].result();
+}
+
 // the remaining (boundary) rows with the general element loop
 template <int KIND, int DEG, int H0, int NH>
 __global__ void __launch_bounds__(kBlock) k_contract_row_df_bnd(const DevPatch* __restrict__ P,
@@ -279,6 +371,27 @@ void contractRowDF(int P, const DevPatch* Pd, const BlkEnt* tabInt, long long nI
     }
 #undef ROW_CASE
 }
+template <int P, int H0>
+void stage31TileLaunch(const DevPatch* Pd, const BlkEnt* tab, long long ntiles, const df32* in, df32* out,
+                       const df32* pf, cudaStream_t s) {
+    constexpr size_t bytes = size_t(dev::tilePfCount(P, H0) + dev::tileFieldCount(P, H0)) * sizeof(df32);
+    // a failure here shows as the launch error the caller checks
+    cudaFuncSetAttribute(k_stage31_tile<P, H0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+    k_stage31_tile<P, H0><<<unsigned(ntiles), dev::kTileLines * dev::kTileRows, bytes, s>>>(Pd, tab, in, out, pf);
+}
+
+void stage31Tile(int P, const DevPatch* Pd, const BlkEnt* tab, long long ntiles, const df32* in, df32* out,
+                 const df32* pf, cudaStream_t s) {
+    if (ntiles <= 0) return;
+    if (P == 2) {
+        stage31TileLaunch<2, 0>(Pd, tab, ntiles, in, out, pf, s);
+        stage31TileLaunch<2, 4>(Pd, tab, ntiles, in, out, pf, s);
+    } else if (P == 3) {
+        stage31TileLaunch<3, 0>(Pd, tab, ntiles, in, out, pf, s);
+        stage31TileLaunch<3, 4>(Pd, tab, ntiles, in, out, pf, s);
+    }
+}
+
 #define INST_ROW(K, H0, NH)                                                                                      \
     template void contractRowDF<K, H0, NH>(int, const DevPatch*, const BlkEnt*, long long, const BlkEnt*, long long, \
                                            const df32*, df32*, const int*, const df32*, cudaStream_t);

@@ -109,6 +109,14 @@ void gaussLegendre(int n, std::vector<double>& x, std::vector<double>& w) {
 // ---------------------------------------------------------------------------------------------
 // closed-form fields: kappa = exp(alpha g), g = scale sum_m amp_m cos(pi k_m.x + phase_m),
 // u = prod_i sin(freq pi x_i), f = -div(kappa grad u)
+// u alone (the Dirichlet data): the same operations as the u of evalFields, so the same value
+static double evalU(const FieldParams& F, const double* x) {
+    const double w = F.ufreq * M_PI;
+    double u = 1.0;
+    for (int i = 0; i < F.dim; ++i) u *= std::sin(w * x[i]);
+    return u;
+}
+
 void evalFields(const FieldParams& F, const double* x, double& kappa, double& f, double& u) {
     const int d = F.dim;
     const double w = F.ufreq * M_PI;
@@ -703,31 +711,6 @@ void buildPattern(const ProblemDesc& pd, const DofMap& map, const Layout& L, Pat
 }
 
 // ---------------------------------------------------------------------------------------------
-static void geoEvalHost(const HostPatch& P, const double* xi, double* x) {
-    const int d = P.dim;
-    int first[3] = {0, 0, 0}, pp[3] = {0, 0, 0}, ng[3] = {1, 1, 1};
-    double v[3][32];
-    double buf[64];
-    for (int k = 0; k < d; ++k) {
-        const Basis1D& B = P.g[k];
-        const int s = B.span(xi[k]);
-        B.eval(s, xi[k], buf);
-        first[k] = s - B.p;
-        pp[k] = B.p;
-        ng[k] = B.n();
-        for (int r = 0; r <= B.p; ++r) v[k][r] = buf[r];
-    }
-    for (int m = 0; m < d; ++m) x[m] = 0.0;
-    for (int c = 0; c <= pp[2]; ++c)
-        for (int b = 0; b <= pp[1]; ++b)
-            for (int a = 0; a <= pp[0]; ++a) {
-                const long long gi = first[0] + a + (long long)ng[0] * (first[1] + b + (d == 3 ? (long long)ng[1] * (first[2] + c) : 0));
-                double w = v[0][a] * v[1][b];
-                if (d == 3) w *= v[2][c];
-                for (int m = 0; m < d; ++m) x[m] += w * P.coefs[gi * d + m];
-            }
-}
-
 // values of one Dirichlet side at its boundary dofs (sideDofs order); `par`: OpenMP inside the side
 static std::vector<double> sideValues(const ProblemDesc& pd, size_t si, bool par) {
     const int dim = pd.dim;
@@ -741,22 +724,61 @@ static std::vector<double> sideValues(const ProblemDesc& pd, size_t si, bool par
     for (int o = 0; o < no; ++o) { gv[o] = P.b[odirs[o]].greville(); npts *= int(gv[o].size()); }
     const double fixv = parity ? P.b[dir].t.back() : P.b[dir].t.front();
     const FieldParams& F = pd.fieldsOf(pd.dsides[si]);
-    std::vector<double> f(npts);
-#pragma omp parallel for schedule(static) if (par)
-    for (int i = 0; i < npts; ++i) {
-        double xi[3] = {0, 0, 0}, x[3];
-        int r = i;
-        for (int o = 0; o < no; ++o) {
-            const int c = r % int(gv[o].size());
-            r /= int(gv[o].size());
-            xi[odirs[o]] = gv[o][c];
-        }
-        xi[dir] = fixv;
-        geoEvalHost(P, xi, x);
-        double kap, ff, u;
-        evalFields(F, x, kap, ff, u);
-        f[i] = u;
+    // the geometry map on the side's Greville grid, sum-factorised: the geometry control points
+    // contracted with the basis of the fixed direction at the side's parameter, then with the
+    // basis of one side direction at a time (each evaluated once per abscissa)
+    const int ng[3] = {P.g[0].n(), dim > 1 ? P.g[1].n() : 1, dim > 2 ? P.g[2].n() : 1};
+    const long long gstride[3] = {1, ng[0], (long long)ng[0] * ng[1]};
+    auto basisAt = [](const Basis1D& B, double u, int& first, std::vector<double>& v) {
+        std::vector<double> buf(2 * (B.p + 1));
+        const int sp = B.span(u);
+        B.eval(sp, u, buf.data());
+        first = sp - B.p;
+        v.assign(buf.begin(), buf.begin() + B.p + 1);
+    };
+    int ffirst;
+    std::vector<double> fv;
+    basisAt(P.g[dir], fixv, ffirst, fv);
+    // F[j0 + n0 j1][m] over the control points of the side directions
+    const int n0 = ng[odirs[0]], n1 = no > 1 ? ng[odirs[1]] : 1;
+    std::vector<double> Fc(size_t(n0) * n1 * dim, 0.0);
+    for (int j1 = 0; j1 < n1; ++j1)
+        for (int j0 = 0; j0 < n0; ++j0)
+            for (int c = 0; c <= P.g[dir].p; ++c) {
+                long long gi = (long long)j0 * gstride[odirs[0]] + (long long)(ffirst + c) * gstride[dir];
+                if (no > 1) gi += (long long)j1 * gstride[odirs[1]];
+                for (int m = 0; m < dim; ++m) Fc[(size_t(j0) + size_t(n0) * j1) * dim + m] += fv[c] * P.coefs[gi * dim + m];
+            }
+    // direction odirs[0] at its abscissae: G[a + na j1][m]
+    const int na = int(gv[0].size()), nb = no > 1 ? int(gv[1].size()) : 1;
+    std::vector<double> G(size_t(na) * n1 * dim, 0.0);
+    for (int a = 0; a < na; ++a) {
+        int f0;
+        std::vector<double> v0;
+        basisAt(P.g[odirs[0]], gv[0][a], f0, v0);
+        for (int j1 = 0; j1 < n1; ++j1)
+            for (int i = 0; i < int(v0.size()); ++i)
+                for (int m = 0; m < dim; ++m)
+                    G[(size_t(a) + size_t(na) * j1) * dim + m] += v0[i] * Fc[(size_t(f0 + i) + size_t(n0) * j1) * dim + m];
     }
+    // direction odirs[1] (3D) at its abscissae: the points x[a + na b][m]
+    std::vector<double> X(size_t(npts) * dim, 0.0);
+    if (no > 1) {
+        for (int b = 0; b < nb; ++b) {
+            int f1;
+            std::vector<double> v1;
+            basisAt(P.g[odirs[1]], gv[1][b], f1, v1);
+            for (int a = 0; a < na; ++a)
+                for (int j = 0; j < int(v1.size()); ++j)
+                    for (int m = 0; m < dim; ++m)
+                        X[(size_t(a) + size_t(na) * b) * dim + m] += v1[j] * G[(size_t(a) + size_t(na) * (f1 + j)) * dim + m];
+        }
+    } else {
+        X = G;
+    }
+    std::vector<double> f(npts);
+#pragma omp parallel for schedule(static) if (par && npts >= 4096)
+    for (int i = 0; i < npts; ++i) f[i] = evalU(F, &X[size_t(i) * dim]);
     // tensor collocation solve, one direction at a time (LU with partial pivoting). The
     // collocation matrix is banded (p sub- and super-diagonals); with pivoting inside the band the
     // factors stay within w = 3(p+1) of the diagonal, so the loops skip only exact zeros.
@@ -812,10 +834,11 @@ static std::vector<double> sideValues(const ProblemDesc& pd, size_t si, bool par
 void dirichletValues(const ProblemDesc& pd, const DofMap& map, std::vector<double>& ddof) {
     ddof.assign(map.boundarySize, 0.0);
     const int nsides = int(pd.dsides.size() / 2);
-    // many sides (batches, multipatch): one side per thread; few sides: threads inside each side
-    const bool across = nsides >= 32;
+    // one side per thread; threads inside the side only for a single side (the work of one side is
+    // a few milliseconds at most, below what OpenMP regions inside it would save)
+    const bool across = nsides >= 2;
     std::vector<std::vector<double>> vals(nsides);
-#pragma omp parallel for schedule(dynamic, 4) if (across)
+#pragma omp parallel for schedule(dynamic, 1) if (across)
     for (int k = 0; k < nsides; ++k) vals[k] = sideValues(pd, size_t(2 * k), !across);
     // scatter in side order (a dof on two sides takes the later side's value)
     std::vector<int> bd;

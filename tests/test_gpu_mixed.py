@@ -72,3 +72,33 @@ def test_mixed_needs_mixed_assembly():
         A.solve(precision="mixed")
     assert e.value.code == ERR_STATE
     A.close()
+
+
+TILE_CASES = {
+    "volume_p3_16": lambda: P.volume_poisson(16, 3, seed=2),
+    "volume_p3_40": lambda: P.volume_poisson(40, 3, seed=6),  # two row segments per line
+    "disp3d_p2_40x10x12": lambda: P.displaced_single_patch(3, (40, 10, 12), (2, 2, 2), 4, 0.04),
+    "disp3d_p3x2x4_36x8x9": lambda: P.displaced_single_patch(3, (36, 8, 9), (3, 2, 4), 5, 0.04),
+    "cubegrid2_p2_n4": lambda: P.cube_grid(n=2, n_elem=4, p=2, seed=3, kappa_modes=8),
+}
+
+
+@pytest.mark.parametrize("case", sorted(TILE_CASES))
+def test_stage31_tiles_are_bitwise_neutral(case):
+    """Stage 1 of the df32 stiffness contraction in shared-memory tiles gives the operator of the
+    row kernel bit for bit (same products, same compensated summation order)."""
+    import os
+    from gismo_gb300.assembler import GpuPoissonAssembler
+    prob = TILE_CASES[case]()
+    vals = []
+    for off in (False, True):
+        if off:
+            os.environ["GSGPU_NO_TILE31"] = "1"
+        try:
+            A = GpuPoissonAssembler(prob)
+            A.assemble("mixed")
+            vals.append(A.csr()[2])
+            A.close()
+        finally:
+            os.environ.pop("GSGPU_NO_TILE31", None)
+    assert np.array_equal(vals[0], vals[1])
