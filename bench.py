@@ -343,7 +343,8 @@ def main():
     achieved = sp_bytes / (sp_ms / nl * 1e-3) / 1e9 if nl else None
     if args.mode == "mixed":
         traffic = profiled_traffic("k_spmv32_dot_volume_p3_64")
-        kname = "k_spmv32_dot (CSR SpMV + p.Ap of the FP32 inner operator, int16 column offsets)"
+        kname = ("k_spmv32_dot (CSR SpMV + p.Ap of the FP32 inner operator; box rows take their column "
+                 "offsets from shared memory, the other rows int16 offsets)")
     else:
         traffic = profiled_traffic("k_spmv_dot_fp64_volume_p3_64")
         kname = "k_spmv_dot (CSR SpMV + p.Ap, FP64 values)"
@@ -356,9 +357,11 @@ def main():
     it = infos[-1]["iterations"]
     chunks = math.ceil(it / 16) + 1 if it else 1
     if args.mode == "mixed":
-        # assemble: basis 2, pair 1, to_df 2, geo 2, point 1, contraction 4, load 3, gather 1, rhs 1;
-        # solve: dinv 1, init 2, per graph chunk 16 x 5 iteration kernels + 5 replacement kernels
-        launches_per_step = 17 + 3 + (16 * 5 + 5) * chunks
+        # assemble: basis 2, pair 1, to_df 2, geo 2, point 1, contraction 7 (stage 1: two tile
+        # launches + two boundary-row launches; stage 2: interior + boundary rows; stage 3), load 3,
+        # gather 1, rhs 1; solve: dinv 1, init 2, per graph chunk 16 x 5 iteration kernels + 5
+        # replacement kernels
+        launches_per_step = 20 + 3 + (16 * 5 + 5) * chunks
     else:
         launches_per_step = 13 + 3 + 5 * 16 * chunks
     amean = np.mean(np.array(asm_ms), axis=0)
