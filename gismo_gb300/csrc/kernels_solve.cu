@@ -30,18 +30,6 @@ __device__ __forceinline__ double warpSum(double v) {
     return v;
 }
 
-// block sum of one value per thread into out[blockIdx.x] (fixed order -> deterministic)
-__device__ __forceinline__ void blockSumStore(double v, double* out) {
-    __shared__ double ws[kB / 32];
-    v = warpSum(v);
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int w = 0; w < kB / 32; ++w) s += ws[w];
-        out[blockIdx.x] = s;
-    }
-}
 __device__ __forceinline__ void blockSumStore2(double a, double b, double* outa, double* outb) {
     __shared__ double wa[kB / 32], wb[kB / 32];
     a = warpSum(a);
@@ -114,9 +102,10 @@ __device__ __forceinline__ double reducePartials(const double* part, int n) {
 // the block's copy of the box-row offset table (BOX kernels)
 template <bool BOX>
 __device__ __forceinline__ void stageBox(int* sbox, const int* __restrict__ off, int nbox) {
-    if (!BOX) return;
-    for (int j = threadIdx.x; j < nbox; j += blockDim.x) sbox[j] = off[j];
-    __syncthreads();
+    if constexpr (BOX) {
+        for (int j = threadIdx.x; j < nbox; j += blockDim.x) sbox[j] = off[j];
+        __syncthreads();
+    }
 }
 
 // t = A p (LPR lanes per row, grid-stride over row groups) and block partial sums of p.t
