@@ -15,7 +15,7 @@ EXPORTS = [
     "gsgpu_solve", "gsgpu_l2_error", "gsgpu_min_jacobian", "gsgpu_assemble_times", "gsgpu_stream",
     "gsgpu_set_profiling", "gsgpu_spmv_stats", "gsgpu_cg_jacobi_noalloc", "gsgpu_set_batch", "gsgpu_batch_info",
     "gsgpu_batch_l2_error", "gsgpu_server_create", "gsgpu_server_submit", "gsgpu_server_wait",
-    "gsgpu_server_last_error", "gsgpu_server_destroy", "gsgpu_apply", "gsgpu_mg_apply",
+    "gsgpu_server_last_error", "gsgpu_server_destroy", "gsgpu_apply", "gsgpu_mg_apply", "gsgpu_set_fixed_dofs",
 ]
 
 OK, ERR_INVALID, ERR_CUDA, ERR_BUDGET, ERR_NOT_CONVERGED, ERR_JACOBIAN, ERR_STATE, ERR_TIMEOUT = range(8)
@@ -85,6 +85,7 @@ def lib() -> C.CDLL:
         L.gsgpu_matrix_csr.argtypes = [vp, vp, vp, vp]
         L.gsgpu_rhs.argtypes = [vp, vp]
         L.gsgpu_fixed_dofs.argtypes = [vp, vp]
+        L.gsgpu_set_fixed_dofs.argtypes = [vp, vp, C.c_int]
         L.gsgpu_dof_map.argtypes = [vp, vp]
         L.gsgpu_solve.argtypes = [vp, C.POINTER(SolverOpts), vp, C.POINTER(SolveInfo)]
         L.gsgpu_l2_error.argtypes = [vp, C.POINTER(C.c_double)]

@@ -166,6 +166,15 @@ class GpuPoissonAssembler:
         self._check(self.L.gsgpu_mg_apply(self.h, C.byref(o), r.ctypes.data, z.ctypes.data))
         return z
 
+    def set_fixed_dofs(self, ddof):
+        """Eliminated-dof values for the next assembles (e.g. the caller's own interpolation or
+        L2 projection of the Dirichlet data); None restores the built-in interpolation."""
+        if ddof is None:
+            self._check(self.L.gsgpu_set_fixed_dofs(self.h, None, 0))
+            return
+        self._fixed = np.ascontiguousarray(ddof, np.float64)
+        self._check(self.L.gsgpu_set_fixed_dofs(self.h, self._fixed.ctypes.data, len(self._fixed)))
+
     def l2_error(self) -> float:
         """gsField::distanceL2 of the last solution against the manufactured solution."""
         v = C.c_double()

@@ -406,7 +406,8 @@ void Context::assemble(int precision) {
     dir.th = std::thread([&] {
         try {
             auto t0 = std::chrono::steady_clock::now();
-            dirichletValues(pd, map, ddofNew);
+            if (ddofFromUser) ddofNew = ddofUser;
+            else dirichletValues(pd, map, ddofNew);
             dirMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         } catch (...) {
             dir.err = std::current_exception();
@@ -1144,6 +1145,23 @@ int gsgpu_fixed_dofs(gsgpu_context* ctx, double* ddof) {
         auto& c = ctx->c;
         if (!c.assembled) throw gsgpu::StateError("fixedDofs() before assemble()");
         std::copy(c.ddof.begin(), c.ddof.end(), ddof);
+    });
+}
+
+int gsgpu_set_fixed_dofs(gsgpu_context* ctx, const double* ddof, int n) {
+    return guarded(ctx, [&] {
+        auto& c = ctx->c;
+        if (!c.refreshed) throw gsgpu::StateError("set_fixed_dofs() before refresh()");
+        if (!ddof) {
+            c.ddofUser.clear();
+            c.ddofFromUser = false;
+            return;
+        }
+        if (n != c.map.boundarySize)
+            throw std::invalid_argument("set_fixed_dofs(): " + std::to_string(n) + " values for " +
+                                        std::to_string(c.map.boundarySize) + " eliminated dofs");
+        c.ddofUser.assign(ddof, ddof + n);
+        c.ddofFromUser = true;
     });
 }
 

@@ -134,6 +134,8 @@ struct Context {
     int nBox = 0;
     long long nBoxRows = 0;
     long long nnz = 0;           // non-zeros of the CSR system
+    std::vector<double> ddofUser;  // eliminated-dof values given by the caller (gsgpu_set_fixed_dofs)
+    bool ddofFromUser = false;
     bool devPattern = false;     // pattern built on the device (no interfaces): no host col/src arrays
     uint32_t *dSrc = nullptr, *dOvfPtr = nullptr, *dOvfIdx = nullptr, *dLptr = nullptr, *dLidx = nullptr,
              *dFptr = nullptr, *dFband = nullptr, *dFbidx = nullptr;

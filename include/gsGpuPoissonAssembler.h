@@ -40,6 +40,80 @@ struct gsGpuFields {
     int ufreq = 1;
 };
 
+/// A G+Smo problem packed into the C-ABI struct (include/gsgpu.h gsgpu_problem) together with the
+/// arrays it points to: tensor B-spline patches and bases, conforming identity-oriented
+/// interfaces, the Dirichlet sides (patch, side index pairs) and the device fields
+template <class T = real_t>
+struct gsGpuProblemPack {
+    std::vector<int> degree, nknots, gdegree, gnknots, ifaces, dsides;
+    std::vector<double> knots, gknots, coefs;
+    gsGpuFields fields;
+    gsgpu_problem prob{};
+
+    void pack(const gsMultiPatch<T>& mp, const gsMultiBasis<T>& mb, const std::vector<int>& dirichletSides,
+              const gsGpuFields& f, double quA, int quB) {
+        const short_t d = mp.parDim();
+        degree.clear(); nknots.clear(); knots.clear(); gdegree.clear(); gnknots.clear(); gknots.clear();
+        coefs.clear(); ifaces.clear();
+        for (size_t k = 0; k < mp.nPatches(); ++k) {
+            if (d == 2) packPatch<2>(mp, mb, index_t(k));
+            else if (d == 3) packPatch<3>(mp, mb, index_t(k));
+            else throw std::invalid_argument("gsgpu: dimension 2 or 3 only");
+        }
+        for (typename gsMultiPatch<T>::const_iiterator it = mp.iBegin(); it != mp.iEnd(); ++it) {
+            if (!it->dirOrientation().all()) throw std::invalid_argument("gsgpu: re-oriented interface");
+            for (index_t i = 0; i < it->dirMap().size(); ++i)
+                if (it->dirMap()(i) != i) throw std::invalid_argument("gsgpu: permuted interface");
+            ifaces.push_back(it->first().patch);
+            ifaces.push_back(it->first().side().index());
+            ifaces.push_back(it->second().patch);
+            ifaces.push_back(it->second().side().index());
+        }
+        dsides = dirichletSides;
+        fields = f;
+        prob = gsgpu_problem{};
+        prob.dim = d;
+        prob.npatches = int(mp.nPatches());
+        prob.degree = degree.data(); prob.nknots = nknots.data(); prob.knots = knots.data();
+        prob.gdegree = gdegree.data(); prob.gnknots = gnknots.data(); prob.gknots = gknots.data();
+        prob.coefs = coefs.data();
+        prob.ninterfaces = int(ifaces.size() / 4); prob.interfaces = ifaces.data();
+        prob.ndirichlet = int(dsides.size() / 2); prob.dirichlet = dsides.data();
+        prob.kappa_fourier = fields.kappaFourier ? 1 : 0;
+        prob.kappa_const = fields.kappaConst; prob.kappa_alpha = fields.kappaAlpha; prob.kappa_scale = fields.kappaScale;
+        prob.kappa_nmodes = int(fields.amp.size());
+        prob.kappa_amp = fields.amp.data(); prob.kappa_k = fields.waves.data(); prob.kappa_phase = fields.phase.data();
+        prob.ufreq = fields.ufreq;
+        prob.quA = quA;
+        prob.quB = quB;
+    }
+
+private:
+    template <short_t D>
+    void packPatch(const gsMultiPatch<T>& mp, const gsMultiBasis<T>& mb, index_t k) {
+        const gsTensorBSplineBasis<D, T>* db = dynamic_cast<const gsTensorBSplineBasis<D, T>*>(&mb[k]);
+        const gsTensorBSpline<D, T>* geo = dynamic_cast<const gsTensorBSpline<D, T>*>(&mp.patch(k));
+        if (!db || !geo) throw std::invalid_argument("gsgpu: tensor B-spline patches and bases only");
+        for (short_t i = 0; i < 3; ++i) {
+            if (i < D) {
+                const gsKnotVector<T>& kv = db->knots(i);
+                degree.push_back(kv.degree());
+                nknots.push_back(index_t(kv.size()));
+                knots.insert(knots.end(), kv.begin(), kv.end());
+                const gsKnotVector<T>& gk = geo->basis().knots(i);
+                gdegree.push_back(gk.degree());
+                gnknots.push_back(index_t(gk.size()));
+                gknots.insert(gknots.end(), gk.begin(), gk.end());
+            } else {
+                degree.push_back(0); nknots.push_back(0); gdegree.push_back(0); gnknots.push_back(0);
+            }
+        }
+        const gsMatrix<T>& c = geo->coefs();
+        for (index_t r = 0; r < c.rows(); ++r)
+            for (index_t m = 0; m < c.cols(); ++m) coefs.push_back(c(r, m));
+    }
+};
+
 template <class T = real_t>
 class gsGpuPoissonAssembler : public gsPoissonAssembler<T> {
 public:
@@ -147,80 +221,23 @@ private:
             throw std::runtime_error(std::string("gsgpu: ") + (m_ctx ? gsgpu_last_error(m_ctx) : "no context"));
     }
 
-    template <short_t D>
-    void packPatch(index_t k) {
-        const gsTensorBSplineBasis<D, T>* db =
-            dynamic_cast<const gsTensorBSplineBasis<D, T>*>(&this->m_bases[0][k]);
-        const gsTensorBSpline<D, T>* geo = dynamic_cast<const gsTensorBSpline<D, T>*>(&this->patches().patch(k));
-        if (!db || !geo) throw std::invalid_argument("gsGpuPoissonAssembler: tensor B-spline patches and bases only");
-        for (short_t i = 0; i < 3; ++i) {
-            if (i < D) {
-                const gsKnotVector<T>& kv = db->knots(i);
-                m_degree.push_back(kv.degree());
-                m_nknots.push_back(index_t(kv.size()));
-                m_knots.insert(m_knots.end(), kv.begin(), kv.end());
-                const gsKnotVector<T>& gk = geo->basis().knots(i);
-                m_gdegree.push_back(gk.degree());
-                m_gnknots.push_back(index_t(gk.size()));
-                m_gknots.insert(m_gknots.end(), gk.begin(), gk.end());
-            } else {
-                m_degree.push_back(0); m_nknots.push_back(0); m_gdegree.push_back(0); m_gnknots.push_back(0);
-            }
-        }
-        const gsMatrix<T>& c = geo->coefs();
-        for (index_t r = 0; r < c.rows(); ++r)
-            for (index_t m = 0; m < c.cols(); ++m) m_coefs.push_back(c(r, m));
-    }
-
     void upload() {
-        const gsMultiPatch<T>& mp = this->patches();
-        const short_t d = mp.parDim();
-        m_degree.clear(); m_nknots.clear(); m_knots.clear();
-        m_gdegree.clear(); m_gnknots.clear(); m_gknots.clear(); m_coefs.clear();
-        m_ifaces.clear(); m_dsides.clear();
-        for (size_t k = 0; k < mp.nPatches(); ++k) {
-            if (d == 2) packPatch<2>(index_t(k));
-            else if (d == 3) packPatch<3>(index_t(k));
-            else throw std::invalid_argument("gsGpuPoissonAssembler: dimension 2 or 3 only");
-        }
-        for (typename gsMultiPatch<T>::const_iiterator it = mp.iBegin(); it != mp.iEnd(); ++it) {
-            if (!it->dirOrientation().all()) throw std::invalid_argument("gsGpuPoissonAssembler: re-oriented interface");
-            for (index_t i = 0; i < it->dirMap().size(); ++i)
-                if (it->dirMap()(i) != i) throw std::invalid_argument("gsGpuPoissonAssembler: permuted interface");
-            m_ifaces.push_back(it->first().patch);
-            m_ifaces.push_back(it->first().side().index());
-            m_ifaces.push_back(it->second().patch);
-            m_ifaces.push_back(it->second().side().index());
-        }
+        std::vector<int> dsides;
         const gsBoundaryConditions<T>& bc = this->pde().bc();
         for (typename gsBoundaryConditions<T>::const_iterator it = bc.dirichletBegin(); it != bc.dirichletEnd(); ++it) {
-            m_dsides.push_back(it->patch());
-            m_dsides.push_back(it->side().index());
+            dsides.push_back(it->patch());
+            dsides.push_back(it->side().index());
         }
-        gsgpu_problem p;
-        p.dim = d;
-        p.npatches = int(mp.nPatches());
-        p.degree = m_degree.data(); p.nknots = m_nknots.data(); p.knots = m_knots.data();
-        p.gdegree = m_gdegree.data(); p.gnknots = m_gnknots.data(); p.gknots = m_gknots.data();
-        p.coefs = m_coefs.data();
-        p.ninterfaces = int(m_ifaces.size() / 4); p.interfaces = m_ifaces.data();
-        p.ndirichlet = int(m_dsides.size() / 2); p.dirichlet = m_dsides.data();
-        p.kappa_fourier = m_fields.kappaFourier ? 1 : 0;
-        p.kappa_const = m_fields.kappaConst; p.kappa_alpha = m_fields.kappaAlpha; p.kappa_scale = m_fields.kappaScale;
-        p.kappa_nmodes = int(m_fields.amp.size());
-        p.kappa_amp = m_fields.amp.data(); p.kappa_k = m_fields.waves.data(); p.kappa_phase = m_fields.phase.data();
-        p.ufreq = m_fields.ufreq;
-        p.quA = this->m_options.getReal("quA");
-        p.quB = this->m_options.getInt("quB");
-        check(gsgpu_set_problem(m_ctx, &p));
+        m_pack.pack(this->patches(), this->m_bases[0], dsides, m_fields, this->m_options.getReal("quA"),
+                    this->m_options.getInt("quB"));
+        check(gsgpu_set_problem(m_ctx, &m_pack.prob));
         check(gsgpu_refresh(m_ctx));
     }
 
     gsgpu_context* m_ctx = nullptr;
     double m_error = 0.0;
     gsGpuFields m_fields;
-    std::vector<int> m_degree, m_nknots, m_gdegree, m_gnknots, m_ifaces, m_dsides;
-    std::vector<double> m_knots, m_gknots, m_coefs;
+    gsGpuProblemPack<T> m_pack;
 };
 
 /// The assembled device matrix as a gsLinearOperator (gsMatrixOp semantics: x = K input, column

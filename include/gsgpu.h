@@ -124,6 +124,12 @@ int gsgpu_matrix_csr(gsgpu_context* ctx, int* ptr, int* col, double* val);
 int gsgpu_rhs(gsgpu_context* ctx, double* rhs);
 /* gsAssembler::fixedDofs() (gsAssembler.h:538) */
 int gsgpu_fixed_dofs(gsgpu_context* ctx, double* ddof);
+/* the eliminated-dof values (m_ddof, eliminated-dof order of gsgpu_fixed_dofs) computed by the
+ * caller, e.g. gsFeSpace::setup's interpolation or L2 projection (gsExpressions.h:1091-1212,
+ * gsAssembler::computeDirichletDofs gsAssembler.hpp:231-534), used by the following assembles
+ * instead of the built-in interpolation; n = the eliminated-dof count. ddof == NULL restores the
+ * built-in values. Cleared by set_problem. */
+int gsgpu_set_fixed_dofs(gsgpu_context* ctx, const double* ddof, int n);
 /* gsDofMapper::asVector() (gsDofMapper.cpp:80-87) over all patches */
 int gsgpu_dof_map(gsgpu_context* ctx, int* index);
 

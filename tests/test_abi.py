@@ -80,3 +80,20 @@ def test_invalid_problem_is_rejected(lib):
     assert b"dirichlet" in lib.gsgpu_last_error(h)
     assert lib.gsgpu_refresh(h) == _lib.ERR_STATE
     lib.gsgpu_destroy(h)
+
+
+def test_dropin_headers_compile_against_reference():
+    """include/gsGpuPoissonAssembler.h and include/gsGpuExprAssembler.h compile against the G+Smo
+    headers as a user's driver would use them (oracle/ref/adaptor_check.cpp), and the expression
+    recogniser classifies the Poisson, diffusion and source forms (and not a mass matrix) at
+    compile time. Needs the G+Smo source tree; skipped where it is absent."""
+    import shutil
+    import subprocess
+    mk = os.path.join(ROOT, "oracle", "ref")
+    if shutil.which("make") is None or shutil.which("g++") is None:
+        pytest.skip("no make / g++")
+    ref = subprocess.run(["make", "-s", "-C", mk, "print-ref"], capture_output=True, text=True).stdout.strip()
+    if not ref or not os.path.isdir(os.path.join(ref, "src", "gsAssembler")):
+        pytest.skip("G+Smo source tree not available")
+    r = subprocess.run(["make", "-s", "-C", mk, "dropin-syntax"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]

@@ -93,3 +93,36 @@ def test_wcycle_is_symmetric_positive(assembled):
     assert r1 @ z1 > 0 and r2 @ z2 > 0
     # a W-cycle is a different operator from the V-cycle
     assert np.linalg.norm(z1 - A.mg_apply(r1, mg_levels=3)) > 1e-6 * np.linalg.norm(z1)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_fixed_dofs_from_the_caller(precision):
+    """gsgpu_set_fixed_dofs: the Dirichlet lift uses the caller's eliminated-dof values (as the
+    expression assembler's space setup supplies them). The rhs is affine in those values:
+    rhs(2 g) = 2 rhs(g) - rhs(0); the built-in values reproduce the built-in rhs bit for bit."""
+    from gismo_gb300._lib import GsGpuError
+    from gismo_gb300.assembler import GpuPoissonAssembler
+    prob = P.displaced_single_patch(3, (6, 7, 5), (2, 3, 2), 4, 0.04)
+    A = GpuPoissonAssembler(prob, device=0)
+    A.assemble(precision)
+    g = A.fixedDofs()
+    b1 = A.rhs()
+    assert np.abs(g).max() > 0
+    A.set_fixed_dofs(g)
+    A.assemble(precision)
+    assert np.array_equal(A.rhs(), b1) and np.array_equal(A.fixedDofs(), g)
+    A.set_fixed_dofs(2 * g)
+    A.assemble(precision)
+    b2 = A.rhs()
+    assert np.array_equal(A.fixedDofs(), 2 * g)
+    A.set_fixed_dofs(np.zeros_like(g))
+    A.assemble(precision)
+    b0 = A.rhs()
+    assert np.abs(b2 - (2 * b1 - b0)).max() <= 1e-12 * np.abs(b1).max()
+    assert np.abs(b1 - b0).max() > 1e-6 * np.abs(b1).max()
+    A.set_fixed_dofs(None)
+    A.assemble(precision)
+    assert np.array_equal(A.rhs(), b1)
+    with pytest.raises(GsGpuError):
+        A.set_fixed_dofs(g[:-1])
+    A.close()
