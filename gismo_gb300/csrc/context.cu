@@ -32,7 +32,8 @@ void* DeviceArena::alloc(size_t bytes) {
     if (bytes == 0) return nullptr;
     if (budget > 0 && used + bytes > budget) throw BudgetError("device-memory budget exceeded");
     void* p = nullptr;
-    GSGPU_CUDA_TRY(cudaMalloc(&p, bytes));
+    if (stream) GSGPU_CUDA_TRY(cudaMallocAsync(&p, bytes, stream));
+    else GSGPU_CUDA_TRY(cudaMalloc(&p, bytes));
     used += bytes;
     sizes.push_back({p, bytes});
     return p;
@@ -43,12 +44,16 @@ void DeviceArena::release(void* p) {
         if (sizes[i].first == p) {
             used -= sizes[i].second;
             sizes.erase(sizes.begin() + long(i));
-            cudaFree(p);
+            if (stream) cudaFreeAsync(p, stream);
+            else cudaFree(p);
             return;
         }
 }
 void DeviceArena::releaseAll() {
-    for (auto& s : sizes) cudaFree(s.first);
+    for (auto& s : sizes) {
+        if (stream) cudaFreeAsync(s.first, stream);
+        else cudaFree(s.first);
+    }
     sizes.clear();
     used = 0;
 }
@@ -648,6 +653,7 @@ Context Context::reset(Context&& c) {
     n.hasProblem = c.hasProblem;
     n.batch = c.batch;
     n.arena.budget = c.arena.budget;
+    n.arena.stream = n.stream;
     c.stream = nullptr;
     for (int i = 0; i < 8; ++i) c.ev[i] = nullptr;
     return n;
@@ -975,6 +981,14 @@ int gsgpu_create(gsgpu_context** out, int device) {
     if (cudaStreamCreateWithFlags(&c->c.stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete c;
         return GSGPU_ERR_CUDA;
+    }
+    c->c.arena.stream = c->c.stream;
+    // keep freed blocks in the device's pool for the next batch instead of returning them at
+    // every synchronisation (a property of this process's pool, not of the GPU)
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = ~0ULL;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
     }
     *out = c;
     return GSGPU_OK;

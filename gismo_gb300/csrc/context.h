@@ -34,9 +34,13 @@ struct JacobianError : std::runtime_error {
 };
 
 // every device allocation of a context goes through here (accounting against a budget)
+// device buffers of one context, stream-ordered on the context's stream (cudaMallocAsync /
+// cudaFreeAsync from the device's default pool): freeing never synchronises the device, so the
+// contexts of a server's slots do not stall each other between batches
 struct DeviceArena {
     size_t used = 0;
     size_t budget = 0;  // 0 = unlimited
+    cudaStream_t stream = nullptr;  // the owning context's stream (nullptr: plain cudaMalloc / cudaFree)
     std::vector<std::pair<void*, size_t>> sizes;
     void* alloc(size_t bytes);
     void release(void* p);
@@ -187,6 +191,9 @@ struct Context {
     std::vector<SegState> segLast;
     void batchSetup();
     void solveBatch(const gsgpu_solver_opts& o, gsgpu_solve_info& info);
+    static constexpr int kSegChunk = 16;  // segmented CG iterations per captured graph
+    template <typename T>
+    void segChunk(const SegCg<T>& B, cudaGraphExec_t& exec);
     template <typename T>
     void segRun(const SegCg<T>& B, cudaGraphExec_t& exec, int maxit);
     template <typename T>

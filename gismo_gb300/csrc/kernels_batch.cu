@@ -36,8 +36,11 @@ __device__ __forceinline__ double warpRange(const double* __restrict__ part, int
 }
 
 __device__ __forceinline__ bool rowActive(const int* __restrict__ rowSeg, const SegState* __restrict__ st, int row) {
-    return !st[rowSeg[row]].done;
+    const SegState& S = st[rowSeg[row]];
+    return !S.done && !S.pause;
 }
+
+constexpr double kReplaceDrop = 1e-2;  // mixed: replace once the recursive residual dropped by this factor
 
 template <typename T>
 __global__ void __launch_bounds__(kB) k_seg_dinv(int n, const int* __restrict__ diag, const T* __restrict__ val,
@@ -82,6 +85,8 @@ __global__ void __launch_bounds__(kB) k_seg_init_seg(SegCg<T> B, double tol, int
         S.maxit = maxit;
         S.iters = 0;
         S.relres = bb > 0.0 ? 1.0 : 0.0;
+        S.pause = 0;
+        S.last_true = 1.0;
         S.done = (skip || bb == 0.0) ? 1 : 0;
         if (S.done) atomicAdd(B.ndone, 1);
     }
@@ -113,6 +118,10 @@ __global__ void __launch_bounds__(kB) k_seg_alpha(SegCg<T> B) {
     const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (s >= B.nseg || B.st[s].done) return;
+    if (B.st[s].pause) {  // idle until the replacement; the pausing iteration's p update has run
+        if (lane == 0) B.st[s].pause = 2;
+        return;
+    }
     const double pAp = warpRange(B.rc0, B.segRow[s], B.segRow[s + 1], lane);
     if (lane == 0) B.st[s].alpha = B.st[s].rho / pAp;
 }
@@ -122,7 +131,7 @@ template <typename T>
 __global__ void __launch_bounds__(kB) k_seg_update(SegCg<T> B) {
     for (int i = blockIdx.x * kB + threadIdx.x; i < B.n; i += gridDim.x * kB) {
         const SegState& S = B.st[B.rowSeg[i]];
-        if (S.done) continue;
+        if (S.done || S.pause) continue;
         const T alpha = T(S.alpha);
         B.x[i] += alpha * B.p[i];
         const T ri = B.r[i] - alpha * B.t[i];
@@ -138,16 +147,22 @@ template <typename T>
 __global__ void __launch_bounds__(kB) k_seg_scalars(SegCg<T> B) {
     const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (s >= B.nseg || B.st[s].done) return;
+    if (s >= B.nseg || B.st[s].done || B.st[s].pause) return;
     const double rr = warpRange(B.rc0, B.segRow[s], B.segRow[s + 1], lane);
     const double rz = warpRange(B.rc1, B.segRow[s], B.segRow[s + 1], lane);
     if (lane == 0) {
         SegState& S = B.st[s];
         S.iters += 1;
         S.relres = sqrt(rr) / S.bnorm;
-        if (S.relres < S.tol) S.done = 1;
-        else if (S.iters >= S.maxit) S.done = 2;
-        if (S.done) atomicAdd(B.ndone, 1);
+        if (B.outer) {
+            // mixed: the FP32 recursion stops for a true-residual replacement at the tolerance,
+            // once it has gained kReplaceDrop over the last true residual, or at the limit
+            if (S.relres < S.tol || S.relres < kReplaceDrop * S.last_true || S.iters >= S.maxit) S.pause = 1;
+        } else {
+            if (S.relres < S.tol) S.done = 1;
+            else if (S.iters >= S.maxit) S.done = 2;
+            if (S.done) atomicAdd(B.ndone, 1);
+        }
         S.beta = rz / S.rho;
         S.rho = rz;
     }
@@ -157,7 +172,7 @@ template <typename T>
 __global__ void __launch_bounds__(kB) k_seg_pupd(SegCg<T> B) {
     for (int i = blockIdx.x * kB + threadIdx.x; i < B.n; i += gridDim.x * kB) {
         const SegState& S = B.st[B.rowSeg[i]];
-        if (S.done) continue;
+        if (S.done || S.pause > 1) continue;
         B.p[i] = B.z[i] + T(S.beta) * B.p[i];
     }
 }
@@ -166,12 +181,14 @@ __global__ void __launch_bounds__(kB) k_seg_pupd(SegCg<T> B) {
 
 // r = b - (hi + lo) x on the rows of segments not yet converged; rc0 = r .* r
 template <bool REL>
-__global__ void __launch_bounds__(kB) k_ref_resid(SegCg<float> B, SegRefine R) {
+__global__ void __launch_bounds__(kB) k_ref_resid(SegCg<float> B, SegRefine R, int first) {
     constexpr int rpb = kB / kLanes;
     const int lane = threadIdx.x % kLanes;
     for (int base = blockIdx.x * rpb; base < B.n; base += gridDim.x * rpb) {
         const int row = base + threadIdx.x / kLanes;
-        const bool act = row < B.n && rowActive(B.rowSeg, R.st, row);
+        // the first residual on every running segment, later ones on the segments whose FP32
+        // recursion is waiting for its replacement
+        const bool act = row < B.n && rowActive(B.rowSeg, R.st, row) && (first || B.st[B.rowSeg[row]].pause);
         double acc = 0.0;
         if (act)
             dev::rowMac<kLanes, kUnroll, REL>(
@@ -190,7 +207,7 @@ __global__ void __launch_bounds__(kB) k_ref_resid(SegCg<float> B, SegRefine R) {
 __global__ void __launch_bounds__(kB) k_ref_seg(SegCg<float> B, SegRefine R, double tol, int maxref, int first) {
     const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (s >= B.nseg || R.st[s].done) return;
+    if (s >= B.nseg || R.st[s].done || (!first && !B.st[s].pause)) return;
     const double rr = warpRange(B.rc0, B.segRow[s], B.segRow[s + 1], lane);
     if (lane == 0) {
         SegState& S = R.st[s];
@@ -201,7 +218,7 @@ __global__ void __launch_bounds__(kB) k_ref_seg(SegCg<float> B, SegRefine R, dou
             S.tol = tol;
             S.maxit = maxref;
         } else {
-            S.iters += 1;  // refinements done
+            S.iters += 1;  // replacements done
         }
         S.relres = S.bnorm > 0.0 ? sqrt(rr) / S.bnorm : 0.0;
         if (S.relres < tol) S.done = 1;
@@ -215,9 +232,59 @@ __global__ void __launch_bounds__(kB) k_ref_rhs(SegCg<float> B, SegRefine R) {
         if (rowActive(B.rowSeg, R.st, i)) R.r32[i] = float(R.r[i]);
 }
 
-__global__ void __launch_bounds__(kB) k_ref_correct(SegCg<float> B, SegRefine R) {
+// x += d (FP64) and d = 0 on the rows of running segments: the FP32 recursion's progress moves into x
+__global__ void __launch_bounds__(kB) k_ref_absorb(SegCg<float> B, SegRefine R) {
     for (int i = blockIdx.x * kB + threadIdx.x; i < B.n; i += gridDim.x * kB)
-        if (rowActive(B.rowSeg, R.st, i)) R.x[i] += double(R.d32[i]);
+        if (rowActive(B.rowSeg, R.st, i)) {
+            R.x[i] += double(B.x[i]);
+            B.x[i] = 0.f;
+        }
+}
+
+// a paused segment's recursion continues from the true residual: r32 = fl32(r), z = D^-1 r32,
+// rc1 = r32 . z; the search direction is kept unless the true residual is more than 4x the
+// recursive one (then p = z)
+__global__ void __launch_bounds__(kB) k_ref_replace(SegCg<float> B, SegRefine R) {
+    for (int i = blockIdx.x * kB + threadIdx.x; i < B.n; i += gridDim.x * kB) {
+        const int sg = B.rowSeg[i];
+        if (R.st[sg].done || B.st[sg].done || !B.st[sg].pause) continue;
+        const float ri = float(R.r[i]);
+        B.r[i] = ri;
+        const float zi = B.dinv[i] * ri;
+        B.z[i] = zi;
+        if (R.st[sg].relres > 4.0 * B.st[sg].relres) B.p[i] = zi;
+        B.rc1[i] = double(ri) * double(zi);
+    }
+}
+
+// per segment: a segment the true residual has finished leaves the recursion; a paused one
+// resumes with rho of the replaced residual (or ends at its iteration limit)
+__global__ void __launch_bounds__(kB) k_ref_replace_seg(SegCg<float> B, SegRefine R) {
+    const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (s >= B.nseg || B.st[s].done) return;
+    if (R.st[s].done) {
+        if (lane == 0) {
+            B.st[s].done = R.st[s].done;
+            atomicAdd(B.ndone, 1);
+        }
+        return;
+    }
+    if (!B.st[s].pause) return;
+    const double rz = warpRange(B.rc1, B.segRow[s], B.segRow[s + 1], lane);
+    if (lane == 0) {
+        SegState& S = B.st[s];
+        if (S.iters >= S.maxit) {
+            S.done = 2;
+            atomicAdd(B.ndone, 1);
+            R.st[s].done = 2;
+            atomicAdd(R.ndone, 1);
+            return;
+        }
+        S.rho = rz;
+        S.last_true = R.st[s].relres;
+        S.pause = 0;
+    }
 }
 
 __global__ void __launch_bounds__(kB) k_ref_count(SegCg<float> B, SegRefine R) {
@@ -259,8 +326,8 @@ void refineResidual(const SegCg<float>& B, const SegRefine& R, double tol, int m
         GSGPU_CUDA_TRY(cudaMemsetAsync(R.ndone, 0, sizeof(int), s));
     }
     const int gs = gridFor(B.n, kB / kLanes);
-    if (B.coff) k_ref_resid<true><<<gs, kB, 0, s>>>(B, R);
-    else k_ref_resid<false><<<gs, kB, 0, s>>>(B, R);
+    if (B.coff) k_ref_resid<true><<<gs, kB, 0, s>>>(B, R, first);
+    else k_ref_resid<false><<<gs, kB, 0, s>>>(B, R, first);
     k_ref_seg<<<segGrid(B.nseg), kB, 0, s>>>(B, R, tol, maxref, first);
 }
 
@@ -268,8 +335,11 @@ void refineRhs(const SegCg<float>& B, const SegRefine& R, cudaStream_t s) {
     k_ref_rhs<<<gridFor(B.n, kB), kB, 0, s>>>(B, R);
 }
 
-void refineCorrect(const SegCg<float>& B, const SegRefine& R, cudaStream_t s) {
-    k_ref_correct<<<gridFor(B.n, kB), kB, 0, s>>>(B, R);
+void refineReplace(const SegCg<float>& B, const SegRefine& R, double tol, int maxref, cudaStream_t s) {
+    k_ref_absorb<<<gridFor(B.n, kB), kB, 0, s>>>(B, R);
+    refineResidual(B, R, tol, maxref, 0, s);
+    k_ref_replace<<<gridFor(B.n, kB), kB, 0, s>>>(B, R);
+    k_ref_replace_seg<<<segGrid(B.nseg), kB, 0, s>>>(B, R);
 }
 
 void refineCount(const SegCg<float>& B, const SegRefine& R, cudaStream_t s) {

@@ -13,6 +13,10 @@ namespace gsgpu {
 struct SegState {
     double rho, alpha, beta, bnorm, relres, tol;
     int iters, maxit, done, total;  // done: 0 running, 1 converged, 2 reached maxit; total: iterations summed
+    // mixed recursion: waiting for a true-residual replacement (1: set in this iteration, whose
+    // direction update still runs; 2: idle), and the true relative residual of the last replacement
+    int pause;
+    double last_true;
 };
 
 // The batch matrix is one CSR matrix (block diagonal, rows of segment s in [segRow[s], segRow[s+1]))
@@ -43,9 +47,8 @@ struct SegRefine {
     const double* b = nullptr;
     double* x = nullptr;         // FP64 solution
     double* r = nullptr;         // FP64 residual
-    float* r32 = nullptr;        // inner right-hand side
-    const float* d32 = nullptr;  // inner solution (correction)
-    SegState* st = nullptr;      // outer state: relres of b - A x, refinements in iters
+    float* r32 = nullptr;        // FP32 copy of the first residual (the recursion's right-hand side)
+    SegState* st = nullptr;      // outer state: relres of b - A x, residual replacements in iters
     int* ndone = nullptr;
 };
 
@@ -57,12 +60,16 @@ template <typename T>
 void segInit(const SegCg<T>& B, double tol, int maxit, cudaStream_t s);
 template <typename T>
 void segIteration(const SegCg<T>& B, cudaStream_t s);
-// refinement: x = 0 (first) then r = b - (hi + lo) x and the outer stopping test per segment
+// mixed precision: FP32 segmented CG on hi (x = the correction d) with FP64-accurate residual
+// replacement. refineResidual: x = 0 (first) then r = b - (hi + lo) x and the stopping test per
+// segment on that true residual
 void refineResidual(const SegCg<float>& B, const SegRefine& R, double tol, int maxref, int first, cudaStream_t s);
-// r32 = r (active segments), before an inner solve; x += d32 after it
+// r32 = r (running segments): the recursion's start
 void refineRhs(const SegCg<float>& B, const SegRefine& R, cudaStream_t s);
-void refineCorrect(const SegCg<float>& B, const SegRefine& R, cudaStream_t s);
-// per segment: add the inner iterations of the last inner solve to the outer state's total
+// x += d, d = 0, the true residual and its test, then the recursion continues from it with its
+// search direction kept (finished segments leave it)
+void refineReplace(const SegCg<float>& B, const SegRefine& R, double tol, int maxref, cudaStream_t s);
+// per segment: the recursion's iteration count into the outer state's total
 void refineCount(const SegCg<float>& B, const SegRefine& R, cudaStream_t s);
 }  // namespace launch
 }  // namespace gsgpu

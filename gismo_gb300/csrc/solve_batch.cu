@@ -48,25 +48,30 @@ void Context::batchSetup() {
     allocN(arena, dSegDone, 2);  // [inner done, outer done]
 }
 
-// iterations in chunks of 16 under one captured graph (per precision, once per context) until
-// every segment is done
+// one chunk of 16 iterations as a captured graph (per precision, once per context)
 template <typename T>
-void Context::segRun(const SegCg<T>& B, cudaGraphExec_t& exec, int maxit) {
+void Context::segChunk(const SegCg<T>& B, cudaGraphExec_t& exec) {
     cudaStream_t s = stream;
-    const int chunk = 16;
     if (!exec) {
         cudaGraph_t g;
         GSGPU_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < chunk; ++k) launch::segIteration<T>(B, s);
+        for (int k = 0; k < kSegChunk; ++k) launch::segIteration<T>(B, s);
         GSGPU_CUDA_TRY(cudaStreamEndCapture(s, &g));
         GSGPU_CUDA_TRY(cudaGraphInstantiate(&exec, g, 0));
         cudaGraphDestroy(g);
     }
+    GSGPU_CUDA_TRY(cudaGraphLaunch(exec, s));
+}
+
+// chunks until every segment is done
+template <typename T>
+void Context::segRun(const SegCg<T>& B, cudaGraphExec_t& exec, int maxit) {
+    cudaStream_t s = stream;
     int ndone = 0;
     GSGPU_CUDA_TRY(cudaMemcpyAsync(&ndone, B.ndone, sizeof(int), cudaMemcpyDeviceToHost, s));
     GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
-    for (int it = 0; it < maxit + chunk && ndone < B.nseg; it += chunk) {
-        GSGPU_CUDA_TRY(cudaGraphLaunch(exec, s));
+    for (int it = 0; it < maxit + kSegChunk && ndone < B.nseg; it += kSegChunk) {
+        segChunk<T>(B, exec);
         GSGPU_CUDA_TRY(cudaMemcpyAsync(&ndone, B.ndone, sizeof(int), cudaMemcpyDeviceToHost, s));
         GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
     }
@@ -120,7 +125,11 @@ void Context::solveBatch(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
         GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
         for (SegState& S : segLast) S.total = S.iters;
     } else {
-        // inner FP32 system A_hi d = r32: rhs in the (otherwise unused) x-high buffer, d in dDx32
+        // FP32 segmented CG on hi for the correction d (dDx32) from r32 = fl32(b), each
+        // segment's recursion running on; every chunk, x += d, the true residual b - (hi + lo) x
+        // decides per segment, and the recursion continues from it with its search direction
+        // kept (residual replacement, as in the single-problem mixed CG), instead of restarting
+        // CG for every refinement
         SegCg<float> B;
         common(B);
         B.val = dValHi;
@@ -139,25 +148,22 @@ void Context::solveBatch(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
         R.x = dX;
         R.r = dR;
         R.r32 = dXhi;
-        R.d32 = dDx32;
         R.st = dSegOuter;
         R.ndone = dSegDone + 1;
-        const double innerTol = o.inner_tol > 0 ? o.inner_tol : 1e-5;
-        const int maxref = 30;
+        const int maxref = maxit + 2;  // chunks: each advances every running segment by one iteration at least
         launch::segDinv<float>(B, dDiag, s);
         launch::refineResidual(B, R, tol, maxref, 1, s);
-        for (int ref = 0; ref <= maxref; ++ref) {
+        launch::refineRhs(B, R, s);
+        launch::segInit<float>(B, tol, maxit, s);
+        for (int ref = 0; ref < maxref; ++ref) {
             int ndone = 0;
             GSGPU_CUDA_TRY(cudaMemcpyAsync(&ndone, R.ndone, sizeof(int), cudaMemcpyDeviceToHost, s));
             GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
             if (ndone >= nseg) break;
-            launch::refineRhs(B, R, s);
-            launch::segInit<float>(B, innerTol, maxit, s);
-            segRun<float>(B, gexecSeg[1], maxit);
-            launch::refineCount(B, R, s);
-            launch::refineCorrect(B, R, s);
-            launch::refineResidual(B, R, tol, maxref, 0, s);
+            segChunk<float>(B, gexecSeg[1]);
+            launch::refineReplace(B, R, tol, maxref, s);
         }
+        launch::refineCount(B, R, s);
         GSGPU_CUDA_TRY(cudaMemcpyAsync(segLast.data(), dSegOuter, sizeof(SegState) * nseg, cudaMemcpyDeviceToHost, s));
         GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
     }

@@ -80,7 +80,7 @@ typedef struct {
     int mg_levels;         /* "Levels" of gsGridHierarchy::buildByCoarsening */
     int mg_npre, mg_npost; /* "NumPreSmooth", "NumPostSmooth" */
     double mg_damping;     /* damping of the Jacobi smoother */
-    double inner_tol;      /* mixed precision: FP32 inner reduction per refinement step */
+    double inner_tol;      /* unused (the mixed solves replace residuals instead of restarting) */
     int mg_cycles;         /* "NumCycles": 1 = V-cycle, 2 = W-cycle (0: 1) */
     double mg_cgc_damping; /* "CoarseGridCorrectionDamping" (0: 1) */
 } gsgpu_solver_opts;
