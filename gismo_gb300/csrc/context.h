@@ -172,6 +172,8 @@ struct Context {
     int mgPrecision = -1, mgCoarseIters = 0;
     double mgCoarseTol = 0.0;
     double *dMgVec0 = nullptr, *dMgPart = nullptr, *dRold = nullptr;  // level 0 FP64: dinv b x r z
+    float* dFieldC32 = nullptr;  // FP32 copy of the df32 coefficient fields (coarse operators of the FP32 cycle)
+    float* dMgPsplit = nullptr;  // outer MG-CG direction as double-float (hi, lo), mixed form
     float* dMgVec0f = nullptr;                                       // level 0 FP32: dinv b x r z
     CgState *dMgCoarseSt = nullptr, *dMgSt = nullptr;
     cudaGraphExec_t gexecMg = nullptr;

@@ -48,6 +48,8 @@ void loadContract(const DevPatch* P, const BlkEnt* tab, long long nblk, const Ti
 void gatherCsrDF(long long nnz, const uint32_t* src, const df32* band, const uint32_t* ovf_ptr, const uint32_t* ovf_idx,
                  float* hi, float* lo, cudaStream_t s);
 void toDF(long long n, const double* in, df32* out, cudaStream_t s);
+// FP32 rounding of double-float values
+void dfToFloat(long long n, const df32* in, float* out, cudaStream_t s);
 template <typename T>
 void gatherCsr(long long nnz, const uint32_t* src, const T* band, const uint32_t* ovf_ptr, const uint32_t* ovf_idx,
                T* val, cudaStream_t s);

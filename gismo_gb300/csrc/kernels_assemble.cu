@@ -279,6 +279,12 @@ __global__ void __launch_bounds__(kBlock) k_to_df(long long n, const double* __r
     if (i < n) out[i] = df32(in[i]);
 }
 
+// the FP32 rounding of double-float values (hi + lo rounded to nearest)
+__global__ void __launch_bounds__(kBlock) k_df_to_f32(long long n, const df32* __restrict__ in, float* __restrict__ out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = __fadd_rn(in[i].hi, in[i].lo);
+}
+
 template <typename TB>
 __global__ void __launch_bounds__(kBlock) k_rhs(int n, const double* __restrict__ lvec, const uint32_t* __restrict__ lptr,
                                                 const uint32_t* __restrict__ lidx, const TB* __restrict__ band,
@@ -316,6 +322,7 @@ void pairFactors(const PfJob* jobs, const BlkEnt* tab, long long nblk, const dou
 }
 template void pairFactors<double>(const PfJob*, const BlkEnt*, long long, const double*, double*, cudaStream_t);
 template void pairFactors<df32>(const PfJob*, const BlkEnt*, long long, const double*, df32*, cudaStream_t);
+template void pairFactors<float>(const PfJob*, const BlkEnt*, long long, const double*, float*, cudaStream_t);
 
 template <typename R>
 void geoStage1(const DevPatch* P, const BlkEnt* tab, long long nblk, const R* coefs, const R* gtab, const int* ibuf,
@@ -416,6 +423,10 @@ void toDF(long long n, const double* in, df32* out, cudaStream_t s) {
     if (n > 0) k_to_df<<<grid1(n), kBlock, 0, s>>>(n, in, out);
 }
 
+void dfToFloat(long long n, const df32* in, float* out, cudaStream_t s) {
+    if (n > 0) k_df_to_f32<<<grid1(n), kBlock, 0, s>>>(n, in, out);
+}
+
 template <typename T, int KIND>
 void contract(const DevPatch* P, const BlkEnt* tab, long long nblk, const T* in, T* out, const int* ibuf, const T* pf,
               cudaStream_t s) {
@@ -428,6 +439,12 @@ INST_CONTRACT(double, 32)
 INST_CONTRACT(double, 33)
 INST_CONTRACT(double, 21)
 INST_CONTRACT(double, 22)
+// FP32: the coarse operators of the FP32 multigrid cycle
+INST_CONTRACT(float, 31)
+INST_CONTRACT(float, 32)
+INST_CONTRACT(float, 33)
+INST_CONTRACT(float, 21)
+INST_CONTRACT(float, 22)
 
 template <int KIND, typename Tin>
 void loadContract(const DevPatch* P, const BlkEnt* tab, long long nblk, const Tin* in, double* out,

@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cstdint>
 
+#include "df32.cuh"
 #include "kernels_mg.h"
 #include "spmv_row.cuh"
 
@@ -301,30 +302,60 @@ __global__ void __launch_bounds__(kB) k_mg_beta(int np, const double* __restrict
 
 template <typename Tz>
 __global__ void __launch_bounds__(kB) k_mg_pupd(int n, double* __restrict__ p, const Tz* __restrict__ z,
+                                                float* __restrict__ phi, float* __restrict__ plo,
                                                 const CgState* __restrict__ st) {
     if (stopped(st, nullptr)) return;
     const double beta = st->beta;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        p[i] = double(z[i]) + beta * p[i];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double pi = double(z[i]) + beta * p[i];
+        p[i] = pi;
+        if (phi) {
+            const df32 v(pi);
+            phi[i] = v.hi;
+            plo[i] = v.lo;
+        }
+    }
 }
 
 // t = A p and partial sums of p.t; A = val or hi + lo
+// (the hi + lo form multiplies double-floats on the FP32 pipe with compensated accumulation, as
+// the residual replacement of the mixed CG does: FP64 products would be FP64-pipe bound on GB300)
 template <int LPR, bool REL, bool SPLIT>
 __global__ void __launch_bounds__(kB) k_mg_spmv(int n, const int* __restrict__ ptr, const int* __restrict__ col,
                                                 const int16_t* __restrict__ coff, const double* __restrict__ val,
                                                 const float* __restrict__ hi, const float* __restrict__ lo,
+                                                const float* __restrict__ phi, const float* __restrict__ plo,
                                                 const double* __restrict__ p, double* __restrict__ t,
                                                 double* __restrict__ part, const CgState* __restrict__ st) {
     if (stopped(st, nullptr)) return;
     double contrib = 0.0;
-    auto v = [&](int k) -> double {
-        if (SPLIT) return double(hi[k]) + double(lo[k]);
-        return val[k];
-    };
-    rowLoop<double, LPR, REL>(n, ptr, col, coff, v, p, [&](int row, double ax) {
-        t[row] = ax;
-        contrib += ax * p[row];
-    });
+    if constexpr (SPLIT) {
+        const int rowsPerBlock = kB / LPR;
+        const int lane = threadIdx.x % LPR;
+        for (int base = blockIdx.x * rowsPerBlock; base < n; base += gridDim.x * rowsPerBlock) {
+            const int row = base + threadIdx.x / LPR;
+            Dot2 acc;
+            if (row < n)
+                dev::rowMac<LPR, kUnroll, REL>(
+                    row, ptr[row], ptr[row + 1], lane, col, coff, [&](int k) { return df32(hi[k], lo[k]); },
+                    [&](int c) { return df32(phi[c], plo[c]); }, [&](df32 a, df32 x) { acc.mac(a, x); });
+            df32 y = acc.result();
+            for (int o = LPR / 2; o > 0; o >>= 1) {
+                const df32 oth(__shfl_xor_sync(0xffffffffu, y.hi, o), __shfl_xor_sync(0xffffffffu, y.lo, o));
+                y = y + oth;
+            }
+            if (row < n && lane == 0) {
+                const double ax = y.toDouble();
+                t[row] = ax;
+                contrib += ax * p[row];
+            }
+        }
+    } else {
+        rowLoop<double, LPR, REL>(n, ptr, col, coff, [&](int k) { return val[k]; }, p, [&](int row, double ax) {
+            t[row] = ax;
+            contrib += ax * p[row];
+        });
+    }
     blockSum(contrib, part);
 }
 
@@ -481,7 +512,7 @@ void mgPcgPrecond(const MgOuter& O, const std::vector<MgLevelDev<T>>& lv, const 
     vcycle<T>(lv, 0, prm, O.st, s);
     k_mg_dots<T><<<nb, kB, 0, s>>>(O.n, O.r, O.rold, lv[0].x, O.part0, O.part1, O.st);
     k_mg_beta<<<1, kB, 0, s>>>(nb, O.part0, O.part1, O.st);
-    k_mg_pupd<T><<<nb, kB, 0, s>>>(O.n, O.p, lv[0].x, O.st);
+    k_mg_pupd<T><<<nb, kB, 0, s>>>(O.n, O.p, lv[0].x, O.phi, O.plo, O.st);
 }
 
 void mgPcgStep(const MgOuter& O, cudaStream_t s) {
@@ -489,20 +520,13 @@ void mgPcgStep(const MgOuter& O, cudaStream_t s) {
     const int nrb = rowBlocks(O.n, O.lpr);
     const bool split = O.val == nullptr;
     const bool rel = O.coff != nullptr;
-#define MG_OUTER(LPR)                                                                                       \
-    do {                                                                                                    \
-        if (split && rel)                                                                                   \
-            k_mg_spmv<LPR, true, true><<<nrb, kB, 0, s>>>(O.n, O.ptr, O.col, O.coff, O.val, O.hi, O.lo, O.p, \
-                                                          O.t, O.part2, O.st);                              \
-        else if (split)                                                                                     \
-            k_mg_spmv<LPR, false, true><<<nrb, kB, 0, s>>>(O.n, O.ptr, O.col, O.coff, O.val, O.hi, O.lo,     \
-                                                           O.p, O.t, O.part2, O.st);                        \
-        else if (rel)                                                                                       \
-            k_mg_spmv<LPR, true, false><<<nrb, kB, 0, s>>>(O.n, O.ptr, O.col, O.coff, O.val, O.hi, O.lo,     \
-                                                           O.p, O.t, O.part2, O.st);                        \
-        else                                                                                                \
-            k_mg_spmv<LPR, false, false><<<nrb, kB, 0, s>>>(O.n, O.ptr, O.col, O.coff, O.val, O.hi, O.lo,    \
-                                                            O.p, O.t, O.part2, O.st);                       \
+#define MG_OUTER_ARGS O.n, O.ptr, O.col, O.coff, O.val, O.hi, O.lo, O.phi, O.plo, O.p, O.t, O.part2, O.st
+#define MG_OUTER(LPR)                                                                        \
+    do {                                                                                     \
+        if (split && rel) k_mg_spmv<LPR, true, true><<<nrb, kB, 0, s>>>(MG_OUTER_ARGS);      \
+        else if (split) k_mg_spmv<LPR, false, true><<<nrb, kB, 0, s>>>(MG_OUTER_ARGS);       \
+        else if (rel) k_mg_spmv<LPR, true, false><<<nrb, kB, 0, s>>>(MG_OUTER_ARGS);         \
+        else k_mg_spmv<LPR, false, false><<<nrb, kB, 0, s>>>(MG_OUTER_ARGS);                 \
     } while (0)
     switch (O.lpr) {
         case 4: MG_OUTER(4); break;
@@ -511,6 +535,7 @@ void mgPcgStep(const MgOuter& O, cudaStream_t s) {
         default: MG_OUTER(32); break;
     }
 #undef MG_OUTER
+#undef MG_OUTER_ARGS
     k_mg_update<<<nb, kB, 0, s>>>(O.n, nrb, O.part2, O.x, O.r, O.rold, O.p, O.t, O.part0, O.st);
     k_mg_check<<<1, kB, 0, s>>>(nb, O.part0, O.st);
 }

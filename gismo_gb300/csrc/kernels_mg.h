@@ -51,6 +51,7 @@ struct MgOuter {
     const float* lo = nullptr;
     const double* b = nullptr;
     double *x = nullptr, *r = nullptr, *rold = nullptr, *p = nullptr, *t = nullptr;
+    float *phi = nullptr, *plo = nullptr;  // hi + lo operator: p as double-float, for the SpMV on the FP32 pipe
     double *part0 = nullptr, *part1 = nullptr, *part2 = nullptr;
     CgState* st = nullptr;
 };

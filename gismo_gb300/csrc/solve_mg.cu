@@ -142,9 +142,10 @@ void Context::mgAssemble(bool mixed) {
     if (mgSerial == assembleSerial && mgPrecision == prec) return;
     cudaStream_t s = stream;
     const df32* cDf = reinterpret_cast<const df32*>(dFieldC);
-    df32* sDf = reinterpret_cast<df32*>(dS);
-    df32* uDf = reinterpret_cast<df32*>(dU);
-    df32* bandDf = reinterpret_cast<df32*>(dBand);
+    if (mixed) {
+        if (!dFieldC32) allocN(arena, dFieldC32, L.fields);
+        launch::dfToFloat(L.fields, cDf, dFieldC32, s);
+    }
     for (MgLevelBuf& M : mgl) {
         const Layout& LL = M.plan.L;
         const Pattern& P = M.plan.pat;
@@ -168,26 +169,23 @@ void Context::mgAssemble(bool mixed) {
                 upload(arena, M.dRval, M.plan.Rval, s);
             }
         } else {
-            df32* pf = reinterpret_cast<df32*>(M.dPf);
-            launch::pairFactors<df32>(M.dPfJobs, M.tabPf.d, (long long)M.tabPf.h.size(), M.dTab, pf, s);
+            // the coarse operators only serve the FP32 cycle: FP32 contractions of the FP32-rounded
+            // fields (the outer CG keeps the double-float fine operator)
+            float* pf = reinterpret_cast<float*>(M.dPf);
+            float* s32 = reinterpret_cast<float*>(dS);
+            float* u32 = reinterpret_cast<float*>(dU);
+            float* band32 = reinterpret_cast<float*>(dBand);
+            launch::pairFactors<float>(M.dPfJobs, M.tabPf.d, (long long)M.tabPf.h.size(), M.dTab, pf, s);
             if (pd.dim == 3) {
-                launch::contractDF<31>(M.dPatches, M.tabSt[0].d, nb(0), cDf, sDf, M.dIbuf, pf, s);
-                launch::contractDF<32>(M.dPatches, M.tabSt[1].d, nb(1), sDf, uDf, M.dIbuf, pf, s);
-                launch::contractDF<33>(M.dPatches, M.tabSt[2].d, nb(2), uDf, bandDf, M.dIbuf, pf, s);
+                launch::contract<float, 31>(M.dPatches, M.tabSt[0].d, nb(0), dFieldC32, s32, M.dIbuf, pf, s);
+                launch::contract<float, 32>(M.dPatches, M.tabSt[1].d, nb(1), s32, u32, M.dIbuf, pf, s);
+                launch::contract<float, 33>(M.dPatches, M.tabSt[2].d, nb(2), u32, band32, M.dIbuf, pf, s);
             } else {
-                launch::contractDF<21>(M.dPatches, M.tabSt[0].d, nb(0), cDf, sDf, M.dIbuf, pf, s);
-                launch::contractDF<22>(M.dPatches, M.tabSt[1].d, nb(1), sDf, bandDf, M.dIbuf, pf, s);
+                launch::contract<float, 21>(M.dPatches, M.tabSt[0].d, nb(0), dFieldC32, s32, M.dIbuf, pf, s);
+                launch::contract<float, 22>(M.dPatches, M.tabSt[1].d, nb(1), s32, band32, M.dIbuf, pf, s);
             }
             if (!M.dVal32) allocN(arena, M.dVal32, nnz);
-            // the low halves are not used by the FP32 V-cycle: they go to the free stage-1 buffer
-            float* loScratch = reinterpret_cast<float*>(dS);
-            float* loOwn = nullptr;
-            if (2 * L.s < nnz) allocN(arena, loOwn, nnz), loScratch = loOwn;
-            launch::gatherCsrDF(nnz, M.dSrc, bandDf, M.dOvfPtr, M.dOvfIdx, M.dVal32, loScratch, s);
-            if (loOwn) {
-                GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
-                arena.release(loOwn);
-            }
+            launch::gatherCsr<float>(nnz, M.dSrc, band32, M.dOvfPtr, M.dOvfIdx, M.dVal32, s);
             if (!M.dPval32) {
                 upload(arena, M.dPval32, toFloat(M.plan.Pval), s);
                 upload(arena, M.dRval32, toFloat(M.plan.Rval), s);
@@ -328,6 +326,9 @@ void Context::mgRun(const gsgpu_solver_opts& o, gsgpu_solve_info& info, bool mix
     if (mixed) {
         O.hi = dValHi;
         O.lo = dValLo;
+        if (!dMgPsplit) allocN(arena, dMgPsplit, 2LL * n);
+        O.phi = dMgPsplit;
+        O.plo = dMgPsplit + n;
     } else {
         O.val = dVal;
     }
