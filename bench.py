@@ -363,7 +363,9 @@ def main():
         # replacement kernels
         launches_per_step = 20 + 3 + (16 * 5 + 5) * chunks
     else:
-        launches_per_step = 13 + 3 + 5 * 16 * chunks
+        # assemble 13; solve: dinv 1, init 2, per graph chunk 16 x 3 iteration kernels (alpha and beta
+        # are formed by the last block of the SpMV and of the update)
+        launches_per_step = 13 + 3 + 3 * 16 * chunks
     amean = np.mean(np.array(asm_ms), axis=0)
     line = {"metric": METRIC, "value": value, "unit": "DoF/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",

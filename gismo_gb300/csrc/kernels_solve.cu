@@ -99,6 +99,34 @@ __device__ __forceinline__ double reducePartials(const double* part, int n) {
     return s;
 }
 
+// the same sum for the block that finishes last (partials written by other blocks of this
+// launch: read past L1)
+__device__ __forceinline__ double reducePartialsLast(const double* part, int n) {
+    __shared__ double ws[kB / 32];
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) v += __ldcg(part + i);
+    v = warpSum(v);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0.0;
+    for (int w = 0; w < kB / 32; ++w) s += ws[w];
+    __syncthreads();
+    return s;
+}
+
+// true in every thread of the block that is the last of the grid to store its partial sums (each
+// block fences its stores before counting itself; no block waits for another)
+__device__ __forceinline__ bool lastBlock(unsigned* arrive) {
+    __shared__ bool last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(arrive, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    return last;
+}
+
 // the block's copy of the box-row offset table (BOX kernels)
 template <bool BOX>
 __device__ __forceinline__ void stageBox(int* sbox, const int* __restrict__ off, int nbox) {
@@ -115,7 +143,7 @@ __global__ void __launch_bounds__(kB) k_spmv_dot(int n, const int* __restrict__ 
                                                  const int* __restrict__ boxOff, int nbox,
                                                  const double* __restrict__ val, const double* __restrict__ p,
                                                  double* __restrict__ t, double* __restrict__ part,
-                                                 const CgState* __restrict__ st) {
+                                                 CgState* __restrict__ st) {
     if (st->done) return;
     __shared__ int sbox[BOX ? launch::kMaxBox : 1];
     stageBox<BOX>(sbox, boxOff, nbox);
@@ -140,20 +168,23 @@ __global__ void __launch_bounds__(kB) k_spmv_dot(int n, const int* __restrict__ 
         }
     }
     leaderSumStore<kB / LPR>(contrib, lane == 0, threadIdx.x / LPR, part);
+    // the block that finishes last forms alpha = rho / p.Ap from the partials (fixed order)
+    if (lastBlock(&st->arrive)) {
+        const double pAp = reducePartialsLast(part, gridDim.x);
+        if (threadIdx.x == 0) {
+            st->alpha = st->rho / pAp;
+            st->arrive = 0;
+        }
+    }
 }
 
-__global__ void __launch_bounds__(kB) k_alpha(int nparts, const double* __restrict__ part, CgState* __restrict__ st) {
-    if (st->done) return;
-    const double pAp = reducePartials(part, nparts);
-    if (threadIdx.x == 0) st->alpha = st->rho / pAp;
-}
-
-// x += alpha p; r -= alpha t; z = dinv r; partial sums of r.r and r.z
+// x += alpha p; r -= alpha t; z = dinv r; partial sums of r.r and r.z; the block that finishes
+// last takes the stopping test (gsConjugateGradient::step) and forms beta = (r.z) / rho
 __global__ void __launch_bounds__(kB) k_update(int n, double* __restrict__ x, double* __restrict__ r,
                                                double* __restrict__ z, const double* __restrict__ p,
                                                const double* __restrict__ t, const double* __restrict__ dinv,
                                                double* __restrict__ prr, double* __restrict__ prz,
-                                               const CgState* __restrict__ st) {
+                                               CgState* __restrict__ st) {
     if (st->done) return;
     const double alpha = st->alpha;
     double rr = 0.0, rz = 0.0;
@@ -167,14 +198,12 @@ __global__ void __launch_bounds__(kB) k_update(int n, double* __restrict__ x, do
         rz += ri * zi;
     }
     blockSumStore2(rr, rz, prr, prz);
-}
-
-__global__ void __launch_bounds__(kB) k_beta(int nparts, const double* __restrict__ prr, const double* __restrict__ prz,
-                                             CgState* __restrict__ st) {
-    if (st->done) return;
-    const double rr = reducePartials(prr, nparts);
-    const double rz = reducePartials(prz, nparts);
+    if (!lastBlock(&st->arrive)) return;
+    const double rrs = reducePartialsLast(prr, gridDim.x);
+    const double rzs = reducePartialsLast(prz, gridDim.x);
     if (threadIdx.x == 0) {
+        st->arrive = 0;
+        const double rr = rrs, rz = rzs;
         st->iters += 1;
         st->relres = sqrt(rr) / st->bnorm;
         if (st->relres < st->tol) {
@@ -234,6 +263,7 @@ __global__ void __launch_bounds__(kB) k_init_reduce(int nparts, const double* __
         st->restart = 0;
         st->last_true = 1.0;
         st->delta = delta;
+        st->arrive = 0;
         // zero rhs: x = 0 is the solution; x0 = 0 gives ||r||/||b|| = 1 >= tol otherwise
         st->done = (bb == 0.0 || 1.0 < tol) ? 1 : (maxit <= 0 ? 2 : 0);
     }
@@ -547,10 +577,7 @@ void cgSpmv(const CgBuffers& B, cudaStream_t s) {
 
 void cgRest(const CgBuffers& B, cudaStream_t s) {
     const int np = cgPartials(B.n);
-    const int nb = spmvPartials(B.n, B.lanes_per_row);
-    k_alpha<<<1, kB, 0, s>>>(nb, B.part2, B.st);
     k_update<<<np, kB, 0, s>>>(B.n, B.x, B.r, B.z, B.p, B.t, B.dinv, B.part0, B.part1, B.st);
-    k_beta<<<1, kB, 0, s>>>(np, B.part0, B.part1, B.st);
     k_pupd<<<np, kB, 0, s>>>(B.n, B.p, B.z, B.st);
 }
 

@@ -19,6 +19,7 @@ struct CgState {
     int replacements;  // mixed: number of true-residual evaluations
     int replaced;      // mixed: a replacement ran in this chunk (restart the FP32 recursion)
     int restart;       // mixed: the replacement moved the residual a lot; restart p = z
+    unsigned arrive;   // blocks of the running kernel that have stored their partial sums
 };
 
 struct CgBuffers {
