@@ -34,7 +34,7 @@ class Problem(C.Structure):
         ("kappa_fourier", C.c_int), ("kappa_const", C.c_double), ("kappa_alpha", C.c_double),
         ("kappa_scale", C.c_double), ("kappa_nmodes", C.c_int), ("kappa_amp", C.POINTER(C.c_double)),
         ("kappa_k", C.POINTER(C.c_int)), ("kappa_phase", C.POINTER(C.c_double)),
-        ("ufreq", C.c_int), ("quA", C.c_double), ("quB", C.c_int),
+        ("ufreq", C.c_int), ("quA", C.c_double), ("quB", C.c_int), ("dirichlet_strategy", C.c_int),
     ]
 
 

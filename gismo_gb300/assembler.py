@@ -63,6 +63,7 @@ class PackedProblem:
         s.kappa_amp = _ptr(a["amp"], C.c_double); s.kappa_k = _ptr(a["kk"], C.c_int)
         s.kappa_phase = _ptr(a["phase"], C.c_double)
         s.ufreq = prob.ufreq; s.quA = prob.quA; s.quB = prob.quB
+        s.dirichlet_strategy = 1 if getattr(prob, "dirichlet_l2", False) else 0
         self.struct = s
 
 

@@ -1157,6 +1157,12 @@ int gsgpu_rhs(gsgpu_context* ctx, double* rhs) {
 int gsgpu_fixed_dofs(gsgpu_context* ctx, double* ddof) {
     return guarded(ctx, [&] {
         auto& c = ctx->c;
+        if (c.device < 0 && c.refreshed) {  // host-only context: the values of the problem's strategy
+            std::vector<double> v;
+            gsgpu::dirichletValues(c.pd, c.map, v);
+            std::copy(v.begin(), v.end(), ddof);
+            return;
+        }
         if (!c.assembled) throw gsgpu::StateError("fixedDofs() before assemble()");
         std::copy(c.ddof.begin(), c.ddof.end(), ddof);
     });

@@ -831,7 +831,238 @@ static std::vector<double> sideValues(const ProblemDesc& pd, size_t si, bool par
     return f;
 }
 
+// geometry map of patch P at the parameter xi: point x and Jacobian J[m][k] = d x_m / d xi_k
+static void geoMapHost(const HostPatch& P, const double* xi, double* x, double J[3][3]) {
+    const int d = P.dim;
+    int first[3] = {0, 0, 0}, pp[3] = {0, 0, 0}, ng[3] = {1, 1, 1};
+    double v[3][32], dv[3][32];
+    double buf[64];
+    for (int k = 0; k < 3; ++k) {
+        v[k][0] = 1.0;
+        dv[k][0] = 0.0;
+    }
+    for (int k = 0; k < d; ++k) {
+        const Basis1D& B = P.g[k];
+        const int sp = B.span(xi[k]);
+        B.eval(sp, xi[k], buf);
+        first[k] = sp - B.p;
+        pp[k] = B.p;
+        ng[k] = B.n();
+        for (int r = 0; r <= B.p; ++r) {
+            v[k][r] = buf[r];
+            dv[k][r] = buf[B.p + 1 + r];
+        }
+    }
+    for (int m = 0; m < d; ++m) {
+        x[m] = 0.0;
+        for (int k = 0; k < d; ++k) J[m][k] = 0.0;
+    }
+    for (int c = 0; c <= pp[2]; ++c)
+        for (int b = 0; b <= pp[1]; ++b)
+            for (int a = 0; a <= pp[0]; ++a) {
+                const long long gi = first[0] + a + (long long)ng[0] * (first[1] + b + (long long)ng[1] * (first[2] + c));
+                const int idx[3] = {a, b, c};
+                double w = 1.0, dw[3];
+                for (int k = 0; k < d; ++k) w *= v[k][idx[k]];
+                for (int k = 0; k < d; ++k) {
+                    dw[k] = dv[k][idx[k]];
+                    for (int l = 0; l < d; ++l)
+                        if (l != k) dw[k] *= v[l][idx[l]];
+                }
+                for (int m = 0; m < d; ++m) {
+                    const double cm = P.coefs[size_t(gi) * d + m];
+                    x[m] += w * cm;
+                    for (int k = 0; k < d; ++k) J[m][k] += dw[k] * cm;
+                }
+            }
+}
+
+// Dirichlet values by L2 projection (gsAssembler::computeDirichletDofsL2Proj,
+// gsAssembler.hpp:392-534): one mass system over all eliminated dofs, assembled on the elements of
+// every Dirichlet side with p_k + 1 Gauss points in each side direction (the fixed direction
+// weighs 1), the weight times |det J| of the full geometry Jacobian at the boundary point (the
+// reference's map data carries no side, so that is its measure), the boundary data u at the
+// mapped point; solved by Jacobi-preconditioned CG to round-off (the reference: Eigen's
+// diagonal-preconditioned CG at its default tolerance)
+static void dirichletValuesL2(const ProblemDesc& pd, const DofMap& map, std::vector<double>& ddof) {
+    const int nb = map.boundarySize;
+    ddof.assign(nb, 0.0);
+    if (nb == 0) return;
+    const int dim = pd.dim;
+    const int nsides = int(pd.dsides.size() / 2);
+    struct Trip {
+        int i, j;
+        double v;
+    };
+    std::vector<std::vector<Trip>> trips(nsides);
+    std::vector<std::vector<std::pair<int, double>>> rhsParts(nsides);
+#pragma omp parallel for schedule(dynamic, 1) if (nsides >= 2)
+    for (int sd = 0; sd < nsides; ++sd) {
+        const HostPatch& P = pd.patches[pd.dsides[2 * sd]];
+        const int side = pd.dsides[2 * sd + 1];
+        const int dir = (side - 1) / 2, parity = (side - 1) % 2;
+        int od[2] = {0, 0}, no = 0;
+        for (int k = 0; k < dim; ++k)
+            if (k != dir) od[no++] = k;
+        const double fixv = parity ? P.b[dir].t.back() : P.b[dir].t.front();
+        const FieldParams& F = pd.fieldsOf(pd.dsides[2 * sd]);
+        std::vector<double> gx[2], gw[2];
+        for (int o = 0; o < no; ++o) gaussLegendre(P.b[od[o]].p + 1, gx[o], gw[o]);
+        const int ne0 = P.b[od[0]].nelem(), ne1 = no > 1 ? P.b[od[1]].nelem() : 1;
+        const int sfix = P.b[dir].span(fixv);
+        std::vector<double> fixBuf(2 * (P.b[dir].p + 1));
+        P.b[dir].eval(sfix, fixv, fixBuf.data());
+        std::vector<Trip>& T = trips[sd];
+        std::vector<std::pair<int, double>>& R = rhsParts[sd];
+        for (int e1 = 0; e1 < ne1; ++e1)
+            for (int e0 = 0; e0 < ne0; ++e0) {
+                const int e[2] = {e0, e1};
+                int spn[3];
+                double lo[3], hi[3];
+                spn[dir] = sfix;
+                for (int o = 0; o < no; ++o) {
+                    const Basis1D& B = P.b[od[o]];
+                    spn[od[o]] = B.elementSpan(e[o]);
+                    lo[o] = B.breaks[e[o]];
+                    hi[o] = B.breaks[e[o] + 1];
+                }
+                // eliminated dofs active on this element (local slot, boundary index)
+                int pp[3] = {0, 0, 0}, nloc[3] = {1, 1, 1};
+                for (int k = 0; k < dim; ++k) {
+                    pp[k] = P.b[k].p;
+                    nloc[k] = P.b[k].n();
+                }
+                std::vector<std::pair<int, int>> act;
+                for (int c = 0; c <= (dim > 2 ? pp[2] : 0); ++c)
+                    for (int b = 0; b <= pp[1]; ++b)
+                        for (int a = 0; a <= pp[0]; ++a) {
+                            const int i0 = spn[0] - pp[0] + a, i1 = spn[1] - pp[1] + b;
+                            const int i2 = dim > 2 ? spn[2] - pp[2] + c : 0;
+                            const int loc = i0 + nloc[0] * (i1 + nloc[1] * i2);
+                            const int gl = map.index[P.offset + loc];
+                            if (gl >= map.freeSize) act.push_back({a + (pp[0] + 1) * (b + (pp[1] + 1) * c), gl - map.freeSize});
+                        }
+                if (act.empty()) continue;
+                const int na = int(act.size());
+                std::vector<double> Me(size_t(na) * na, 0.0), re(na, 0.0), vals(na);
+                const int nq0 = int(gx[0].size()), nq1 = no > 1 ? int(gx[1].size()) : 1;
+                for (int q1 = 0; q1 < nq1; ++q1)
+                    for (int q0 = 0; q0 < nq0; ++q0) {
+                        double xi[3] = {0, 0, 0};
+                        xi[dir] = fixv;
+                        double w = 1.0;  // the fixed direction: weight 2 on a zero-length interval, factor 1/2
+                        const int q[2] = {q0, q1};
+                        for (int o = 0; o < no; ++o) {
+                            const double h = 0.5 * (hi[o] - lo[o]);
+                            xi[od[o]] = lo[o] + h * (gx[o][q[o]] + 1.0);
+                            w *= (h == 0.0 ? 0.5 : h) * gw[o][q[o]];
+                        }
+                        double x[3], J[3][3];
+                        geoMapHost(P, xi, x, J);
+                        double det;
+                        if (dim == 3)
+                            det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                                  J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                                  J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+                        else
+                            det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+                        const double wk = w * std::fabs(det);
+                        const double g = evalU(F, x);
+                        double bv[3][32];
+                        double buf[64];
+                        for (int k = 0; k < dim; ++k) {
+                            if (k == dir) {
+                                for (int r = 0; r <= pp[k]; ++r) bv[k][r] = fixBuf[r];
+                            } else {
+                                P.b[k].eval(spn[k], xi[k], buf);
+                                for (int r = 0; r <= pp[k]; ++r) bv[k][r] = buf[r];
+                            }
+                        }
+                        for (int i = 0; i < na; ++i) {
+                            int sl = act[i].first;
+                            const int a = sl % (pp[0] + 1);
+                            sl /= pp[0] + 1;
+                            const int b = sl % (pp[1] + 1);
+                            const int c = sl / (pp[1] + 1);
+                            double v = bv[0][a] * bv[1][b];
+                            if (dim > 2) v *= bv[2][c];
+                            vals[i] = v;
+                        }
+                        for (int i = 0; i < na; ++i) {
+                            for (int j = 0; j < na; ++j) Me[size_t(i) * na + j] += wk * vals[i] * vals[j];
+                            re[i] += wk * vals[i] * g;
+                        }
+                    }
+                for (int i = 0; i < na; ++i) {
+                    for (int j = 0; j < na; ++j) T.push_back({act[i].second, act[j].second, Me[size_t(i) * na + j]});
+                    R.push_back({act[i].second, re[i]});
+                }
+            }
+    }
+    // CSR of the projection matrix (entries summed in side order, then element order)
+    std::vector<Trip> all;
+    std::vector<double> rhs(nb, 0.0);
+    for (int sd = 0; sd < nsides; ++sd) {
+        all.insert(all.end(), trips[sd].begin(), trips[sd].end());
+        for (auto& pr : rhsParts[sd]) rhs[pr.first] += pr.second;
+    }
+    std::stable_sort(all.begin(), all.end(), [](const Trip& a, const Trip& b) { return a.i != b.i ? a.i < b.i : a.j < b.j; });
+    std::vector<int> ptr(nb + 1, 0), col;
+    std::vector<double> val;
+    for (size_t k = 0; k < all.size();) {
+        size_t e = k;
+        double v = 0.0;
+        while (e < all.size() && all[e].i == all[k].i && all[e].j == all[k].j) v += all[e++].v;
+        col.push_back(all[k].j);
+        val.push_back(v);
+        ++ptr[all[k].i + 1];
+        k = e;
+    }
+    for (int i = 0; i < nb; ++i) ptr[i + 1] += ptr[i];
+    // Jacobi-PCG to round-off
+    std::vector<double> dinv(nb, 0.0), r = rhs, z(nb), p(nb), t(nb);
+    for (int i = 0; i < nb; ++i)
+        for (int k = ptr[i]; k < ptr[i + 1]; ++k)
+            if (col[k] == i && val[k] != 0.0) dinv[i] = 1.0 / val[k];
+    double bb = 0.0;
+    for (double v : rhs) bb += v * v;
+    if (bb == 0.0) return;
+    for (int i = 0; i < nb; ++i) z[i] = dinv[i] * r[i];
+    p = z;
+    double rz = 0.0;
+    for (int i = 0; i < nb; ++i) rz += r[i] * z[i];
+    for (int it = 0; it < 10 * nb + 100; ++it) {
+        double pt = 0.0;
+        for (int i = 0; i < nb; ++i) {
+            double acc = 0.0;
+            for (int k = ptr[i]; k < ptr[i + 1]; ++k) acc += val[k] * p[col[k]];
+            t[i] = acc;
+            pt += p[i] * acc;
+        }
+        const double a = rz / pt;
+        double rr = 0.0;
+        for (int i = 0; i < nb; ++i) {
+            ddof[i] += a * p[i];
+            r[i] -= a * t[i];
+            rr += r[i] * r[i];
+        }
+        if (rr <= 1e-30 * bb) break;
+        double rzn = 0.0;
+        for (int i = 0; i < nb; ++i) {
+            z[i] = dinv[i] * r[i];
+            rzn += r[i] * z[i];
+        }
+        const double beta = rzn / rz;
+        rz = rzn;
+        for (int i = 0; i < nb; ++i) p[i] = z[i] + beta * p[i];
+    }
+}
+
 void dirichletValues(const ProblemDesc& pd, const DofMap& map, std::vector<double>& ddof) {
+    if (pd.dirL2) {
+        dirichletValuesL2(pd, map, ddof);
+        return;
+    }
     ddof.assign(map.boundarySize, 0.0);
     const int nsides = int(pd.dsides.size() / 2);
     // one side per thread; threads inside the side only for a single side (the work of one side is
@@ -922,6 +1153,9 @@ void problemFromC(const void* ptr, ProblemDesc& pd) {
     F.ufreq = pr->ufreq;
     pd.quA = pr->quA;
     pd.quB = pr->quB;
+    if (pr->dirichlet_strategy != 0 && pr->dirichlet_strategy != 1)
+        throw std::invalid_argument("dirichlet_strategy must be interpolation (0) or L2 projection (1)");
+    pd.dirL2 = pr->dirichlet_strategy;
 }
 
 void batchFromDescs(std::vector<ProblemDesc>& items, ProblemDesc& pd) {
@@ -937,8 +1171,10 @@ void batchFromDescs(std::vector<ProblemDesc>& items, ProblemDesc& pd) {
             pd.quA = one.quA;
             pd.quB = one.quB;
             pd.fields = one.fields;
-        } else if (one.dim != pd.dim || one.quA != pd.quA || one.quB != pd.quB) {
-            throw std::invalid_argument("batch: dimension and quadrature rule must agree across problems");
+            pd.dirL2 = one.dirL2;
+        } else if (one.dim != pd.dim || one.quA != pd.quA || one.quB != pd.quB || one.dirL2 != pd.dirL2) {
+            throw std::invalid_argument(
+                "batch: dimension, quadrature rule and Dirichlet strategy must agree across problems");
         }
         HostPatch P = std::move(one.patches[0]);
         P.field = int(j);

@@ -51,6 +51,7 @@ struct ProblemDesc {
     std::vector<FieldParams> pfields;
     double quA = 1.0;
     int quB = 1;
+    int dirL2 = 0;  // Dirichlet values by L2 projection (else interpolation)
     const FieldParams& fieldsOf(int patch) const {
         return pfields.empty() ? fields : pfields[size_t(patches[size_t(patch)].field)];
     }

@@ -93,7 +93,8 @@ struct Server {
         double sum = 0.0;
         for (auto it = queue.begin(); it != queue.end() && int(batch.size()) < maxBatch;) {
             Request* r = *it;
-            const bool same = r->pd.dim == dim && r->tol == tol && r->pd.quA == quA && r->pd.quB == quB;
+            const bool same = r->pd.dim == dim && r->tol == tol && r->pd.quA == quA && r->pd.quB == quB &&
+                              r->pd.dirL2 == head->pd.dirL2;
             if (same && reserved + sum + r->est <= budget) {
                 sum += r->est;
                 batch.push_back(r);

@@ -143,6 +143,7 @@ class Problem:
     mg_damping: float = 0.6
     mg_cycles: int = 1            # gsMultiGridOp "NumCycles" (1 = V-cycle, 2 = W-cycle)
     mg_cgc_damping: float = 1.0   # gsMultiGridOp "CoarseGridCorrectionDamping"
+    dirichlet_l2: bool = False    # Dirichlet values by L2 projection (dirichlet::l2Projection)
     name: str = ""
 
     # ---- closed forms (numpy, used by the generator's checks and by the host tests) ----
@@ -452,6 +453,8 @@ def write_spec(prob: Problem, path: str) -> None:
         lines.append(f"kappa_const {fmt(prob.kappa_const)}")
     lines.append(f"ufreq {prob.ufreq}")
     lines.append(f"quad {fmt(prob.quA)} {prob.quB}")
+    if prob.dirichlet_l2:
+        lines.append("dirichlet_values l2")
     lines.append(f"solver {prob.solver} {fmt(prob.tol)} {prob.maxit}")
     lines.append(f"mg {prob.mg_levels} {prob.mg_npre} {prob.mg_npost} {fmt(prob.mg_damping)}")
     if prob.mg_cycles != 1 or prob.mg_cgc_damping != 1.0:

@@ -51,7 +51,7 @@ struct gsGpuProblemPack {
     gsgpu_problem prob{};
 
     void pack(const gsMultiPatch<T>& mp, const gsMultiBasis<T>& mb, const std::vector<int>& dirichletSides,
-              const gsGpuFields& f, double quA, int quB) {
+              const gsGpuFields& f, double quA, int quB, int dirichletStrategy = GSGPU_DIRICHLET_INTERPOLATION) {
         const short_t d = mp.parDim();
         degree.clear(); nknots.clear(); knots.clear(); gdegree.clear(); gnknots.clear(); gknots.clear();
         coefs.clear(); ifaces.clear();
@@ -86,6 +86,7 @@ struct gsGpuProblemPack {
         prob.ufreq = fields.ufreq;
         prob.quA = quA;
         prob.quB = quB;
+        prob.dirichlet_strategy = dirichletStrategy;
     }
 
 private:
@@ -228,8 +229,13 @@ private:
             dsides.push_back(it->patch());
             dsides.push_back(it->side().index());
         }
+        // "DirichletValues": interpolation or L2 projection (gsAssembler.hpp:34, 231-534)
+        const index_t dv = this->m_options.getInt("DirichletValues");
+        if (dv != dirichlet::interpolation && dv != dirichlet::l2Projection)
+            throw std::invalid_argument("gsGpuPoissonAssembler: DirichletValues must be interpolation or l2Projection");
         m_pack.pack(this->patches(), this->m_bases[0], dsides, m_fields, this->m_options.getReal("quA"),
-                    this->m_options.getInt("quB"));
+                    this->m_options.getInt("quB"),
+                    dv == dirichlet::l2Projection ? GSGPU_DIRICHLET_L2 : GSGPU_DIRICHLET_INTERPOLATION);
         check(gsgpu_set_problem(m_ctx, &m_pack.prob));
         check(gsgpu_refresh(m_ctx));
     }

@@ -35,7 +35,8 @@ typedef struct gsgpu_context gsgpu_context;
  * Interfaces are conforming with identity orientation (the gsBoxTopology interfaces of
  * gsNurbsCreator::BSplineSquareGrid / BSplineCubeGrid), eliminated by gluing (iFace::glue).
  * Dirichlet sides are eliminated (dirichlet::elimination) with values by interpolation
- * (dirichlet::interpolation, gsAssembler.hpp:314-390) of the exact solution u.
+ * (dirichlet::interpolation, gsAssembler.hpp:314-390) or L2 projection (dirichlet::l2Projection,
+ * gsAssembler.hpp:392-534) of the exact solution u.
  * Coefficient, source and exact solution are closed forms evaluated on the device:
  *   g(x) = kappa_scale * sum_m kappa_amp[m] cos(pi kappa_k[m].x + kappa_phase[m])
  *   kappa = exp(kappa_alpha * g) if kappa_fourier else kappa_const
@@ -64,7 +65,12 @@ typedef struct {
     int ufreq;
     double quA;            /* Gauss points per direction: quA * degree + quB (gsQuadrature.h:151-171) */
     int quB;
+    int dirichlet_strategy; /* GSGPU_DIRICHLET_INTERPOLATION (0) or GSGPU_DIRICHLET_L2 (1): the
+                               "DirichletValues" option, dirichlet::interpolation or
+                               dirichlet::l2Projection (gsAssembler.hpp:231-534) */
 } gsgpu_problem;
+#define GSGPU_DIRICHLET_INTERPOLATION 0
+#define GSGPU_DIRICHLET_L2 1
 
 /* solver options (gsIterativeSolver::defaultOptions gsIterativeSolver.h:92-99,
  * gsMultiGridOp options gsMultiGrid.hpp:299-328, gsJacobiOp "Damping") */
@@ -122,7 +128,8 @@ int gsgpu_sizes(gsgpu_context* ctx, int* nfree, long long* nnz, int* nfixed, int
 int gsgpu_matrix_csr(gsgpu_context* ctx, int* ptr, int* col, double* val);
 /* gsAssembler::rhs() (gsAssembler.h:618) */
 int gsgpu_rhs(gsgpu_context* ctx, double* rhs);
-/* gsAssembler::fixedDofs() (gsAssembler.h:538) */
+/* gsAssembler::fixedDofs() (gsAssembler.h:538); on a host-only context (device -1) computed on
+ * the host after refresh() */
 int gsgpu_fixed_dofs(gsgpu_context* ctx, double* ddof);
 /* the eliminated-dof values (m_ddof, eliminated-dof order of gsgpu_fixed_dofs) computed by the
  * caller, e.g. gsFeSpace::setup's interpolation or L2 projection (gsExpressions.h:1091-1212,

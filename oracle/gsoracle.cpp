@@ -6,6 +6,7 @@
 #include "gsoracle.h"
 
 #include <algorithm>
+#include <map>
 #include <chrono>
 #include <cmath>
 #include <cstdint>
@@ -311,6 +312,7 @@ struct Oracle {
     int nlocal = 0;
     Csr A;
     std::vector<double> rhs, ddof;
+    bool dirL2 = false;  // Dirichlet values by L2 projection instead of interpolation
     bool assembled = false;
 
     int nq(int p) const { return int(quA * p + quB + 0.5); }
@@ -421,6 +423,7 @@ struct Oracle {
         F.ufreq = pr->ufreq;
         quA = pr->quA;
         quB = pr->quB;
+        dirL2 = pr->dirichlet_l2 != 0;
 
         // gsDofMapper(mb, bc, 0): markBoundary for every Dirichlet side
         // (gsDofMapper.hpp:100-111), then matchInterface for every interface
@@ -542,10 +545,128 @@ struct Oracle {
         }
     }
 
+    // Dirichlet values by L2 projection (gsAssembler::computeDirichletDofsL2Proj,
+    // src/gsAssembler/gsAssembler.hpp:392-534): on every element of every Dirichlet side,
+    // p_k + 1 Gauss points per side direction (the fixed direction: one node of weight 2 on a
+    // zero-length interval, i.e. 1), weight times |det J| of the full map (the map data carries no
+    // side), the mass matrix and the moments of u over the eliminated dofs active there; the
+    // global system is solved by Jacobi-preconditioned CG (gsSparseSolver::CGDiagonal)
+    void dirichletValuesL2() {
+        const int nb = map.boundarySize;
+        ddof.assign(nb, 0.0);
+        std::vector<std::map<int, double>> M(nb);
+        std::vector<double> g(nb, 0.0);
+        for (size_t si = 0; si < dsides.size(); si += 2) {
+            const PatchData& P = patches[dsides[si]];
+            const int side = dsides[si + 1];
+            const int dir = (side - 1) / 2, par = (side - 1) % 2;
+            std::vector<int> odirs;
+            for (int k = 0; k < dim; ++k) if (k != dir) odirs.push_back(k);
+            const double fixv = par ? P.b[dir].t.back() : P.b[dir].t.front();
+            const int no = int(odirs.size());
+            std::vector<std::vector<double>> qx(no), qw(no);
+            for (int o = 0; o < no; ++o) gaussRule(P.b[odirs[o]].p + 1, qx[o], qw[o]);
+            const int ne0 = P.b[odirs[0]].nelem(), ne1 = no > 1 ? P.b[odirs[1]].nelem() : 1;
+            for (int e1 = 0; e1 < ne1; ++e1)
+                for (int e0 = 0; e0 < ne0; ++e0) {
+                    const int el[2] = {e0, e1};
+                    const int nq0 = int(qx[0].size()), nq1 = no > 1 ? int(qx[1].size()) : 1;
+                    for (int q1 = 0; q1 < nq1; ++q1)
+                        for (int q0 = 0; q0 < nq0; ++q0) {
+                            const int qq[2] = {q0, q1};
+                            double xi[3] = {0, 0, 0};
+                            xi[dir] = fixv;
+                            double w = 1.0;
+                            for (int o = 0; o < no; ++o) {
+                                const Basis1D& B = P.b[odirs[o]];
+                                const double a = B.breaks[el[o]], b = B.breaks[el[o] + 1];
+                                const double h = 0.5 * (b - a);
+                                xi[odirs[o]] = a + h * (qx[o][qq[o]] + 1.0);
+                                w *= h * qw[o][qq[o]];
+                            }
+                            double x[3], J[9];
+                            geoEval(P, xi, x, J);
+                            double det = dim == 2 ? J[0] * J[3] - J[1] * J[2]
+                                                  : J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
+                                                        J[2] * (J[3] * J[7] - J[4] * J[6]);
+                            const double wk = w * std::fabs(det);
+                            double kap, ff, u;
+                            F.eval(x, kap, ff, u);
+                            // discretisation basis values at xi; the eliminated dofs among them
+                            int sp[3], first[3];
+                            double v[3][16], buf[64];
+                            for (int k = 0; k < dim; ++k) {
+                                const Basis1D& B = P.b[k];
+                                sp[k] = B.span(xi[k]);
+                                first[k] = sp[k] - B.p;
+                                B.ders(sp[k], xi[k], 0, buf);
+                                for (int r = 0; r <= B.p; ++r) v[k][r] = buf[r];
+                            }
+                            std::vector<std::pair<int, double>> act;
+                            const int p2 = dim == 3 ? P.b[2].p : 0;
+                            for (int c = 0; c <= p2; ++c)
+                                for (int b = 0; b <= P.b[1].p; ++b)
+                                    for (int a = 0; a <= P.b[0].p; ++a) {
+                                        const int loc = first[0] + a +
+                                                        P.b[0].n() * (first[1] + b + (dim == 3 ? P.b[1].n() * (first[2] + c) : 0));
+                                        const int gi = map.index[P.offset + loc];
+                                        if (gi < map.freeSize) continue;
+                                        double val = v[0][a] * v[1][b];
+                                        if (dim == 3) val *= v[2][c];
+                                        act.push_back({gi - map.freeSize, val});
+                                    }
+                            for (auto& ai : act) {
+                                for (auto& aj : act) M[ai.first][aj.first] += wk * ai.second * aj.second;
+                                g[ai.first] += wk * ai.second * u;
+                            }
+                        }
+                }
+        }
+        // Jacobi-preconditioned CG to round-off
+        std::vector<double> dinv(nb, 0.0), r = g, z(nb), pv(nb), t(nb);
+        for (int i = 0; i < nb; ++i) {
+            auto it = M[i].find(i);
+            if (it != M[i].end() && it->second != 0.0) dinv[i] = 1.0 / it->second;
+        }
+        double bb = 0.0;
+        for (double a : g) bb += a * a;
+        if (bb == 0.0) return;
+        for (int i = 0; i < nb; ++i) z[i] = dinv[i] * r[i];
+        pv = z;
+        double rz = 0.0;
+        for (int i = 0; i < nb; ++i) rz += r[i] * z[i];
+        for (int it = 0; it < 10 * nb + 100; ++it) {
+            double pt = 0.0;
+            for (int i = 0; i < nb; ++i) {
+                double acc = 0.0;
+                for (auto& e : M[i]) acc += e.second * pv[e.first];
+                t[i] = acc;
+                pt += pv[i] * acc;
+            }
+            const double al = rz / pt;
+            double rr = 0.0;
+            for (int i = 0; i < nb; ++i) {
+                ddof[i] += al * pv[i];
+                r[i] -= al * t[i];
+                rr += r[i] * r[i];
+            }
+            if (rr <= 1e-30 * bb) break;
+            double rzn = 0.0;
+            for (int i = 0; i < nb; ++i) { z[i] = dinv[i] * r[i]; rzn += r[i] * z[i]; }
+            const double be = rzn / rz;
+            rz = rzn;
+            for (int i = 0; i < nb; ++i) pv[i] = z[i] + be * pv[i];
+        }
+    }
+
     // Dirichlet values by interpolation at the boundary basis anchors
     // (gsAssembler::computeDirichletDofsIntpl, src/gsAssembler/gsAssembler.hpp:314-390, with
     //  gsTensorBasis::interpolateAtAnchors, gsTensorBasis.hpp:906-960)
     void dirichletValues() {
+        if (dirL2) {
+            dirichletValuesL2();
+            return;
+        }
         ddof.assign(map.boundarySize, 0.0);
         for (size_t si = 0; si < dsides.size(); si += 2) {
             const PatchData& P = patches[dsides[si]];

@@ -37,6 +37,7 @@ typedef struct {
     int ufreq;
     double quA;
     int quB;
+    int dirichlet_l2;           /* 1: Dirichlet values by L2 projection, 0: by interpolation */
 } orc_problem;
 
 void* orc_create(const orc_problem* prob);

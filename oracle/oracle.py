@@ -33,7 +33,7 @@ class _Problem(C.Structure):
         ("kappa_fourier", C.c_int), ("kappa_const", C.c_double), ("kappa_alpha", C.c_double),
         ("kappa_scale", C.c_double), ("kappa_nmodes", C.c_int), ("kappa_amp", C.POINTER(C.c_double)),
         ("kappa_k", C.POINTER(C.c_int)), ("kappa_phase", C.POINTER(C.c_double)),
-        ("ufreq", C.c_int), ("quA", C.c_double), ("quB", C.c_int),
+        ("ufreq", C.c_int), ("quA", C.c_double), ("quB", C.c_int), ("dirichlet_l2", C.c_int),
     ]
 
 
@@ -111,6 +111,7 @@ class OracleProblem:
         s.kappa_nmodes = len(prob.kappa_amp) if prob.kappa_fourier else 0
         s.kappa_amp = _ptr(a["amp"], C.c_double); s.kappa_k = _ptr(a["kk"], C.c_int); s.kappa_phase = _ptr(a["phase"], C.c_double)
         s.ufreq = prob.ufreq; s.quA = prob.quA; s.quB = prob.quB
+        s.dirichlet_l2 = 1 if getattr(prob, "dirichlet_l2", False) else 0
         self._s = s
         self.prob = prob
         self.h = lib().orc_create(C.byref(s))

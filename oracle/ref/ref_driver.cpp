@@ -68,6 +68,7 @@ struct Spec {
     double damping = 0.6;
     int cycles = 1;
     double cgc = 1.0;
+    int dirL2 = 0;  // Dirichlet values by L2 projection instead of interpolation
 };
 
 Spec readSpec(const std::string& path) {
@@ -99,6 +100,7 @@ Spec readSpec(const std::string& path) {
             for (auto& m : s.modes) in >> m.amp >> m.k[0] >> m.k[1] >> m.k[2] >> m.phase;
         } else if (tok == "ufreq") in >> s.ufreq;
         else if (tok == "quad") in >> s.quA >> s.quB;
+        else if (tok == "dirichlet_values") { std::string v; in >> v; s.dirL2 = v == "l2" ? 1 : 0; }
         else if (tok == "solver") in >> s.solver >> s.tol >> s.maxit;
         else if (tok == "mg") in >> s.levels >> s.npre >> s.npost >> s.damping;
         else if (tok == "mgcycle") in >> s.cycles >> s.cgc;
@@ -260,6 +262,7 @@ int main(int argc, char** argv) {
         A.reset(new gsCDRAssembler<>(mp, mb, bc, rhsF, kappaA, zeroB, zeroC, dirichlet::elimination, iFace::glue));
     A->options().setReal("quA", s.quA);
     A->options().setInt("quB", s.quB);
+    if (s.dirL2) A->options().setInt("DirichletValues", dirichlet::l2Projection);
 
     auto t0 = std::chrono::steady_clock::now();
     A->assemble();

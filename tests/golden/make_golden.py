@@ -48,6 +48,12 @@ def cases():
     pr.mg_levels, pr.mg_cycles, pr.mg_cgc_damping = 4, 2, 0.8  # W-cycle, damped coarse correction
     pr.tol = 1e-8
     out["disp2d_p2_32x24_mgw"] = pr
+    pr = P.displaced_single_patch(3, (4, 5, 3), (2, 3, 2), 7, 0.04, ufreq=2)
+    pr.dirichlet_l2 = True  # dirichlet::l2Projection
+    out["disp3d_p232_4x5x3_l2dir"] = pr
+    pr = P.cube_grid(n=2, n_elem=3, p=2, seed=4, kappa_modes=8)
+    pr.dirichlet_l2 = True
+    out["cubegrid2_p2_n3_l2dir"] = pr
     pr = P.cube_grid(n=2, n_elem=4, p=2, seed=3, kappa_modes=8)
     pr.solver = "cg"
     pr.tol = 1e-8

@@ -63,6 +63,12 @@ def test_host_plan_matches_reference(lib, path):
         assert lib.gsgpu_matrix_csr(h, ptr.ctypes.data, col.ctypes.data, None) == _lib.OK
         K = _csr_from_csc(g)
         assert np.array_equal(ptr, K.indptr) and np.array_equal(col, K.indices)
+        # eliminated-dof values of the problem's Dirichlet strategy (interpolation or L2
+        # projection), computed on the host: the reference's own values
+        dd = np.empty(nb.value, np.float64)
+        assert lib.gsgpu_fixed_dofs(h, dd.ctypes.data) == _lib.OK
+        if nb.value:
+            assert np.abs(dd - g["ddof"]).max() <= 1e-12 * max(1.0, np.abs(g["ddof"]).max()), name
         # numerical calls are refused without a device
         assert lib.gsgpu_assemble(h, 0) == _lib.ERR_STATE
     finally:
