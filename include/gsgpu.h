@@ -99,8 +99,9 @@ typedef struct {
 } gsgpu_solve_info;
 
 /* lifetime. device >= 0: a CUDA device. device == -1: a host-only context that computes the
- * dof map and the sparsity pattern (set_problem, refresh, sizes, dof_map, matrix_csr with
- * val == NULL) and refuses every numerical call with GSGPU_ERR_STATE. */
+ * dof map, the sparsity pattern and the eliminated-dof values (set_problem, refresh, sizes,
+ * dof_map, matrix_csr with val == NULL, fixed_dofs) and refuses every device call with
+ * GSGPU_ERR_STATE. */
 int gsgpu_create(gsgpu_context** ctx, int device);
 int gsgpu_destroy(gsgpu_context* ctx);
 const char* gsgpu_last_error(const gsgpu_context* ctx);
