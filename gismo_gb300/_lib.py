@@ -35,6 +35,7 @@ class Problem(C.Structure):
         ("kappa_scale", C.c_double), ("kappa_nmodes", C.c_int), ("kappa_amp", C.POINTER(C.c_double)),
         ("kappa_k", C.POINTER(C.c_int)), ("kappa_phase", C.POINTER(C.c_double)),
         ("ufreq", C.c_int), ("quA", C.c_double), ("quB", C.c_int), ("dirichlet_strategy", C.c_int),
+        ("nneumann", C.c_int), ("neumann", C.POINTER(C.c_int)),
     ]
 
 

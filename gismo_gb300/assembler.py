@@ -43,6 +43,7 @@ class PackedProblem:
             gdegree=np.array(gdeg, np.int32), gnknots=np.array(gnk, np.int32), gknots=np.array(gkn, np.float64),
             coefs=np.concatenate(co), ifaces=np.array(prob.interfaces, np.int32).reshape(-1),
             dirichlet=np.array(prob.dirichlet, np.int32).reshape(-1),
+            neumann=np.array(getattr(prob, "neumann", []), np.int32).reshape(-1),
             amp=np.ascontiguousarray(prob.kappa_amp, np.float64),
             kk=np.ascontiguousarray(prob.kappa_k, np.int32).reshape(-1),
             phase=np.ascontiguousarray(prob.kappa_phase, np.float64),
@@ -64,6 +65,7 @@ class PackedProblem:
         s.kappa_phase = _ptr(a["phase"], C.c_double)
         s.ufreq = prob.ufreq; s.quA = prob.quA; s.quB = prob.quB
         s.dirichlet_strategy = 1 if getattr(prob, "dirichlet_l2", False) else 0
+        s.nneumann = len(a["neumann"]) // 2; s.neumann = _ptr(a["neumann"], C.c_int)
         self.struct = s
 
 

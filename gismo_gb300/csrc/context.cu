@@ -116,6 +116,13 @@ void Context::buildTables() {
         mk(tabLd[0], [](const DevPatch& D) { return dev::loadWork<21>(D); });
         mk(tabLd[1], [](const DevPatch& D) { return dev::loadWork<22>(D); });
     }
+    buildNeumann(pd, L, launch::kBlock, neu);
+    if (!neu.sides.empty()) {
+        upload(arena, dNeuSides, neu.sides, stream);
+        upload(arena, dNeuDofs, neu.dofs, stream);
+        upload(arena, dNeuBlocks, neu.blocks, stream);
+        allocN(arena, dNeuVals, neu.nvals);
+    }
 }
 
 void Context::refresh() {
@@ -424,6 +431,9 @@ void Context::assemble(int precision) {
     if (mixed) ensureMixedBuffers();
     launch::basisTables(dTabJobs, (long long)L.tabjobs.size(), dKnots, dTab, s);
     launch::basisTables(dGtabJobs, (long long)L.gtabjobs.size(), dGknots, dGtab, s);
+    // Neumann face values in FP64, from the FP64 geometry table (both precisions)
+    launch::neumannFace(dNeuSides, dNeuBlocks, (long long)neu.blocks.size(), dPatches, dFields, dCoefs, dGtab, dIbuf,
+                        dWq, dNeuVals, s);
     // the df32 path reuses the FP64 intermediate buffers (same 8-byte element size)
     df32* gtabDf = reinterpret_cast<df32*>(dGtab);
     df32* pfDf = reinterpret_cast<df32*>(dPf);
@@ -527,6 +537,8 @@ void Context::assemble(int precision) {
             launch::loadContract<21, double>(dPatches, tabLd[0].d, (long long)tabLd[0].h.size(), dFieldL, dLv1, dTab, dIbuf, s);
         launch::loadContract<22, double>(dPatches, tabLd[1].d, (long long)tabLd[1].h.size(), dLv1, dLvec, dTab, dIbuf, s);
     }
+    // Neumann integrals into the load vector of the dofs on Neumann sides
+    launch::neumannDofs(dNeuDofs, (long long)neu.dofs.size(), dNeuSides, dPatches, dTab, dIbuf, dNeuVals, dLvec, s);
     GSGPU_CUDA_TRY(cudaEventRecord(ev[5], s));
     // K4: CSR values (segmented gather) and rhs with the Dirichlet lift
     dir.th.join();

@@ -155,6 +155,13 @@ struct Context {
     Tab tabRow[3][5];  // [stage][degree along the stage axis]: interior rows of simple axes
     Tab tabRowB[3][5]; // the remaining rows
     Tab tabTile31[5];  // 3D stage 1 interior rows in shared-memory tiles (degrees 2, 3)
+    // Neumann boundary integrals: the host plan, its sides, dofs and face-point blocks on the
+    // device, and the face quadrature values
+    NeumannPlan neu;
+    NeuSide* dNeuSides = nullptr;
+    NeuDof* dNeuDofs = nullptr;
+    BlkEnt* dNeuBlocks = nullptr;
+    double* dNeuVals = nullptr;
 
     // device buffers (solve)
     int solveN = -1;

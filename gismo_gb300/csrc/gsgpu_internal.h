@@ -75,6 +75,29 @@ struct PfJob {
     int p, q, E, pad;
 };
 
+// one Neumann side: the patch, the fixed direction and end, the side directions t[0], t[1] (t[1] = -1
+// in 2D), the first function and the values at the boundary parameter of the geometry (gfirst,
+// gval) and discretisation (bfirst, bval) bases of the fixed direction, and the side's block of
+// face quadrature values (qbase, nq = Q[t0] Q[t1] points, t0 fastest)
+constexpr int kMaxNeuDeg = 15;
+struct NeuSide {
+    int patch, dir, upper, t[2];
+    int gfirst, gp, bfirst, bp;
+    int pad;
+    double gval[kMaxNeuDeg + 1];
+    double bval[kMaxNeuDeg + 1];
+    long long qbase, nq;
+};
+
+// one patch-local dof on Neumann sides: its coordinates, its load-vector slot and the sides
+struct NeuDof {
+    int patch, nside;
+    int side[6];
+    int i[3];
+    int pad;
+    long long lvec;
+};
+
 // closed-form coefficient / source / exact-solution parameters (device constant-style struct)
 constexpr int kMaxModes = 64;
 struct FieldParams {

@@ -66,6 +66,14 @@ void l2Partials(const DevPatch* P, const BlkEnt* tab, long long nblk, const dev:
                 const double* Y1, const double* Y2, const double* gtab, const int* ibuf, const double* wq,
                 const double* btab, const double* coef, double* part, cudaStream_t s);
 
+// Neumann boundary integrals: w |n| h per face quadrature point (before the geometry table turns
+// into double-float values), then per dof on a Neumann side its sums added to the load vector
+void neumannFace(const NeuSide* sides, const BlkEnt* tab, long long nblk, const DevPatch* P,
+                 const dev::FieldConst<double>* F, const double* coefs, const double* gtab, const int* ibuf,
+                 const double* wq, double* vals, cudaStream_t s);
+void neumannDofs(const NeuDof* dofs, long long ndofs, const NeuSide* sides, const DevPatch* P, const double* btab,
+                 const int* ibuf, const double* vals, double* lvec, cudaStream_t s);
+
 // sparsity pattern of a problem without interfaces on the device (pattern_dev.cu) from the host's
 // row plan (plan.h RowPlan): counts and exclusive scans (nslot, nlift: n+1 entries), then the fill
 struct RowPlanDev {

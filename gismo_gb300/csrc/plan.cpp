@@ -7,6 +7,7 @@
 #include <cmath>
 #include <numeric>
 #include <stdexcept>
+#include <unordered_map>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -1128,6 +1129,24 @@ void problemFromC(const void* ptr, ProblemDesc& pd) {
             throw std::invalid_argument("dirichlet: bad patch or side index");
         pd.dsides.insert(pd.dsides.end(), f, f + 2);
     }
+    // Neumann sides: one condition per side, on a boundary side (gsBoundaryConditions holds one
+    // condition per side; interface sides are not boundaries)
+    for (int i = 0; i < pr->nneumann; ++i) {
+        const int* f = pr->neumann + 2 * i;
+        if (f[0] < 0 || f[0] >= pr->npatches || f[1] < 1 || f[1] > 2 * pr->dim)
+            throw std::invalid_argument("neumann: bad patch or side index");
+        auto onList = [&](const std::vector<int>& v, int stride) {
+            for (size_t k = 0; k < v.size(); k += size_t(stride))
+                if (v[k] == f[0] && v[k + 1] == f[1]) return true;
+            return false;
+        };
+        if (onList(pd.dsides, 2) || onList(pd.nsides, 2))
+            throw std::invalid_argument("neumann: side already carries a boundary condition");
+        for (size_t k = 0; k < pd.ifaces.size(); k += 4)
+            if ((pd.ifaces[k] == f[0] && pd.ifaces[k + 1] == f[1]) || (pd.ifaces[k + 2] == f[0] && pd.ifaces[k + 3] == f[1]))
+                throw std::invalid_argument("neumann: side is an interface");
+        pd.nsides.insert(pd.nsides.end(), f, f + 2);
+    }
     FieldParams& F = pd.fields;
     F = FieldParams{};
     F.dim = pr->dim;
@@ -1185,6 +1204,10 @@ void batchFromDescs(std::vector<ProblemDesc>& items, ProblemDesc& pd) {
             pd.dsides.push_back(int(j));
             pd.dsides.push_back(one.dsides[i + 1]);
         }
+        for (size_t i = 0; i < one.nsides.size(); i += 2) {
+            pd.nsides.push_back(int(j));
+            pd.nsides.push_back(one.nsides[i + 1]);
+        }
         pd.pfields.push_back(one.fields);
     }
 }
@@ -1195,6 +1218,75 @@ void batchFromC(int count, const void* ptr, ProblemDesc& pd) {
     std::vector<ProblemDesc> items(static_cast<size_t>(count));
     for (int j = 0; j < count; ++j) problemFromC(&pr[j], items[size_t(j)]);
     batchFromDescs(items, pd);
+}
+
+void buildNeumann(const ProblemDesc& pd, const Layout& L, int block, NeumannPlan& np) {
+    np = NeumannPlan();
+    const int dim = pd.dim;
+    const int nside = int(pd.nsides.size() / 2);
+    std::unordered_map<long long, size_t> slot;  // load-vector slot -> entry of np.dofs
+    for (int k = 0; k < nside; ++k) {
+        const int pi = pd.nsides[2 * k], side = pd.nsides[2 * k + 1];
+        const HostPatch& P = pd.patches[size_t(pi)];
+        const DevPatch& D = L.dev[size_t(pi)];
+        NeuSide S{};
+        S.patch = pi;
+        S.dir = (side - 1) / 2;
+        S.upper = (side - 1) % 2;
+        int no = 0;
+        S.t[1] = -1;
+        for (int a = 0; a < dim; ++a)
+            if (a != S.dir) S.t[no++] = a;
+        // the bases of the fixed direction at the boundary parameter
+        const Basis1D& G = P.g[S.dir];
+        const Basis1D& B = P.b[S.dir];
+        if (G.p > kMaxNeuDeg || B.p > kMaxNeuDeg) throw std::invalid_argument("neumann: degree too high");
+        const double fixv = S.upper ? B.t.back() : B.t.front();
+        std::vector<double> buf(2 * (kMaxNeuDeg + 1));
+        int sp = G.span(fixv);
+        G.eval(sp, fixv, buf.data());
+        S.gfirst = sp - G.p;
+        S.gp = G.p;
+        for (int c = 0; c <= G.p; ++c) S.gval[c] = buf[size_t(c)];
+        sp = B.span(fixv);
+        B.eval(sp, fixv, buf.data());
+        S.bfirst = sp - B.p;
+        S.bp = B.p;
+        for (int c = 0; c <= B.p; ++c) S.bval[c] = buf[size_t(c)];
+        S.qbase = np.nvals;
+        S.nq = (long long)D.Q[S.t[0]] * (dim == 3 ? D.Q[S.t[1]] : 1);
+        np.nvals += S.nq;
+        for (long long b = 0; b < S.nq; b += block) np.blocks.push_back({k, 0, b});
+        // the functions on the side: the layers of the fixed direction with a non-zero value
+        const int n0 = D.n[S.t[0]], n1 = dim == 3 ? D.n[S.t[1]] : 1;
+        for (int c = 0; c <= B.p; ++c) {
+            if (S.bval[c] == 0.0) continue;
+            for (int j1 = 0; j1 < n1; ++j1)
+                for (int j0 = 0; j0 < n0; ++j0) {
+                    int ii[3] = {0, 0, 0};
+                    ii[S.dir] = S.bfirst + c;
+                    ii[S.t[0]] = j0;
+                    if (dim == 3) ii[S.t[1]] = j1;
+                    const long long loc = ii[0] + (long long)D.n[0] * (ii[1] + (long long)D.n[1] * ii[2]);
+                    const long long lv = D.lvec_off + loc;
+                    auto it = slot.find(lv);
+                    if (it == slot.end()) {
+                        NeuDof J{};
+                        J.patch = pi;
+                        for (int a = 0; a < 3; ++a) J.i[a] = ii[a];
+                        J.lvec = lv;
+                        it = slot.emplace(lv, np.dofs.size()).first;
+                        np.dofs.push_back(J);
+                    }
+                    NeuDof& J = np.dofs[it->second];
+                    if (J.nside >= 6) throw std::invalid_argument("neumann: function on more than six sides");
+                    J.side[J.nside++] = k;
+                }
+        }
+        np.sides.push_back(S);
+    }
+    // load-vector order: neighbouring threads write neighbouring slots
+    std::sort(np.dofs.begin(), np.dofs.end(), [](const NeuDof& a, const NeuDof& b) { return a.lvec < b.lvec; });
 }
 
 void blockTable(const std::vector<long long>& work, int block, std::vector<BlkEnt>& tab) {

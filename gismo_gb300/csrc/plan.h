@@ -45,6 +45,7 @@ struct ProblemDesc {
     std::vector<HostPatch> patches;
     std::vector<int> ifaces;    // 4 per interface
     std::vector<int> dsides;    // 2 per Dirichlet side
+    std::vector<int> nsides;    // 2 per Neumann side
     FieldParams fields{};
     // batches of independent problems: one field set per problem (HostPatch::field indexes it);
     // empty for a single problem, whose patches all use `fields`
@@ -139,6 +140,18 @@ void dirichletValues(const ProblemDesc& pd, const DofMap& map, std::vector<doubl
 // closed-form fields on the host (same formulas as the device)
 void evalFields(const FieldParams& F, const double* x, double& kappa, double& f, double& u);
 void gaussLegendre(int n, std::vector<double>& x, std::vector<double>& w);
+
+// Neumann boundary integrals (gsVisitorNeumann): per Neumann side, its face quadrature grid (the
+// volume rule's abscissae in the side directions, the boundary parameter in the fixed one) and the
+// normal-direction basis values at the boundary; per patch-local dof on a Neumann side, the sides
+// whose integrals it collects (in side order, so the sum is deterministic)
+struct NeumannPlan {
+    std::vector<NeuSide> sides;
+    std::vector<NeuDof> dofs;
+    std::vector<BlkEnt> blocks;  // face quadrature points, kBlock per entry (patch = side index)
+    long long nvals = 0;         // face quadrature points over all sides
+};
+void buildNeumann(const ProblemDesc& pd, const Layout& L, int block, NeumannPlan& np);
 
 // block -> (patch, base) tables for batched kernels
 void blockTable(const std::vector<long long>& work, int block, std::vector<BlkEnt>& tab);

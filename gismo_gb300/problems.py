@@ -144,6 +144,9 @@ class Problem:
     mg_cycles: int = 1            # gsMultiGridOp "NumCycles" (1 = V-cycle, 2 = W-cycle)
     mg_cgc_damping: float = 1.0   # gsMultiGridOp "CoarseGridCorrectionDamping"
     dirichlet_l2: bool = False    # Dirichlet values by L2 projection (dirichlet::l2Projection)
+    # Neumann sides (patch, side), data h = sgn kappa du/dx_k on side s of direction k = (s-1)//2
+    # (sgn -1 on the lower side, +1 on the upper): the flux of u where the side is a plane x_k = c
+    neumann: List[Tuple[int, int]] = dataclasses.field(default_factory=list)
     name: str = ""
 
     # ---- closed forms (numpy, used by the generator's checks and by the host tests) ----
@@ -289,6 +292,18 @@ def _displaced(patch: Patch, disp: Optional[Displacement]) -> Patch:
 
 def all_sides(dim: int) -> List[int]:
     return list(range(1, 2 * dim + 1))
+
+
+def mixed_boundary(prob: Problem) -> Problem:
+    """Turn the upper boundary sides (east, north, back) of a problem's Dirichlet list into Neumann
+    sides: Dirichlet on the lower sides, Neumann on the upper ones (the gsPoissonSolver_test
+    set-up of mixed conditions). Returns the problem."""
+    keep, neu = [], []
+    for (pt, sd) in prob.dirichlet:
+        (neu if side_parameter(sd) == 1 else keep).append((pt, sd))
+    prob.dirichlet, prob.neumann = keep, neu
+    prob.name = prob.name + "_neu"
+    return prob
 
 
 # ------------------------------------------------------------------------------------------
@@ -445,6 +460,8 @@ def write_spec(prob: Problem, path: str) -> None:
         lines.append("interface " + " ".join(str(int(v)) for v in f))
     for dsd in prob.dirichlet:
         lines.append(f"dirichlet {dsd[0]} {dsd[1]}")
+    for nsd in prob.neumann:
+        lines.append(f"neumann {nsd[0]} {nsd[1]}")
     if prob.kappa_fourier:
         lines.append(f"kappa_fourier {fmt(prob.kappa_alpha)} {fmt(prob.kappa_scale)} {len(prob.kappa_amp)}")
         for a, k, ph in zip(prob.kappa_amp, prob.kappa_k, prob.kappa_phase):

@@ -42,16 +42,17 @@ struct gsGpuFields {
 
 /// A G+Smo problem packed into the C-ABI struct (include/gsgpu.h gsgpu_problem) together with the
 /// arrays it points to: tensor B-spline patches and bases, conforming identity-oriented
-/// interfaces, the Dirichlet sides (patch, side index pairs) and the device fields
+/// interfaces, the Dirichlet and Neumann sides (patch, side index pairs) and the device fields
 template <class T = real_t>
 struct gsGpuProblemPack {
-    std::vector<int> degree, nknots, gdegree, gnknots, ifaces, dsides;
+    std::vector<int> degree, nknots, gdegree, gnknots, ifaces, dsides, nsides;
     std::vector<double> knots, gknots, coefs;
     gsGpuFields fields;
     gsgpu_problem prob{};
 
     void pack(const gsMultiPatch<T>& mp, const gsMultiBasis<T>& mb, const std::vector<int>& dirichletSides,
-              const gsGpuFields& f, double quA, int quB, int dirichletStrategy = GSGPU_DIRICHLET_INTERPOLATION) {
+              const gsGpuFields& f, double quA, int quB, int dirichletStrategy = GSGPU_DIRICHLET_INTERPOLATION,
+              const std::vector<int>& neumannSides = std::vector<int>()) {
         const short_t d = mp.parDim();
         degree.clear(); nknots.clear(); knots.clear(); gdegree.clear(); gnknots.clear(); gknots.clear();
         coefs.clear(); ifaces.clear();
@@ -70,6 +71,7 @@ struct gsGpuProblemPack {
             ifaces.push_back(it->second().side().index());
         }
         dsides = dirichletSides;
+        nsides = neumannSides;
         fields = f;
         prob = gsgpu_problem{};
         prob.dim = d;
@@ -87,6 +89,7 @@ struct gsGpuProblemPack {
         prob.quA = quA;
         prob.quB = quB;
         prob.dirichlet_strategy = dirichletStrategy;
+        prob.nneumann = int(nsides.size() / 2); prob.neumann = nsides.data();
     }
 
 private:
@@ -229,13 +232,20 @@ private:
             dsides.push_back(it->patch());
             dsides.push_back(it->side().index());
         }
+        // Neumann sides (gsPoissonAssembler.hpp:59): their data is the closed-form flux
+        // sgn kappa du/dx_k of the device fields
+        std::vector<int> nsides;
+        for (typename gsBoundaryConditions<T>::const_iterator it = bc.neumannBegin(); it != bc.neumannEnd(); ++it) {
+            nsides.push_back(it->patch());
+            nsides.push_back(it->side().index());
+        }
         // "DirichletValues": interpolation or L2 projection (gsAssembler.hpp:34, 231-534)
         const index_t dv = this->m_options.getInt("DirichletValues");
         if (dv != dirichlet::interpolation && dv != dirichlet::l2Projection)
             throw std::invalid_argument("gsGpuPoissonAssembler: DirichletValues must be interpolation or l2Projection");
         m_pack.pack(this->patches(), this->m_bases[0], dsides, m_fields, this->m_options.getReal("quA"),
                     this->m_options.getInt("quB"),
-                    dv == dirichlet::l2Projection ? GSGPU_DIRICHLET_L2 : GSGPU_DIRICHLET_INTERPOLATION);
+                    dv == dirichlet::l2Projection ? GSGPU_DIRICHLET_L2 : GSGPU_DIRICHLET_INTERPOLATION, nsides);
         check(gsgpu_set_problem(m_ctx, &m_pack.prob));
         check(gsgpu_refresh(m_ctx));
     }

@@ -37,10 +37,16 @@ typedef struct gsgpu_context gsgpu_context;
  * Dirichlet sides are eliminated (dirichlet::elimination) with values by interpolation
  * (dirichlet::interpolation, gsAssembler.hpp:314-390) or L2 projection (dirichlet::l2Projection,
  * gsAssembler.hpp:392-534) of the exact solution u.
- * Coefficient, source and exact solution are closed forms evaluated on the device:
+ * Neumann sides add the boundary integral of gsVisitorNeumann (gsPoissonAssembler.hpp:59,
+ * gsCDRAssembler.hpp:58) to the load vector; the sides that are neither Dirichlet, Neumann nor
+ * interface sides are natural (zero-flux) boundaries, as in the reference.
+ * Coefficient, source, exact solution and Neumann data are closed forms evaluated on the device:
  *   g(x) = kappa_scale * sum_m kappa_amp[m] cos(pi kappa_k[m].x + kappa_phase[m])
  *   kappa = exp(kappa_alpha * g) if kappa_fourier else kappa_const
- *   u = prod_i sin(ufreq pi x_i),  f = -div(kappa grad u). */
+ *   u = prod_i sin(ufreq pi x_i),  f = -div(kappa grad u)
+ *   Neumann data on side s of direction k = (s-1)/2: h(x) = sgn(s) kappa(x) du/dx_k(x),
+ *   sgn = -1 on the lower side (s odd), +1 on the upper side: the flux kappa grad u . n of the
+ *   manufactured solution wherever the side lies in a plane x_k = const. */
 typedef struct {
     int dim;
     int npatches;
@@ -68,6 +74,8 @@ typedef struct {
     int dirichlet_strategy; /* GSGPU_DIRICHLET_INTERPOLATION (0) or GSGPU_DIRICHLET_L2 (1): the
                                "DirichletValues" option, dirichlet::interpolation or
                                dirichlet::l2Projection (gsAssembler.hpp:231-534) */
+    int nneumann;
+    const int* neumann;    /* 2 ints per side: patch side (condition_type::neumann) */
 } gsgpu_problem;
 #define GSGPU_DIRICHLET_INTERPOLATION 0
 #define GSGPU_DIRICHLET_L2 1

@@ -304,7 +304,7 @@ struct Csr {
 struct Oracle {
     int dim = 2;
     std::vector<PatchData> patches;
-    std::vector<int> ifaces, dsides;
+    std::vector<int> ifaces, dsides, nsides;
     Fields F;
     double quA = 1.0;
     int quB = 1;
@@ -411,6 +411,7 @@ struct Oracle {
         nlocal = off;
         ifaces.assign(pr->interfaces, pr->interfaces + 4 * pr->ninterfaces);
         dsides.assign(pr->dirichlet, pr->dirichlet + 2 * pr->ndirichlet);
+        if (pr->nneumann > 0) nsides.assign(pr->neumann, pr->neumann + 2 * pr->nneumann);
         F.dim = dim;
         F.fourier = pr->kappa_fourier;
         F.kconst = pr->kappa_const;
@@ -659,6 +660,102 @@ struct Oracle {
         }
     }
 
+    // Neumann boundary integrals (gsVisitorNeumann, src/gsAssembler/gsVisitorNeumann.h:60-135, pushed
+    // after the volume terms by gsPoissonAssembler.hpp:59 / gsCDRAssembler.hpp:58; the boundary
+    // element loop of gsAssembler::apply, gsAssembler.h:668-722): on every element of the side,
+    // quA p + quB Gauss points in each side direction and one node of weight 1 in the fixed one
+    // (gsQuadrature::get with fixDir, gsQuadrature.h:153-170; gsQuadRule::mapTo, gsQuadRule.h:177-200);
+    // weight |n| with n the outer normal of outerNormal (gsAssembler.h:79-130), whose components
+    // are the signed minors of J without the fixed direction's column; data
+    // h = sgn kappa du/dx_dir; the element's local vector is added to the free rows
+    // (gsSparseSystem::pushToRhs)
+    void neumannRhs() {
+        for (size_t si = 0; si < nsides.size(); si += 2) {
+            const PatchData& P = patches[nsides[si]];
+            const int side = nsides[si + 1];
+            const int dir = (side - 1) / 2, par = (side - 1) % 2;
+            const double sgn = par ? 1.0 : -1.0;
+            std::vector<int> odirs;
+            for (int k = 0; k < dim; ++k) if (k != dir) odirs.push_back(k);
+            const double fixv = par ? P.b[dir].t.back() : P.b[dir].t.front();
+            const int no = int(odirs.size());
+            std::vector<std::vector<double>> qx(no), qw(no);
+            for (int o = 0; o < no; ++o) gaussRule(nq(P.b[odirs[o]].p), qx[o], qw[o]);
+            const int ne0 = P.b[odirs[0]].nelem(), ne1 = no > 1 ? P.b[odirs[1]].nelem() : 1;
+            const int na = (P.b[0].p + 1) * (P.b[1].p + 1) * (dim == 3 ? P.b[2].p + 1 : 1);
+            for (int e1 = 0; e1 < ne1; ++e1)
+                for (int e0 = 0; e0 < ne0; ++e0) {
+                    const int el[2] = {e0, e1};
+                    std::vector<double> loc(na, 0.0);
+                    std::vector<int> act(na);
+                    const int nq0 = int(qx[0].size()), nq1 = no > 1 ? int(qx[1].size()) : 1;
+                    for (int q1 = 0; q1 < nq1; ++q1)
+                        for (int q0 = 0; q0 < nq0; ++q0) {
+                            const int qq[2] = {q0, q1};
+                            double xi[3] = {0, 0, 0};
+                            xi[dir] = fixv;
+                            double w = 1.0;
+                            for (int o = 0; o < no; ++o) {
+                                const Basis1D& B = P.b[odirs[o]];
+                                const double a = B.breaks[el[o]], b = B.breaks[el[o] + 1];
+                                const double h = 0.5 * (b - a);
+                                xi[odirs[o]] = a + h * (qx[o][qq[o]] + 1.0);
+                                w *= h * qw[o][qq[o]];
+                            }
+                            double x[3], J[9];
+                            geoEval(P, xi, x, J);
+                            // |n|: minors of J with row i and column dir removed
+                            double nn = 0.0;
+                            for (int i = 0; i < dim; ++i) {
+                                double mnr;
+                                if (dim == 2) {
+                                    mnr = J[(1 - i) * 2 + (1 - dir)];
+                                } else {
+                                    int r[2], c[2], nr = 0, nc = 0;
+                                    for (int k = 0; k < 3; ++k) {
+                                        if (k != i) r[nr++] = k;
+                                        if (k != dir) c[nc++] = k;
+                                    }
+                                    mnr = J[r[0] * 3 + c[0]] * J[r[1] * 3 + c[1]] - J[r[1] * 3 + c[0]] * J[r[0] * 3 + c[1]];
+                                }
+                                nn += mnr * mnr;
+                            }
+                            const double wk = w * std::sqrt(nn);
+                            double kap, ff, u;
+                            F.eval(x, kap, ff, u);
+                            const double wf = F.ufreq * M_PI;
+                            double du = wf;
+                            for (int i = 0; i < dim; ++i) du *= i == dir ? std::cos(wf * x[i]) : std::sin(wf * x[i]);
+                            const double hN = sgn * kap * du;
+                            int sp[3], first[3];
+                            double v[3][16], buf[64];
+                            for (int k = 0; k < dim; ++k) {
+                                const Basis1D& B = P.b[k];
+                                sp[k] = B.span(xi[k]);
+                                first[k] = sp[k] - B.p;
+                                B.ders(sp[k], xi[k], 0, buf);
+                                for (int r = 0; r <= B.p; ++r) v[k][r] = buf[r];
+                            }
+                            int a = 0;
+                            const int p2 = dim == 3 ? P.b[2].p : 0;
+                            for (int c = 0; c <= p2; ++c)
+                                for (int b = 0; b <= P.b[1].p; ++b)
+                                    for (int aa = 0; aa <= P.b[0].p; ++aa, ++a) {
+                                        act[a] = first[0] + aa +
+                                                 P.b[0].n() * (first[1] + b + (dim == 3 ? P.b[1].n() * (first[2] + c) : 0));
+                                        double val = v[0][aa] * v[1][b];
+                                        if (dim == 3) val *= v[2][c];
+                                        loc[a] += wk * val * hN;
+                                    }
+                        }
+                    for (int a = 0; a < na; ++a) {
+                        const int gi = map.index[P.offset + act[a]];
+                        if (gi < map.freeSize) rhs[gi] += loc[a];
+                    }
+                }
+        }
+    }
+
     // Dirichlet values by interpolation at the boundary basis anchors
     // (gsAssembler::computeDirichletDofsIntpl, src/gsAssembler/gsAssembler.hpp:314-390, with
     //  gsTensorBasis::interpolateAtAnchors, gsTensorBasis.hpp:906-960)
@@ -869,6 +966,7 @@ struct Oracle {
                 }
             }
         }
+        if (maxElems < 0) neumannRhs();
         assembled = true;
         return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }

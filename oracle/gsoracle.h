@@ -38,6 +38,8 @@ typedef struct {
     double quA;
     int quB;
     int dirichlet_l2;           /* 1: Dirichlet values by L2 projection, 0: by interpolation */
+    int nneumann;
+    const int* neumann;         /* 2 per side: patch side (condition_type::neumann) */
 } orc_problem;
 
 void* orc_create(const orc_problem* prob);

@@ -34,6 +34,7 @@ class _Problem(C.Structure):
         ("kappa_scale", C.c_double), ("kappa_nmodes", C.c_int), ("kappa_amp", C.POINTER(C.c_double)),
         ("kappa_k", C.POINTER(C.c_int)), ("kappa_phase", C.POINTER(C.c_double)),
         ("ufreq", C.c_int), ("quA", C.c_double), ("quB", C.c_int), ("dirichlet_l2", C.c_int),
+        ("nneumann", C.c_int), ("neumann", C.POINTER(C.c_int)),
     ]
 
 
@@ -94,6 +95,7 @@ class OracleProblem:
             gdegree=np.array(gdeg, np.int32), gnknots=np.array(gnk, np.int32), gknots=np.array(gkn, np.float64),
             coefs=np.concatenate(co), ifaces=np.array(prob.interfaces, np.int32).reshape(-1),
             dirichlet=np.array(prob.dirichlet, np.int32).reshape(-1),
+            neumann=np.array(getattr(prob, "neumann", []), np.int32).reshape(-1),
             amp=np.ascontiguousarray(prob.kappa_amp, np.float64), kk=np.ascontiguousarray(prob.kappa_k, np.int32).reshape(-1),
             phase=np.ascontiguousarray(prob.kappa_phase, np.float64),
         )
@@ -112,6 +114,7 @@ class OracleProblem:
         s.kappa_amp = _ptr(a["amp"], C.c_double); s.kappa_k = _ptr(a["kk"], C.c_int); s.kappa_phase = _ptr(a["phase"], C.c_double)
         s.ufreq = prob.ufreq; s.quA = prob.quA; s.quB = prob.quB
         s.dirichlet_l2 = 1 if getattr(prob, "dirichlet_l2", False) else 0
+        s.nneumann = len(a["neumann"]) // 2; s.neumann = _ptr(a["neumann"], C.c_int)
         self._s = s
         self.prob = prob
         self.h = lib().orc_create(C.byref(s))

@@ -55,6 +55,7 @@ struct Spec {
     std::vector<Patch> patches;
     std::vector<std::array<int, 4>> ifaces;
     std::vector<std::array<int, 2>> dirichlet;
+    std::vector<std::array<int, 2>> neumann;
     bool kappa_fourier = false;
     double kappa_const = 1.0, kappa_alpha = 0.0, kappa_scale = 0.0;
     std::vector<Mode> modes;
@@ -93,6 +94,8 @@ Spec readSpec(const std::string& path) {
             std::array<int, 4> a; in >> a[0] >> a[1] >> a[2] >> a[3]; s.ifaces.push_back(a);
         } else if (tok == "dirichlet") {
             std::array<int, 2> a; in >> a[0] >> a[1]; s.dirichlet.push_back(a);
+        } else if (tok == "neumann") {
+            std::array<int, 2> a; in >> a[0] >> a[1]; s.neumann.push_back(a);
         } else if (tok == "kappa_const") { in >> s.kappa_const; s.kappa_fourier = false; }
         else if (tok == "kappa_fourier") {
             int nm; in >> s.kappa_alpha >> s.kappa_scale >> nm; s.kappa_fourier = true;
@@ -191,6 +194,28 @@ public:
         for (index_t c = 0; c < u.cols(); ++c) { double k, f, uu; F.eval(u.col(c).data(), k, f, uu); r(0, c) = uu; }
     }
 };
+// Neumann data of side s (direction k = (s-1)/2): sgn kappa du/dx_k, sgn = -1 on the lower side
+class NeumannFunc : public gsFunction<real_t> {
+    Fields F;
+    int k;
+    double sgn;
+public:
+    NeumannFunc(const Spec& s, int side) : F{s}, k((side - 1) / 2), sgn((side - 1) % 2 ? 1.0 : -1.0) {}
+    GISMO_CLONE_FUNCTION(NeumannFunc)
+    short_t domainDim() const override { return F.s.dim; }
+    short_t targetDim() const override { return 1; }
+    void eval_into(const gsMatrix<real_t>& u, gsMatrix<real_t>& r) const override {
+        r.resize(1, u.cols());
+        const double w = F.s.ufreq * M_PI;
+        for (index_t c = 0; c < u.cols(); ++c) {
+            double kap, f, uu;
+            F.eval(u.col(c).data(), kap, f, uu);
+            double du = w;
+            for (int i = 0; i < F.s.dim; ++i) du *= i == k ? std::cos(w * u(i, c)) : std::sin(w * u(i, c));
+            r(0, c) = sgn * kap * du;
+        }
+    }
+};
 class ConstFunc : public gsFunction<real_t> {
     int dd, td; double v;
 public:
@@ -253,6 +278,11 @@ int main(int argc, char** argv) {
     gsBoundaryConditions<> bc;
     for (const auto& d : s.dirichlet)
         bc.addCondition(d[0], boxSide(d[1]), condition_type::dirichlet, &solF);
+    std::vector<std::unique_ptr<NeumannFunc>> neuF;
+    for (const auto& d : s.neumann) {
+        neuF.emplace_back(new NeumannFunc(s, d[1]));
+        bc.addCondition(d[0], boxSide(d[1]), condition_type::neumann, neuF.back().get());
+    }
 
     std::unique_ptr<gsAssembler<>> A;
     const bool poisson = !s.kappa_fourier && s.kappa_const == 1.0;

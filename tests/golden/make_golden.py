@@ -58,6 +58,15 @@ def cases():
     pr.solver = "cg"
     pr.tol = 1e-8
     out["cubegrid2_p2_n4_cg"] = pr
+    # mixed boundary conditions: Dirichlet on the lower sides, Neumann (gsVisitorNeumann) on the
+    # upper ones
+    out["square_p2_n16_neu"] = P.mixed_boundary(P.square_poisson(16, 2))
+    out["disp2d_p3_10x8_neu"] = P.mixed_boundary(P.displaced_single_patch(2, (10, 8), (3, 3), 21, 0.05, ufreq=2))
+    out["disp3d_p232_4x5x3_neu"] = P.mixed_boundary(P.displaced_single_patch(3, (4, 5, 3), (2, 3, 2), 8, 0.04))
+    pr = P.mixed_boundary(P.cube_grid(n=2, n_elem=3, p=2, seed=6, kappa_modes=8))
+    pr.solver = "cg"
+    pr.tol = 1e-8
+    out["cubegrid2_p2_n3_neu"] = pr
     return out
 
 
