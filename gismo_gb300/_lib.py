@@ -16,6 +16,7 @@ EXPORTS = [
     "gsgpu_set_profiling", "gsgpu_spmv_stats", "gsgpu_cg_jacobi_noalloc", "gsgpu_set_batch", "gsgpu_batch_info",
     "gsgpu_batch_l2_error", "gsgpu_server_create", "gsgpu_server_submit", "gsgpu_server_wait",
     "gsgpu_server_last_error", "gsgpu_server_destroy", "gsgpu_apply", "gsgpu_mg_apply", "gsgpu_set_fixed_dofs",
+    "gsgpu_h1_error", "gsgpu_batch_h1_error",
 ]
 
 OK, ERR_INVALID, ERR_CUDA, ERR_BUDGET, ERR_NOT_CONVERGED, ERR_JACOBIAN, ERR_STATE, ERR_TIMEOUT = range(8)
@@ -90,6 +91,8 @@ def lib() -> C.CDLL:
         L.gsgpu_dof_map.argtypes = [vp, vp]
         L.gsgpu_solve.argtypes = [vp, C.POINTER(SolverOpts), vp, C.POINTER(SolveInfo)]
         L.gsgpu_l2_error.argtypes = [vp, C.POINTER(C.c_double)]
+        L.gsgpu_h1_error.argtypes = [vp, C.POINTER(C.c_double)]
+        L.gsgpu_batch_h1_error.argtypes = [vp, vp]
         L.gsgpu_set_batch.argtypes = [vp, C.c_int, vp]
         L.gsgpu_batch_info.argtypes = [vp, vp, vp, vp]
         L.gsgpu_batch_l2_error.argtypes = [vp, vp]

@@ -184,6 +184,12 @@ class GpuPoissonAssembler:
         self._check(self.L.gsgpu_l2_error(self.h, C.byref(v)))
         return v.value
 
+    def h1_error(self) -> float:
+        """gsField::distanceH1 (H1 seminorm of the error) of the last solution."""
+        v = C.c_double()
+        self._check(self.L.gsgpu_h1_error(self.h, C.byref(v)))
+        return v.value
+
     def min_jacobian(self) -> float:
         v = C.c_double()
         self._check(self.L.gsgpu_min_jacobian(self.h, C.byref(v)))
@@ -270,6 +276,11 @@ class GpuPoissonBatch(GpuPoissonAssembler):
     def l2_errors(self) -> np.ndarray:
         out = np.zeros(len(self.problems), np.float64)
         self._check(self.L.gsgpu_batch_l2_error(self.h, out.ctypes.data))
+        return out
+
+    def h1_errors(self) -> np.ndarray:
+        out = np.zeros(len(self.problems), np.float64)
+        self._check(self.L.gsgpu_batch_h1_error(self.h, out.ctypes.data))
         return out
 
 

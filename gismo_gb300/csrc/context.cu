@@ -595,7 +595,7 @@ void Context::applyMatrix(const double* x, double* y) {
 
 // gsField::distanceL2 of the last solution: the geometry stages are re-run in FP64 (after a
 // mixed-precision assembly their buffers hold double-float values), then one quadrature kernel
-std::vector<double> Context::l2PerPatch() {
+std::vector<double> Context::l2PerPatch(bool h1) {
     if (!solved) throw StateError("l2_error() before solve()");
     cudaStream_t s = stream;
     // after a mixed assembly the geometry table holds double-float values: rebuild it in FP64
@@ -611,7 +611,7 @@ std::vector<double> Context::l2PerPatch() {
     allocN(arena, coef, nlocal);
     allocN(arena, part, nblk);
     launch::solutionCoefs(nlocal, dIndex, map.freeSize, dX, dDdof, coef, s);
-    launch::l2Partials(dPatches, tabPoint.d, nblk, dFields, dY1, dY2, dGtab, dIbuf, dWq, dTab, coef, part, s);
+    launch::l2Partials(dPatches, tabPoint.d, nblk, dFields, dY1, dY2, dGtab, dIbuf, dWq, dTab, coef, part, h1, s);
     std::vector<double> h(nblk);
     GSGPU_CUDA_TRY(cudaGetLastError());
     GSGPU_CUDA_TRY(cudaMemcpyAsync(h.data(), part, nblk * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -624,9 +624,9 @@ std::vector<double> Context::l2PerPatch() {
     return acc;
 }
 
-double Context::l2Error() {
+double Context::l2Error(bool h1) {
     double acc = 0.0;
-    for (double v : l2PerPatch()) acc += v;
+    for (double v : l2PerPatch(h1)) acc += v;
     return std::sqrt(acc);
 }
 
@@ -1106,6 +1106,15 @@ int gsgpu_batch_l2_error(gsgpu_context* ctx, double* err) {
     });
 }
 
+int gsgpu_batch_h1_error(gsgpu_context* ctx, double* err) {
+    if (!err) return GSGPU_ERR_INVALID;
+    return guarded(ctx, [&] {
+        if (!ctx->c.batch) throw gsgpu::StateError("batch_h1_error() on a context without a batch");
+        const std::vector<double> sq = ctx->c.l2PerPatch(true);
+        for (size_t j = 0; j < sq.size(); ++j) err[j] = std::sqrt(sq[j]);
+    });
+}
+
 int gsgpu_refresh(gsgpu_context* ctx) { return guarded(ctx, [&] { ctx->c.refresh(); }); }
 
 int gsgpu_set_coefs(gsgpu_context* ctx, const double* coefs) {
@@ -1242,7 +1251,12 @@ int gsgpu_mg_apply(gsgpu_context* ctx, const gsgpu_solver_opts* opts, const doub
 
 int gsgpu_l2_error(gsgpu_context* ctx, double* err) {
     if (!err) return GSGPU_ERR_INVALID;
-    return guarded(ctx, [&] { *err = ctx->c.l2Error(); });
+    return guarded(ctx, [&] { *err = ctx->c.l2Error(false); });
+}
+
+int gsgpu_h1_error(gsgpu_context* ctx, double* err) {
+    if (!err) return GSGPU_ERR_INVALID;
+    return guarded(ctx, [&] { *err = ctx->c.l2Error(true); });
 }
 
 int gsgpu_stream(gsgpu_context* ctx, void** stream) {

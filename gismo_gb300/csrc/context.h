@@ -188,8 +188,8 @@ struct Context {
     void mgSetup(int levels);
     void mgAssemble(bool mixed);
     void solveMG(const gsgpu_solver_opts& o, gsgpu_solve_info& info);
-    double l2Error();
-    std::vector<double> l2PerPatch();  // squared L2 error per patch
+    double l2Error(bool h1);  // sqrt of the summed squared errors (h1: the H1 seminorm)
+    std::vector<double> l2PerPatch(bool h1 = false);  // squared L2 (h1: H1 seminorm) error per patch
     // batches of independent problems (one patch each): segment = problem
     bool batch = false;
     std::vector<int> segRow;  // free-dof offsets per problem (nseg + 1)

@@ -59,12 +59,13 @@ void rhsRows(int n, const double* lvec, const uint32_t* lptr, const uint32_t* li
              cudaStream_t s);
 
 // discrete L2 error: solution coefficients per patch-local dof, then per-block partial sums of
-// (u_h - u)^2 w |det J| over the quadrature points (tabPoint blocks)
+// (u_h - u)^2 w |det J| over the quadrature points (tabPoint blocks); h1: the H1 seminorm
+// integrand |grad u_h - grad u|^2 w |det J| instead
 void solutionCoefs(long long nlocal, const int* index, int nfree, const double* x, const double* ddof, double* coef,
                    cudaStream_t s);
 void l2Partials(const DevPatch* P, const BlkEnt* tab, long long nblk, const dev::FieldConst<double>* F,
                 const double* Y1, const double* Y2, const double* gtab, const int* ibuf, const double* wq,
-                const double* btab, const double* coef, double* part, cudaStream_t s);
+                const double* btab, const double* coef, double* part, bool h1, cudaStream_t s);
 
 // Neumann boundary integrals: w |n| h per face quadrature point (before the geometry table turns
 // into double-float values), then per dof on a Neumann side its sums added to the load vector

@@ -3,6 +3,8 @@
 // Gauss quadrature of (u_h - u)^2 |det J| over every element of every patch, with the assembly's
 // (p+1)^d rule. u_h sums the solution coefficients of the active basis functions (free dofs from
 // x, eliminated dofs from the Dirichlet values); u is the closed-form manufactured solution.
+// The H1 form (gsField::distanceH1, gsField.hpp:44-60, parametric solution field against the
+// physical exact function) integrates |J^-T grad_xi u_h - grad u|^2 |det J| with the same rule.
 #include "kernels.h"
 
 namespace gsgpu {
@@ -20,6 +22,7 @@ __global__ void __launch_bounds__(kBlock) k_solcoef(long long nlocal, const int*
     coef[i] = g < nfree ? x[g] : ddof[g - nfree];
 }
 
+template <bool H1>
 __global__ void __launch_bounds__(kBlock) k_l2(const DevPatch* __restrict__ P, const BlkEnt* __restrict__ tab,
                                                const dev::FieldConst<double>* __restrict__ F,
                                                const double* __restrict__ Y1, const double* __restrict__ Y2,
@@ -55,34 +58,100 @@ __global__ void __launch_bounds__(kBlock) k_l2(const DevPatch* __restrict__ P, c
             b[k] = btab + D.toff[k] + (long long)g[k] * 2 * (pk[k] + 1);
         }
         const double* c = coef + D.lvec_off;
-        double uh = 0.0;
-        if (d == 3) {
-            for (int s2 = 0; s2 <= pk[2]; ++s2) {
-                double a1 = 0.0;
+        if (!H1) {
+            double uh = 0.0;
+            if (d == 3) {
+                for (int s2 = 0; s2 <= pk[2]; ++s2) {
+                    double a1 = 0.0;
+                    for (int s1 = 0; s1 <= pk[1]; ++s1) {
+                        const double* cr = c + ((long long)(f[2] + s2) * D.n[1] + f[1] + s1) * D.n[0] + f[0];
+                        double a0 = 0.0;
+                        for (int s0 = 0; s0 <= pk[0]; ++s0) a0 += b[0][s0] * cr[s0];
+                        a1 += b[1][s1] * a0;
+                    }
+                    uh += b[2][s2] * a1;
+                }
+            } else {
                 for (int s1 = 0; s1 <= pk[1]; ++s1) {
-                    const double* cr = c + ((long long)(f[2] + s2) * D.n[1] + f[1] + s1) * D.n[0] + f[0];
+                    const double* cr = c + (long long)(f[1] + s1) * D.n[0] + f[0];
                     double a0 = 0.0;
                     for (int s0 = 0; s0 <= pk[0]; ++s0) a0 += b[0][s0] * cr[s0];
-                    a1 += b[1][s1] * a0;
+                    uh += b[1][s1] * a0;
                 }
-                uh += b[2][s2] * a1;
             }
+            double u = 1.0;
+            for (int k = 0; k < d; ++k) {
+                double sn, cs;
+                sincospi(double(F[D.field_id].ufreq) * x[k], &sn, &cs);
+                u *= sn;
+            }
+            const double e = uh - u;
+            v = e * e * w * fabs(det);
         } else {
-            for (int s1 = 0; s1 <= pk[1]; ++s1) {
-                const double* cr = c + (long long)(f[1] + s1) * D.n[0] + f[0];
-                double a0 = 0.0;
-                for (int s0 = 0; s0 <= pk[0]; ++s0) a0 += b[0][s0] * cr[s0];
-                uh += b[1][s1] * a0;
+            // parametric gradient of u_h: derivative factor in one direction, values in the others
+            // (b[k][p+1+s] holds the derivative of function s)
+            double gx[3] = {0, 0, 0};
+            if (d == 3) {
+                for (int s2 = 0; s2 <= pk[2]; ++s2) {
+                    double a1[3] = {0, 0, 0};
+                    for (int s1 = 0; s1 <= pk[1]; ++s1) {
+                        const double* cr = c + ((long long)(f[2] + s2) * D.n[1] + f[1] + s1) * D.n[0] + f[0];
+                        double v0 = 0.0, d0 = 0.0;
+                        for (int s0 = 0; s0 <= pk[0]; ++s0) {
+                            v0 += b[0][s0] * cr[s0];
+                            d0 += b[0][pk[0] + 1 + s0] * cr[s0];
+                        }
+                        a1[0] += b[1][s1] * d0;
+                        a1[1] += b[1][pk[1] + 1 + s1] * v0;
+                        a1[2] += b[1][s1] * v0;
+                    }
+                    gx[0] += b[2][s2] * a1[0];
+                    gx[1] += b[2][s2] * a1[1];
+                    gx[2] += b[2][pk[2] + 1 + s2] * a1[2];
+                }
+            } else {
+                for (int s1 = 0; s1 <= pk[1]; ++s1) {
+                    const double* cr = c + (long long)(f[1] + s1) * D.n[0] + f[0];
+                    double v0 = 0.0, d0 = 0.0;
+                    for (int s0 = 0; s0 <= pk[0]; ++s0) {
+                        v0 += b[0][s0] * cr[s0];
+                        d0 += b[0][pk[0] + 1 + s0] * cr[s0];
+                    }
+                    gx[0] += b[1][s1] * d0;
+                    gx[1] += b[1][pk[1] + 1 + s1] * v0;
+                }
             }
+            // physical gradient J^-T grad_xi = cof(J) grad_xi / det J
+            double cof[3][3];
+            if (d == 3) {
+                for (int m = 0; m < 3; ++m)
+                    for (int k = 0; k < 3; ++k) {
+                        const int m1 = (m + 1) % 3, m2 = (m + 2) % 3, k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+                        cof[m][k] = J[m1][k1] * J[m2][k2] - J[m1][k2] * J[m2][k1];
+                    }
+            } else {
+                cof[0][0] = J[1][1];
+                cof[0][1] = -J[1][0];
+                cof[1][0] = -J[0][1];
+                cof[1][1] = J[0][0];
+            }
+            // exact gradient: freq pi cos(freq pi x_j) prod_{i != j} sin(freq pi x_i)
+            const int fq = F[D.field_id].ufreq;
+            double sn[3], cs[3];
+            for (int k = 0; k < d; ++k) sincospi(double(fq) * x[k], &sn[k], &cs[k]);
+            double e2 = 0.0;
+            for (int m = 0; m < d; ++m) {
+                double gh = 0.0;
+                for (int k = 0; k < d; ++k) gh += cof[m][k] * gx[k];
+                gh /= det;
+                double gu = F[D.field_id].wpi * cs[m];
+                for (int i = 0; i < d; ++i)
+                    if (i != m) gu *= sn[i];
+                const double e = gh - gu;
+                e2 += e * e;
+            }
+            v = e2 * w * fabs(det);
         }
-        double u = 1.0;
-        for (int k = 0; k < d; ++k) {
-            double sn, cs;
-            sincospi(double(F[D.field_id].ufreq) * x[k], &sn, &cs);
-            u *= sn;
-        }
-        const double e = uh - u;
-        v = e * e * w * fabs(det);
     }
     // block sum in a fixed order
     __shared__ double ws[kBlock / 32];
@@ -107,8 +176,10 @@ void solutionCoefs(long long nlocal, const int* index, int nfree, const double* 
 
 void l2Partials(const DevPatch* P, const BlkEnt* tab, long long nblk, const dev::FieldConst<double>* F,
                 const double* Y1, const double* Y2, const double* gtab, const int* ibuf, const double* wq,
-                const double* btab, const double* coef, double* part, cudaStream_t s) {
-    if (nblk > 0) k_l2<<<unsigned(nblk), kBlock, 0, s>>>(P, tab, F, Y1, Y2, gtab, ibuf, wq, btab, coef, part);
+                const double* btab, const double* coef, double* part, bool h1, cudaStream_t s) {
+    if (nblk <= 0) return;
+    if (h1) k_l2<true><<<unsigned(nblk), kBlock, 0, s>>>(P, tab, F, Y1, Y2, gtab, ibuf, wq, btab, coef, part);
+    else k_l2<false><<<unsigned(nblk), kBlock, 0, s>>>(P, tab, F, Y1, Y2, gtab, ibuf, wq, btab, coef, part);
 }
 
 }  // namespace launch

@@ -163,6 +163,9 @@ int gsgpu_apply(gsgpu_context* ctx, const double* x, double* y);
 int gsgpu_mg_apply(gsgpu_context* ctx, const gsgpu_solver_opts* opts, const double* r, double* z);
 /* gsField::distanceL2 of the last solution against u (gsField.hpp:23-41) */
 int gsgpu_l2_error(gsgpu_context* ctx, double* err);
+/* gsField::distanceH1 of the last solution against u (gsField.hpp:44-60): the H1 seminorm
+ * sqrt(int |grad u_h - grad u|^2), with the assembly's quadrature rule */
+int gsgpu_h1_error(gsgpu_context* ctx, double* err);
 
 /* Batches of independent problems. No counterpart in the reference, where each problem is its own
  * gsPoissonAssembler + gsConjugateGradient run. `count` single-patch problems (each with its own
@@ -179,6 +182,8 @@ int gsgpu_set_batch(gsgpu_context* ctx, int count, const gsgpu_problem* problems
 int gsgpu_batch_info(gsgpu_context* ctx, int* offsets, int* iterations, double* relres);
 /* per problem: gsField::distanceL2 of the last solution (count values) */
 int gsgpu_batch_l2_error(gsgpu_context* ctx, double* err);
+/* per problem: gsField::distanceH1 of the last solution (count values) */
+int gsgpu_batch_h1_error(gsgpu_context* ctx, double* err);
 
 /* Request server (continuous batching). No counterpart in the reference, which has no serving
  * layer: a caller there runs one gsPoissonAssembler + gsConjugateGradient per request. Requests

@@ -1024,6 +1024,46 @@ struct Oracle {
 
     // L2 error of the discrete solution against the exact one (gsField::distanceL2,
     // src/gsCore/gsField.hpp:23-41, gsAssembler::constructSolution gsAssembler.hpp:536-581)
+    // gsField::distanceH1 (src/gsCore/gsField.hpp:44-60) for the parametric solution field against
+    // the physical exact function: sqrt(sum w |det J| |J^-T grad_xi u_h - grad u|^2)
+    double h1error(const double* x) const {
+        double acc = 0;
+        const long long ne = totalElems();
+#pragma omp parallel for reduction(+ : acc) schedule(static)
+        for (long long ge = 0; ge < ne; ++ge) {
+            std::vector<double> pts, wts, N, dN;
+            std::vector<int> act;
+            const Elem E = elemAt(ge);
+            const PatchData& P = patches[E.patch];
+            int q[3];
+            elementRule(P, E, pts, wts, q);
+            const int nqt = int(wts.size());
+            elementBasis(P, E, pts, nqt, act, N, dN);
+            for (int qi = 0; qi < nqt; ++qi) {
+                double xx[3], J[9], G[9];
+                geoEval(P, &pts[size_t(qi) * dim], xx, J);
+                invT(dim, J, G);
+                double gxi[3] = {0, 0, 0};
+                for (size_t a = 0; a < act.size(); ++a) {
+                    const int gi = map.index[P.offset + act[a]];
+                    const double c = gi < map.freeSize ? x[gi] : ddof[gi - map.freeSize];
+                    for (int n = 0; n < dim; ++n) gxi[n] += c * dN[(a * dim + n) * nqt + qi];
+                }
+                const double w = F.ufreq * M_PI;
+                double e2 = 0;
+                for (int m = 0; m < dim; ++m) {
+                    double gh = 0;
+                    for (int n = 0; n < dim; ++n) gh += G[m * dim + n] * gxi[n];
+                    double gu = w;
+                    for (int i = 0; i < dim; ++i) gu *= i == m ? std::cos(w * xx[i]) : std::sin(w * xx[i]);
+                    e2 += (gh - gu) * (gh - gu);
+                }
+                acc += e2 * wts[qi] * std::fabs(det(dim, J));
+            }
+        }
+        return std::sqrt(acc);
+    }
+
     double l2error(const double* x) const {
         double acc = 0;
         const long long ne = totalElems();
@@ -1403,6 +1443,7 @@ double orc_solve_mg(void* h, double tol, int maxit, int levels, int npre, int np
                                             *relres);
 }
 double orc_l2_error(void* h, const double* x) { return static_cast<Oracle*>(h)->l2error(x); }
+double orc_h1_error(void* h, const double* x) { return static_cast<Oracle*>(h)->h1error(x); }
 void orc_gauss(int n, double* nodes, double* weights) {
     std::vector<double> x, w;
     gaussRule(n, x, w);

@@ -61,6 +61,8 @@ double orc_solve_cg(void* h, double tol, int maxit, double* x, int* iters, doubl
 double orc_solve_mg(void* h, double tol, int maxit, int levels, int npre, int npost, double damping,
                     int cycles, double cgc, double* x, int* iters, double* relres);
 double orc_l2_error(void* h, const double* x);
+/* gsField::distanceH1: H1 seminorm of u_h - u */
+double orc_h1_error(void* h, const double* x);
 /* Gauss-Legendre rule on [-1,1] (ascending nodes) */
 void orc_gauss(int n, double* nodes, double* weights);
 

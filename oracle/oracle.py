@@ -58,6 +58,8 @@ def _lib():
                                  C.c_double, C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)]
     lib.orc_l2_error.restype = C.c_double
     lib.orc_l2_error.argtypes = [vp, C.c_void_p]
+    lib.orc_h1_error.restype = C.c_double
+    lib.orc_h1_error.argtypes = [vp, C.c_void_p]
     lib.orc_gauss.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
     return lib
 
@@ -172,6 +174,10 @@ class OracleProblem:
     def l2_error(self, x):
         x = np.ascontiguousarray(x, np.float64)
         return lib().orc_l2_error(self.h, x.ctypes.data)
+
+    def h1_error(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        return lib().orc_h1_error(self.h, x.ctypes.data)
 
 
 def gauss(n: int):

@@ -193,6 +193,18 @@ public:
         r.resize(1, u.cols());
         for (index_t c = 0; c < u.cols(); ++c) { double k, f, uu; F.eval(u.col(c).data(), k, f, uu); r(0, c) = uu; }
     }
+    // the exact gradient (gsField::distanceH1 differentiates the exact function through this)
+    void deriv_into(const gsMatrix<real_t>& u, gsMatrix<real_t>& r) const override {
+        const int d = F.s.dim;
+        const double w = F.s.ufreq * M_PI;
+        r.resize(d, u.cols());
+        for (index_t c = 0; c < u.cols(); ++c)
+            for (int j = 0; j < d; ++j) {
+                double g = w;
+                for (int i = 0; i < d; ++i) g *= i == j ? std::cos(w * u(i, c)) : std::sin(w * u(i, c));
+                r(j, c) = g;
+            }
+    }
 };
 // Neumann data of side s (direction k = (s-1)/2): sgn kappa du/dx_k, sgn = -1 on the lower side
 class NeumannFunc : public gsFunction<real_t> {
@@ -311,7 +323,7 @@ int main(int argc, char** argv) {
     dump(out + "/ddof.f64", A->fixedDofs().data(), size_t(A->fixedDofs().rows()));
 
     int iters = 0;
-    double err = 0, l2 = 0;
+    double err = 0, l2 = 0, h1 = 0;
     double tsolve = 0;
     if (solve) {
         gsMatrix<> x;
@@ -356,11 +368,12 @@ int main(int argc, char** argv) {
         A->constructSolution(x, sol);
         gsField<> uh(mp, sol);
         l2 = uh.distanceL2(solF, mb, false);
+        h1 = uh.distanceH1(solF, mb, false);
     }
     std::ofstream info(out + "/info.txt");
     info.precision(17);
     info << "free " << A->numDofs() << "\nnnz " << K.nonZeros() << "\nboundary " << map.boundarySize()
-         << "\niters " << iters << "\nerror " << err << "\nl2 " << l2
+         << "\niters " << iters << "\nerror " << err << "\nl2 " << l2 << "\nh1 " << h1
          << "\nt_assemble " << std::chrono::duration<double>(t1 - t0).count() << "\nt_solve " << tsolve << "\n";
     return 0;
 }

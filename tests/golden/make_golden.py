@@ -2,7 +2,7 @@
 
 Builds the reference's own FP64 assembler/solver from its sources (oracle/ref/Makefile, output in
 oracle/_ref/), runs it on seeded problems from gismo_gb300.problems and stores what it returns
-(dof map, CSC matrix, rhs, eliminated-dof values, solution, iterations, L2 error) as compressed
+(dof map, CSC matrix, rhs, eliminated-dof values, solution, iterations, L2 error, H1 seminorm error) as compressed
 .npz files next to this script. Run from the repository root, in a container that has the G+Smo
 source tree:
 
@@ -83,6 +83,7 @@ def run_reference(exe: str, prob, workdir: str) -> dict:
         csc_val=ld("csc_val.f64", np.float64), rhs=ld("rhs.f64", np.float64), ddof=ld("ddof.f64", np.float64),
         x=ld("x.f64", np.float64), free=np.int64(info["free"]), nnz=np.int64(info["nnz"]),
         iters=np.int64(info["iters"]), relres=np.float64(info["error"]), l2=np.float64(info["l2"]),
+        h1=np.float64(info["h1"]),
         spec=np.array(spec_text),
     )
 

@@ -53,6 +53,7 @@ def test_neumann_batch_matches_oracle():
     off = B.offsets()
     xs, info = B.solve(tol=1e-10, max_iters=5000)
     assert info["converged"]
+    h1 = B.h1_errors()
     for j, pr in enumerate(probs):
         o = _oracle(pr)
         orhs = o.rhs()
@@ -60,6 +61,8 @@ def test_neumann_batch_matches_oracle():
         assert np.abs(rhs[a:b] - orhs).max() <= 1e-12 * np.abs(orhs).max(), j
         xo, _, _, _ = o.solve_cg(1e-10, 5000)
         assert np.linalg.norm(xs[j] - xo) <= 1e-7 * np.linalg.norm(xo), j
+        oh1 = o.h1_error(xs[j])
+        assert abs(h1[j] - oh1) <= 1e-9 * oh1, (j, h1[j], oh1)
     B.close()
 
 
@@ -77,16 +80,20 @@ def test_neumann_multigrid_matches_cg():
 
 
 def test_neumann_exact_flux_converges():
-    """u = sin(pi x) sin(pi y) on the unit square, Dirichlet west/south, its flux on east/north."""
+    """u = sin(pi x) sin(pi y) on the unit square, Dirichlet west/south, its flux on east/north:
+    L2 error at rate p + 1, H1 seminorm error at rate p."""
     from gismo_gb300.assembler import GpuPoissonAssembler
     p = 2
-    errs = []
+    errs, h1s = [], []
     for n in (8, 16, 32):
         A = GpuPoissonAssembler(P.mixed_boundary(P.square_poisson(n, p)), device=0)
         A.assemble("fp64")
         _, info = A.solve(tol=1e-13, max_iters=5000)
         assert info["converged"]
         errs.append(A.l2_error())
+        h1s.append(A.h1_error())
         A.close()
     rates = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
     assert np.all(rates >= p + 0.8), (errs, rates)
+    rates = np.log2(np.array(h1s[:-1]) / np.array(h1s[1:]))
+    assert np.all(rates >= p - 0.2), (h1s, rates)

@@ -63,8 +63,11 @@ def test_fp64_matches_reference_fixture(path):
         o.assemble()
         l2 = o.l2_error(x)
         assert abs(l2 - float(g["l2"])) <= 5e-4 * float(g["l2"])
-        # the device quadrature of gsField::distanceL2 on the same solution
+        # the device quadrature of gsField::distanceL2 / distanceH1 on the same solution
         assert abs(A.l2_error() - l2) <= 1e-9 * l2
+        h1 = o.h1_error(x)
+        assert abs(h1 - float(g["h1"])) <= 5e-4 * float(g["h1"])
+        assert abs(A.h1_error() - h1) <= 1e-9 * h1
     A.close()
 
 
@@ -151,8 +154,8 @@ def test_inverted_geometry_is_reported():
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_l2_error_on_device(precision):
-    """gsField::distanceL2 on the device against the oracle's quadrature of the same solution, for
-    a 3D and a multipatch case, after either assembly precision."""
+    """gsField::distanceL2 and distanceH1 on the device against the oracle's quadrature of the same
+    solution, for a 3D and a multipatch case, after either assembly precision."""
     from oracle import oracle as O
     for prob in (P.volume_poisson(12, 3, seed=4), P.cube_grid(n=2, n_elem=5, p=2, seed=6, kappa_modes=8)):
         A = _assembler(prob)
@@ -163,6 +166,8 @@ def test_l2_error_on_device(precision):
         o.assemble()
         l2 = o.l2_error(x)
         assert abs(A.l2_error() - l2) <= 1e-9 * l2, (A.l2_error(), l2)
+        h1 = o.h1_error(x)
+        assert abs(A.h1_error() - h1) <= 1e-9 * h1, (A.h1_error(), h1)
         A.close()
 
 

@@ -52,6 +52,9 @@ def test_oracle_matches_reference(path):
     assert np.linalg.norm(x - g["x"]) <= 1e-9 * np.linalg.norm(g["x"])
     l2 = o.l2_error(x)
     assert abs(l2 - float(g["l2"])) <= 1e-6 * abs(float(g["l2"]))  # >= 3 significant digits
+    # gsField::distanceH1 of the reference's own solution
+    h1 = o.h1_error(g["x"])
+    assert abs(h1 - float(g["h1"])) <= 1e-10 * float(g["h1"])
 
 
 def test_generator_reproduces_fixture_specs():
