@@ -62,9 +62,13 @@ struct gsGpuProblemPack {
             else throw std::invalid_argument("gsgpu: dimension 2 or 3 only");
         }
         for (typename gsMultiPatch<T>::const_iiterator it = mp.iBegin(); it != mp.iEnd(); ++it) {
-            if (!it->dirOrientation().all()) throw std::invalid_argument("gsgpu: re-oriented interface");
-            for (index_t i = 0; i < it->dirMap().size(); ++i)
+            // the orientation of the side's own direction records whether the two sides sit at the
+            // same parameter (gsBoundary.h:665-716); only the tangential directions must be kept
+            const index_t nd = it->first().direction();
+            for (index_t i = 0; i < it->dirMap().size(); ++i) {
                 if (it->dirMap()(i) != i) throw std::invalid_argument("gsgpu: permuted interface");
+                if (i != nd && !it->dirOrientation()(i)) throw std::invalid_argument("gsgpu: re-oriented interface");
+            }
             ifaces.push_back(it->first().patch);
             ifaces.push_back(it->first().side().index());
             ifaces.push_back(it->second().patch);

@@ -194,3 +194,29 @@ def test_device_pattern_equals_host_pattern(monkeypatch):
         (pb, cb, vb), rb, xb = out[1]
         assert np.array_equal(pa, pb) and np.array_equal(ca, cb) and np.array_equal(va, vb)
         assert np.array_equal(ra, rb) and np.array_equal(xa, xb)
+
+
+def test_problem_from_xml_on_device(tmp_path):
+    """A problem read from a G+Smo XML file (two glued squares, refined and degree-elevated, with
+    Neumann data on the upper sides) through the C ABI against the oracle on the same input."""
+    from oracle import oracle as O
+    from gismo_gb300 import xmlio
+    sq = [P.identity_patch(2, (1, 1), (1, 1)), P.identity_patch(2, (1, 1), (1, 1))]
+    sq[1].coefs = sq[1].coefs - np.array([1.0, 0.0])
+    f = str(tmp_path / "two.xml")
+    xmlio.write_xml(P.Problem(2, sq, interfaces=[(1, 2, 0, 1)]), f)
+    prob = xmlio.problem_from_xml(f, refine=4, elevate=1, neumann=[(0, 2), (0, 4), (1, 4)])
+    o = O.OracleProblem(prob)
+    o.assemble()
+    A = _assembler(prob)
+    A.assemble()
+    assert np.array_equal(A.dofMapper(), o.dofmap())
+    ptr, col, val = A.csr()
+    optr, ocol, oval = o.csr()
+    assert np.array_equal(ptr, optr) and np.array_equal(col, ocol)
+    _check_values(val, oval, optr)
+    assert np.abs(A.rhs() - o.rhs()).max() <= REL * np.abs(o.rhs()).max()
+    x, info = A.solve(tol=1e-11)
+    xo, _, _, _ = o.solve_cg(1e-11, 1000)
+    assert info["converged"] and np.linalg.norm(x - xo) <= 1e-8 * np.linalg.norm(xo)
+    A.close()
