@@ -14,7 +14,8 @@
  *  given to the constructor is kept for G+Smo-side post-processing (e.g. distanceL2).
  *  Supported inputs: gsTensorBSpline patches of dimension 2 or 3, tensor B-spline bases,
  *  conforming interfaces with identity orientation (iFace::glue), Dirichlet sides eliminated
- *  with interpolated values. Anything else throws (no CPU fallback).
+ *  with values by interpolation or L2 projection ("DirichletValues"), Neumann sides with the
+ *  closed-form flux of u as data. Anything else throws (no CPU fallback).
  */
 #pragma once
 

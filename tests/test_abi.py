@@ -103,3 +103,21 @@ def test_dropin_headers_compile_against_reference():
         pytest.skip("G+Smo source tree not available")
     r = subprocess.run(["make", "-s", "-C", mk, "dropin-syntax"], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-3000:]
+
+
+def test_dropin_pack_matches_reference_mapper(lib):
+    """The C++ drop-in packs glued multipatch grids built by the reference (its own interface
+    orientation flags) with Dirichlet and Neumann sides from gsBoundaryConditions; a host-only
+    context's dof map equals the reference's gsDofMapper (oracle/ref/pack_check.cpp). Needs the
+    G+Smo source tree; skipped where it is absent."""
+    import shutil
+    import subprocess
+    mk = os.path.join(ROOT, "oracle", "ref")
+    if shutil.which("make") is None or shutil.which("g++") is None:
+        pytest.skip("no make / g++")
+    ref = subprocess.run(["make", "-s", "-C", mk, "print-ref"], capture_output=True, text=True).stdout.strip()
+    if not ref or not os.path.isdir(os.path.join(ref, "src", "gsAssembler")):
+        pytest.skip("G+Smo source tree not available")
+    r = subprocess.run(["make", "-s", "-C", mk, "packcheck"], capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, (r.stdout[-2000:], r.stderr[-3000:])
+    assert r.stdout.strip().endswith("ok")
