@@ -121,3 +121,22 @@ def test_dropin_pack_matches_reference_mapper(lib):
     r = subprocess.run(["make", "-s", "-C", mk, "packcheck"], capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, (r.stdout[-2000:], r.stderr[-3000:])
     assert r.stdout.strip().endswith("ok")
+
+
+@pytest.mark.parametrize("bad", ["dirichlet", "interface", "index", "duplicate"])
+def test_invalid_neumann_sides_are_rejected(lib, bad):
+    """One condition per boundary side (gsBoundaryConditions): a Neumann side that is also
+    Dirichlet, an interface side, a side index out of range or a repeated side is an input error."""
+    from gismo_gb300 import problems as P
+    if bad == "interface":
+        prob = P.mixed_boundary(P.cube_grid(n=2, n_elem=2, p=2, seed=1, kappa_modes=0))
+        prob.neumann.append(tuple(prob.interfaces[0][:2]))
+    else:
+        prob = P.mixed_boundary(P.square_poisson(4, 2))
+        prob.neumann.append({"dirichlet": prob.dirichlet[0], "index": (0, 7), "duplicate": prob.neumann[0]}[bad])
+    h = C.c_void_p()
+    assert lib.gsgpu_create(C.byref(h), -1) == _lib.OK
+    pk = PackedProblem(prob)
+    assert lib.gsgpu_set_problem(h, C.byref(pk.struct)) == _lib.ERR_INVALID
+    assert b"neumann" in lib.gsgpu_last_error(h)
+    lib.gsgpu_destroy(h)
