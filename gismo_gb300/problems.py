@@ -294,6 +294,24 @@ def all_sides(dim: int) -> List[int]:
     return list(range(1, 2 * dim + 1))
 
 
+def square_grid_mms(n_elem: int, p: int = 1) -> Problem:
+    """The set-up of the reference's gsPoissonSolver_test (unittests/gsPoissonSolver_test.cpp:
+    BSplineSquareGrid(2, 2, 0.5), Galerkin with iFace::glue): the unit square as four identity
+    patches of side 0.5 (patch 2i + j at (0.5 i, 0.5 j)), Dirichlet on the west sides of patches 0, 1
+    and the north sides of 1, 3, Neumann (the exact flux) on the east sides of 2, 3 and the south
+    sides of 0, 2; u = sin(pi x) sin(pi y); ``n_elem`` elements per patch and direction."""
+    patches = []
+    for i in range(2):
+        for j in range(2):
+            patches.append(identity_patch(2, (n_elem, n_elem), (p, p), lo=(0.5 * i, 0.5 * j), hi=(0.5 * i + 0.5, 0.5 * j + 0.5)))
+    ifaces = [(0, SIDE_EAST, 2, SIDE_WEST), (1, SIDE_EAST, 3, SIDE_WEST),
+              (0, SIDE_NORTH, 1, SIDE_SOUTH), (2, SIDE_NORTH, 3, SIDE_SOUTH)]
+    return Problem(2, patches, interfaces=ifaces,
+                   dirichlet=[(0, SIDE_WEST), (1, SIDE_WEST), (1, SIDE_NORTH), (3, SIDE_NORTH)],
+                   neumann=[(3, SIDE_EAST), (2, SIDE_EAST), (0, SIDE_SOUTH), (2, SIDE_SOUTH)],
+                   name=f"squaregrid_mms_p{p}_n{n_elem}")
+
+
 def mixed_boundary(prob: Problem) -> Problem:
     """Turn the upper boundary sides (east, north, back) of a problem's Dirichlet list into Neumann
     sides: Dirichlet on the lower sides, Neumann on the upper ones (the gsPoissonSolver_test

@@ -97,3 +97,27 @@ def test_neumann_exact_flux_converges():
     assert np.all(rates >= p + 0.8), (errs, rates)
     rates = np.log2(np.array(h1s[:-1]) / np.array(h1s[1:]))
     assert np.all(rates >= p - 0.2), (h1s, rates)
+
+
+def test_reference_mms_test_on_device():
+    """gsPoissonSolver_test (Galerkin_test) on the device: four glued degree-1 patches, Dirichlet
+    and Neumann sides, L2 rate above the test's 1.85 from the last two meshes and by least squares;
+    the device L2 errors within 1e-9 of the oracle's quadrature of the same solutions."""
+    from gismo_gb300.assembler import GpuPoissonAssembler
+    from tests.test_poisson_solver_mms import CONVRATE_TOL, rates
+    errs, hs = [], []
+    for n in (8, 16, 32):
+        prob = P.square_grid_mms(n, 1)
+        A = GpuPoissonAssembler(prob, device=0)
+        A.assemble("fp64")
+        x, info = A.solve(tol=1e-12, max_iters=20000)
+        assert info["converged"]
+        e = A.l2_error()
+        o = _oracle(prob)
+        oe = o.l2_error(x)
+        assert abs(e - oe) <= 1e-9 * oe
+        errs.append(e)
+        hs.append(0.5 / n)
+        A.close()
+    last, fit = rates(errs, hs)
+    assert last > CONVRATE_TOL and fit > CONVRATE_TOL, (errs, last, fit)
