@@ -227,8 +227,9 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from gismo_gb300.assembler import GpuPoissonAssembler
+    from gismo_gb300 import replicas as R
 
-    args.seed = args.seed + 1000 * rank  # independent replica per rank
+    args.seed = R.replica_seed(args.seed, rank)  # independent replica per rank
     prob = workload(args)
     A = GpuPoissonAssembler(prob, device=local)
     nfree, nnz, _, _ = A.sizes()
@@ -266,12 +267,10 @@ def main():
     t_ms = e0.elapsed_time(e1)
     barrier()
     clocks = clk.stop()
-    if dist is not None:
-        tt = torch.tensor([t_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_ms = float(tt.item())
+    # slowest rank's time, dofs of all ranks' replicas
+    t_ms, units = R.reduce_max_sum(dist, t_ms, nfree, "cuda")
     ms_per_step = t_ms / args.steps
-    value = ws * nfree / (ms_per_step * 1e-3)
+    value = units / (ms_per_step * 1e-3)
 
     # ---- the plain FP64 path on the same workload, and the accuracy of the headline path ----
     fp64_line = None
@@ -328,11 +327,8 @@ def main():
     f1.synchronize()
     te_ms = f0.elapsed_time(f1)
     barrier()
-    if dist is not None:
-        tt = torch.tensor([te_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        te_ms = float(tt.item())
-    e2e_value = ws * nfree / (te_ms / args.steps * 1e-3)
+    te_ms, units = R.reduce_max_sum(dist, te_ms, nfree, "cuda")
+    e2e_value = units / (te_ms / args.steps * 1e-3)
 
     # ---- roofline of the dominant HBM kernel: the CG SpMV, timed per launch with events ----
     A.set_profiling(True)
