@@ -458,6 +458,68 @@ def serving_requests(count: int, rate: float, seed: int = 11, check: bool = Fals
 # text spec for the reference driver (oracle/ref/ref_driver.cpp)
 
 
+def read_spec(text: str) -> Problem:
+    """The Problem of a text spec written by :func:`write_spec` (its exact inverse: every number is
+    written with repr, so the arrays come back bitwise)."""
+    toks = [ln.split() for ln in text.splitlines() if ln.strip()]
+    if not toks or toks[0][:2] != ["GSGPU-SPEC", "1"]:
+        raise ValueError("not a GSGPU-SPEC 1 text")
+    dim = int(toks[1][1])
+    i = 2
+    patches = []
+    prob = Problem(dim, patches)
+    modes = 0
+    while i < len(toks):
+        w = toks[i]
+        key = w[0]
+        if key == "patch":
+            deg = tuple(int(v) for v in toks[i + 1])
+            knots = [np.array([float(v) for v in toks[i + 2 + k][1:]]) for k in range(dim)]
+            gdeg = tuple(int(v) for v in toks[i + 2 + dim])
+            gknots = [np.array([float(v) for v in toks[i + 3 + dim + k][1:]]) for k in range(dim)]
+            nc = int(toks[i + 3 + 2 * dim][0])
+            rows = toks[i + 4 + 2 * dim:i + 4 + 2 * dim + nc]
+            coefs = np.array([[float(v) for v in r] for r in rows], dtype=np.float64).reshape(nc, dim)
+            patches.append(Patch(dim, deg, knots, gdeg, gknots, coefs))
+            i += 4 + 2 * dim + nc
+            continue
+        if key == "interface":
+            prob.interfaces.append(tuple(int(v) for v in w[1:5]))
+        elif key == "dirichlet":
+            prob.dirichlet.append((int(w[1]), int(w[2])))
+        elif key == "neumann":
+            prob.neumann.append((int(w[1]), int(w[2])))
+        elif key == "kappa_fourier":
+            prob.kappa_fourier = True
+            prob.kappa_alpha, prob.kappa_scale, modes = float(w[1]), float(w[2]), int(w[3])
+            rows = toks[i + 1:i + 1 + modes]
+            prob.kappa_amp = np.array([float(r[0]) for r in rows])
+            prob.kappa_k = np.array([[int(r[1]), int(r[2]), int(r[3])] for r in rows], dtype=np.int32).reshape(-1, 3)
+            prob.kappa_phase = np.array([float(r[4]) for r in rows])
+            i += 1 + modes
+            continue
+        elif key == "kappa_const":
+            prob.kappa_const = float(w[1])
+        elif key == "ufreq":
+            prob.ufreq = int(w[1])
+        elif key == "quad":
+            prob.quA, prob.quB = float(w[1]), int(w[2])
+        elif key == "dirichlet_values":
+            prob.dirichlet_l2 = w[1] == "l2"
+        elif key == "solver":
+            prob.solver, prob.tol, prob.maxit = w[1], float(w[2]), int(w[3])
+        elif key == "mg":
+            prob.mg_levels, prob.mg_npre, prob.mg_npost, prob.mg_damping = int(w[1]), int(w[2]), int(w[3]), float(w[4])
+        elif key == "mgcycle":
+            prob.mg_cycles, prob.mg_cgc_damping = int(w[1]), float(w[2])
+        elif key == "end":
+            break
+        else:
+            raise ValueError(f"unknown spec line {key!r}")
+        i += 1
+    return prob
+
+
 def write_spec(prob: Problem, path: str) -> None:
     def fmt(v):
         return repr(float(v))
