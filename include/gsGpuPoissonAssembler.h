@@ -213,6 +213,13 @@ public:
         return e;
     }
 
+    /// gsField::distanceH1 (H1 seminorm of the error) of the last device solution
+    double distanceH1() const {
+        double e = 0.0;
+        check(gsgpu_h1_error(m_ctx, &e));
+        return e;
+    }
+
     gsgpu_context* context() const { return m_ctx; }
 
 private:

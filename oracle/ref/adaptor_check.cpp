@@ -72,7 +72,7 @@ int main(int argc, char**) {
         gsSparseSolver<>::CGDiagonal solver;
         solver.compute(E.matrix());
         gsMatrix<> sol = solver.solve(E.rhs());
-        return int(A.matrix().nonZeros() + x.rows() + z.rows() + A.distanceL2() + A.error() + cg.iterations() +
+        return int(A.matrix().nonZeros() + x.rows() + z.rows() + A.distanceL2() + A.distanceH1() + A.error() + cg.iterations() +
                    E.numDofs() + sol.rows());
     }
     return 0;
