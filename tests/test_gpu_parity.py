@@ -1,6 +1,6 @@
 """GPU parity: the CUDA path (through the C ABI) against the reference fixtures and the CPU oracle.
 
-Bars (the benchmark spec): dof map and sparsity pattern bit-exact; FP64 matrix and rhs entries within
+Bars: dof map and sparsity pattern bit-exact; FP64 matrix and rhs entries within
 1e-12 relative (absolute floor 1e-14 x the row's largest entry for entries that cancel to ~0);
 CG iteration counts within one of the reference's; the discrete L2 error to >= 3 significant
 digits."""
