@@ -8,7 +8,7 @@ source tree:
 
     python tests/golden/make_golden.py --ref /path/to/gismo
 
-The fixtures are committed; nothing on the GPU host runs this script.
+The fixtures are committed; the GPU tests only read them.
 """
 from __future__ import annotations
 
