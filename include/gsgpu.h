@@ -161,10 +161,12 @@ int gsgpu_apply(gsgpu_context* ctx, const double* x, double* y);
  * hierarchy, smoother and cycle options of opts (mg_levels, mg_npre, mg_npost, mg_damping,
  * mg_cycles, mg_cgc_damping) */
 int gsgpu_mg_apply(gsgpu_context* ctx, const gsgpu_solver_opts* opts, const double* r, double* z);
-/* gsField::distanceL2 of the last solution against u (gsField.hpp:23-41) */
+/* gsField::distanceL2 of the last solution against u (gsField.hpp:23-41), integrated with the
+ * assembly's quadrature rule; the reference integrates with its evaluator's default, p + 1 Gauss
+ * points per direction, so the two agree when quA = 1 and quB = 1 (the default) */
 int gsgpu_l2_error(gsgpu_context* ctx, double* err);
 /* gsField::distanceH1 of the last solution against u (gsField.hpp:44-60): the H1 seminorm
- * sqrt(int |grad u_h - grad u|^2), with the assembly's quadrature rule */
+ * sqrt(int |grad u_h - grad u|^2), with the same rule as gsgpu_l2_error */
 int gsgpu_h1_error(gsgpu_context* ctx, double* err);
 
 /* Batches of independent problems. No counterpart in the reference, where each problem is its own

@@ -472,12 +472,14 @@ struct Oracle {
 
     // quadrature nodes / weights on an element, tensor order with direction 0 fastest
     // (gsQuadRule::mapTo, src/gsAssembler/gsQuadRule.hpp:23-37 and gsQuadRule.h:132)
+    // evaluatorRule: p + 1 points per direction, the default rule of gsExprEvaluator
+    // (gsExprEvaluator.h:79-80, quA = 1, quB = 1), which gsField::distanceL2/H1 integrate with
     void elementRule(const PatchData& P, const Elem& E, std::vector<double>& pts, std::vector<double>& wts,
-                     int q[3]) const {
+                     int q[3], bool evaluatorRule = false) const {
         std::vector<double> xr[3], wr[3];
         int nqt = 1;
         for (int k = 0; k < dim; ++k) {
-            q[k] = nq(P.b[k].p);
+            q[k] = evaluatorRule ? P.b[k].p + 1 : nq(P.b[k].p);
             gaussRule(q[k], xr[k], wr[k]);
             const double lo = P.b[k].breaks[E.e[k]], hi = P.b[k].breaks[E.e[k] + 1];
             const double h = (hi - lo) / 2.0;
@@ -1026,7 +1028,7 @@ struct Oracle {
     // src/gsCore/gsField.hpp:23-41, gsAssembler::constructSolution gsAssembler.hpp:536-581)
     // gsField::distanceH1 (src/gsCore/gsField.hpp:44-60) for the parametric solution field against
     // the physical exact function: sqrt(sum w |det J| |J^-T grad_xi u_h - grad u|^2)
-    double h1error(const double* x) const {
+    double h1error(const double* x, bool evaluatorRule = false) const {
         double acc = 0;
         const long long ne = totalElems();
 #pragma omp parallel for reduction(+ : acc) schedule(static)
@@ -1036,7 +1038,7 @@ struct Oracle {
             const Elem E = elemAt(ge);
             const PatchData& P = patches[E.patch];
             int q[3];
-            elementRule(P, E, pts, wts, q);
+            elementRule(P, E, pts, wts, q, evaluatorRule);
             const int nqt = int(wts.size());
             elementBasis(P, E, pts, nqt, act, N, dN);
             for (int qi = 0; qi < nqt; ++qi) {
@@ -1064,7 +1066,7 @@ struct Oracle {
         return std::sqrt(acc);
     }
 
-    double l2error(const double* x) const {
+    double l2error(const double* x, bool evaluatorRule = false) const {
         double acc = 0;
         const long long ne = totalElems();
 #pragma omp parallel for reduction(+ : acc) schedule(static)
@@ -1074,7 +1076,7 @@ struct Oracle {
             const Elem E = elemAt(ge);
             const PatchData& P = patches[E.patch];
             int q[3];
-            elementRule(P, E, pts, wts, q);
+            elementRule(P, E, pts, wts, q, evaluatorRule);
             const int nqt = int(wts.size());
             elementBasis(P, E, pts, nqt, act, N, dN);
             for (int qi = 0; qi < nqt; ++qi) {
@@ -1444,6 +1446,10 @@ double orc_solve_mg(void* h, double tol, int maxit, int levels, int npre, int np
 }
 double orc_l2_error(void* h, const double* x) { return static_cast<Oracle*>(h)->l2error(x); }
 double orc_h1_error(void* h, const double* x) { return static_cast<Oracle*>(h)->h1error(x); }
+double orc_error_evaluator_rule(void* h, const double* x, int h1) {
+    const Oracle* o = static_cast<Oracle*>(h);
+    return h1 ? o->h1error(x, true) : o->l2error(x, true);
+}
 void orc_gauss(int n, double* nodes, double* weights) {
     std::vector<double> x, w;
     gaussRule(n, x, w);

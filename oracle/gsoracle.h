@@ -63,6 +63,10 @@ double orc_solve_mg(void* h, double tol, int maxit, int levels, int npre, int np
 double orc_l2_error(void* h, const double* x);
 /* gsField::distanceH1: H1 seminorm of u_h - u */
 double orc_h1_error(void* h, const double* x);
+/* the same norms (h1 = 0: L2, 1: H1 seminorm) with p + 1 Gauss points per direction, the rule
+ * gsField::distanceL2/H1 integrate with whatever the assembler's quA/quB (gsExprEvaluator
+ * defaults); orc_l2_error / orc_h1_error use the assembly rule, as the device does */
+double orc_error_evaluator_rule(void* h, const double* x, int h1);
 /* Gauss-Legendre rule on [-1,1] (ascending nodes) */
 void orc_gauss(int n, double* nodes, double* weights);
 

@@ -60,6 +60,8 @@ def _lib():
     lib.orc_l2_error.argtypes = [vp, C.c_void_p]
     lib.orc_h1_error.restype = C.c_double
     lib.orc_h1_error.argtypes = [vp, C.c_void_p]
+    lib.orc_error_evaluator_rule.restype = C.c_double
+    lib.orc_error_evaluator_rule.argtypes = [vp, C.c_void_p, C.c_int]
     lib.orc_gauss.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
     return lib
 
@@ -178,6 +180,13 @@ class OracleProblem:
     def h1_error(self, x):
         x = np.ascontiguousarray(x, np.float64)
         return lib().orc_h1_error(self.h, x.ctypes.data)
+
+    def reference_norms(self, x):
+        """(L2, H1 seminorm) errors with gsField::distanceL2/H1's own rule (p + 1 Gauss points per
+        direction, whatever quA/quB the problem assembles with)."""
+        x = np.ascontiguousarray(x, np.float64)
+        return (lib().orc_error_evaluator_rule(self.h, x.ctypes.data, 0),
+                lib().orc_error_evaluator_rule(self.h, x.ctypes.data, 1))
 
 
 def gauss(n: int):
