@@ -61,3 +61,33 @@ def test_save_and_load_state(tmp_path):
     import scipy.sparse as sp
     r = o2.rhs() - sp.csr_matrix((arr["csr_val"], c2, p2)) @ arr["x"]
     assert np.linalg.norm(r) <= 1.01 * float(arr["relres"]) * np.linalg.norm(o2.rhs()) + 1e-14
+
+
+def test_save_assembler_contract(tmp_path):
+    """save_assembler takes what an assembler exposes (prob, csr(), rhs(), fixedDofs()); an
+    oracle-backed stand-in with the same methods gives a checkpoint that loads back bitwise."""
+    from oracle import oracle as O
+
+    class Stand:
+        def __init__(self, prob):
+            self.prob = prob
+            self.o = O.OracleProblem(prob)
+            self.o.assemble()
+
+        def csr(self):
+            return self.o.csr()
+
+        def rhs(self):
+            return self.o.rhs()
+
+        def fixedDofs(self):
+            return self.o.ddof()
+
+    A = Stand(P.mixed_boundary(P.displaced_single_patch(2, (6, 5), (2, 3), 4, 0.05)))
+    x, it, rr, _ = A.o.solve_cg(1e-10, 1000)
+    f = str(tmp_path / "a.npz")
+    K.save_assembler(f, A, x, {"iterations": it, "relres": rr})
+    prob, arr = K.load_state(f)
+    _same(prob, A.prob)
+    assert np.array_equal(arr["x"], x) and np.array_equal(arr["ddof"], A.fixedDofs())
+    assert int(arr["iterations"]) == it and float(arr["relres"]) == rr
