@@ -151,3 +151,30 @@ def test_two_patch_sample_converges():
             errs.append(o.l2_error(x))
     rates = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
     assert np.all(rates >= 2.8), (errs, rates)
+
+
+def test_rejections_and_uniform_knots(tmp_path):
+    """NURBS patches and permuted / reversed interfaces are outside the path (ValueError); a
+    KnotVector in mode="uniform" expands to the open uniform knots of its csize."""
+    nurbs = tmp_path / "nurbs.xml"
+    nurbs.write_text('<xml><Geometry type="TensorNurbs2" id="0"></Geometry></xml>')
+    with pytest.raises(ValueError, match="not supported"):
+        xmlio.read_xml(str(nurbs))
+    two = [P.identity_patch(2, (1, 1), (1, 1)), P.identity_patch(2, (1, 1), (1, 1))]
+    two[1].coefs = two[1].coefs - np.array([1.0, 0.0])
+    f = str(tmp_path / "two.xml")
+    xmlio.write_xml(P.Problem(2, two, interfaces=[(1, 2, 0, 1)]), f)
+    text = open(f).read().replace("1 2 0 1 0 1 1 1", "1 2 0 1 0 1 1 0")  # reverse the side direction
+    bad = tmp_path / "rev.xml"
+    bad.write_text(text)
+    with pytest.raises(ValueError, match="permuted or reversed"):
+        xmlio.problem_from_xml(str(bad))
+    uni = tmp_path / "uni.xml"
+    uni.write_text('<xml><Geometry type="TensorBSpline2" id="0"><Basis type="TensorBSplineBasis2">'
+                   '<Basis type="BSplineBasis" index="0"><KnotVector degree="2" mode="uniform" csize="5"/></Basis>'
+                   '<Basis type="BSplineBasis" index="1"><KnotVector degree="1">0 0 1 1</KnotVector></Basis>'
+                   '</Basis><coefs geoDim="2">' + " ".join("0 0" for _ in range(10)) + '</coefs></Geometry></xml>')
+    d = xmlio.read_xml(str(uni))
+    degs, knots, coefs = d["patches"][0]
+    assert degs == [2, 1] and np.array_equal(knots[0], [0, 0, 0, 1 / 3, 2 / 3, 1, 1, 1]) and coefs.shape == (10, 2)
+    assert d["boundary"] == [(0, s) for s in P.all_sides(2)]
