@@ -178,3 +178,27 @@ def test_rejections_and_uniform_knots(tmp_path):
     degs, knots, coefs = d["patches"][0]
     assert degs == [2, 1] and np.array_equal(knots[0], [0, 0, 0, 1 / 3, 2 / 3, 1, 1, 1]) and coefs.shape == (10, 2)
     assert d["boundary"] == [(0, s) for s in P.all_sides(2)]
+
+
+def test_refine_and_elevate_match_reference():
+    """xmlio's degree elevation and uniform refinement give bitwise the reference's knot vectors
+    (gsKnotVector::degreeElevate / uniformRefine run by oracle/ref/knot_ops.cpp) on seeded knot
+    vectors with repeated interior knots and uneven spans."""
+    if _reference_tree() is None:
+        pytest.skip("G+Smo source tree not available")
+    r = subprocess.run(["make", "-s", "-C", MK, "knotops"], capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-3000:]
+    exe = os.path.join(ROOT, "oracle", "_ref", "gsknot")
+    rng = np.random.default_rng(5)
+    for case in range(12):
+        p = int(rng.integers(1, 4))
+        interior = np.sort(rng.uniform(0.0, 2.0, size=int(rng.integers(0, 5))))
+        reps = rng.integers(1, p + 1, size=len(interior))
+        t = np.concatenate([[0.0] * (p + 1), np.repeat(interior, reps), [2.0] * (p + 1)])
+        e, nref = int(rng.integers(0, 3)), int(rng.integers(0, 3))
+        out = subprocess.run([exe, str(p), str(e), str(nref)] + [repr(float(v)) for v in t], capture_output=True,
+                             text=True, timeout=60, check=True).stdout.split()
+        q, s = xmlio._elevate(p, t, e)
+        s = xmlio._refine(s, nref)
+        assert q == int(out[0]), case
+        assert np.array_equal(s, np.array([float(v) for v in out[1:]])), (case, s, out)
