@@ -140,3 +140,36 @@ def test_invalid_neumann_sides_are_rejected(lib, bad):
     assert lib.gsgpu_set_problem(h, C.byref(pk.struct)) == _lib.ERR_INVALID
     assert b"neumann" in lib.gsgpu_last_error(h)
     lib.gsgpu_destroy(h)
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """The ctypes mirrors of the C-ABI structs (gismo_gb300/_lib.py, and the oracle's problem
+    struct) have the headers' field offsets and sizes: a C program compiled against
+    include/gsgpu.h and oracle/gsoracle.h prints offsetof / sizeof for every field."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("no gcc")
+    from oracle import oracle as O
+    structs = {"gsgpu_problem": _lib.Problem, "gsgpu_solver_opts": _lib.SolverOpts,
+               "gsgpu_solve_info": _lib.SolveInfo, "gsgpu_request_info": _lib.RequestInfo,
+               "orc_problem": O._Problem}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gsgpu.h"', '#include "gsoracle.h"',
+             "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "oracle"), str(src), "-o",
+                        str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {tuple(ln.split()[:2]): int(ln.split()[2]) for ln in out if ln}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
