@@ -134,6 +134,15 @@ class GpuPoissonAssembler:
         n = len(ptr) - 1
         return sp.csr_matrix((val, col, ptr), shape=(n, n))
 
+    def diagonal(self) -> np.ndarray:
+        """matrix().diagonal() (gsSparseMatrix::diagonal), from the downloaded CSR arrays."""
+        ptr, col, val = self.csr()
+        rows = np.repeat(np.arange(len(ptr) - 1, dtype=np.int32), np.diff(ptr))
+        on = col == rows
+        d = np.zeros(len(ptr) - 1)
+        d[rows[on]] = val[on]
+        return d
+
     def rhs(self) -> np.ndarray:
         out = np.empty(self.sizes()[0], np.float64)
         self._check(self.L.gsgpu_rhs(self.h, out.ctypes.data))

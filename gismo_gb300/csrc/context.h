@@ -32,6 +32,9 @@ struct StateError : std::runtime_error {
 struct JacobianError : std::runtime_error {
     using std::runtime_error::runtime_error;
 };
+struct TimeoutError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
 
 // every device allocation of a context goes through here (accounting against a budget)
 // device buffers of one context, stream-ordered on the context's stream (cudaMallocAsync /
@@ -151,6 +154,14 @@ struct Context {
     float *dValHi = nullptr, *dValLo = nullptr, *dDinv32 = nullptr;
     float *dR32 = nullptr, *dZ32 = nullptr, *dP32 = nullptr, *dT32 = nullptr, *dDx32 = nullptr, *dXhi = nullptr,
           *dXlo = nullptr;
+    // the FP32 inner operator as half diagonals (single patch whose free dofs are one box, sdia.cu)
+    bool sdiaOk = false;
+    SdiaOp sdiaOp;
+    SdiaBand sdiaBand;
+    float* dSdia = nullptr;
+    int* dSdiaErr = nullptr;          // set by the TMA-fed product's bounded waits when they expire
+    alignas(64) unsigned char sdiaMaps[256] = {};  // two CUtensorMap (diagonals, x) when TMA is used
+    void setupSdia();
     Tab tabPf, tabCoef, tabGeo1, tabGeo2, tabPoint, tabSt[3], tabLd[3];
     Tab tabRow[3][5];  // [stage][degree along the stage axis]: interior rows of simple axes
     Tab tabRowB[3][5]; // the remaining rows

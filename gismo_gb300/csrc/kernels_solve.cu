@@ -614,7 +614,16 @@ int spmv32Partials(int n, int lanes_per_row) {
     return std::min(spmvPartials(n, lanes_per_row), 152 * kSpmv32BlocksPerSm);
 }
 
+// block partials left by the inner FP32 product
+int mixedSpmvPartials(const CgBuffers& B) {
+    return B.sdia.d ? sdiaPartials(B.sdia) : spmv32Partials(B.n, B.lanes_per_row);
+}
+
 void mixedSpmv(const CgBuffers& B, cudaStream_t s) {
+    if (B.sdia.d) {
+        sdiaSpmv(B.sdia, B.p32, B.t32, B.part2, B.st, s);
+        return;
+    }
     const int nb = spmv32Partials(B.n, B.lanes_per_row);
     GSGPU_BOX_DISPATCH(k_spmv32_dot, nb, B.n, B.ptr, B.col, B.coff, B.box, B.box_off, B.nbox, B.val_hi, B.p32, B.t32,
                        B.part2, B.st);
@@ -622,7 +631,7 @@ void mixedSpmv(const CgBuffers& B, cudaStream_t s) {
 
 void mixedRest(const CgBuffers& B, cudaStream_t s) {
     const int np = cgPartials(B.n);
-    const int nb = spmv32Partials(B.n, B.lanes_per_row);
+    const int nb = mixedSpmvPartials(B);
     k_alpha_m<<<1, kB, 0, s>>>(nb, B.part2, B.st);
     k_update32<<<np, kB, 0, s>>>(B.n, B.dx32, B.r32, B.z32, B.p32, B.t32, B.dinv32, B.part0, B.part1, B.st);
     k_beta_m<<<1, kB, 0, s>>>(np, B.part0, B.part1, B.st);

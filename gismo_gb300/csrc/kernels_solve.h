@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <string>
 
 namespace gsgpu {
 
@@ -20,6 +21,29 @@ struct CgState {
     int replaced;      // mixed: a replacement ran in this chunk (restart the FP32 recursion)
     int restart;       // mixed: the replacement moved the residual a lot; restart p = z
     unsigned arrive;   // blocks of the running kernel that have stored their partial sums
+};
+
+// half-diagonal storage of the FP32 inner operator of a single patch whose free dofs are one box of
+// m0 x m1 x m2 functions numbered lexicographically (sdia.cu): d[h * ns + i] = A(i, i + o_h) for the
+// nh offsets o_h of the half neighbour box (lexicographically >= 0), 0 where i + o_h leaves the box;
+// the diagonal stride ns is n rounded up to a multiple of 256
+struct SdiaOp {
+    const float* d = nullptr;
+    int n = 0, nh = 0, ns = 0;
+    int m[3] = {1, 1, 1};
+    int p[3] = {0, 0, 0};
+    // if set: host copies of the two tensor maps (the diagonals, the vector x) of the TMA-fed product,
+    // and the device word its bounded waits set when they expire
+    const void* tmaps = nullptr;
+    int* err = nullptr;
+};
+// where the free box sits in the patch's band: patch-local dof counts n, band widths W = 2p + 1,
+// the box's lower corner lo and the patch's band offset
+struct SdiaBand {
+    int n[3] = {1, 1, 1};
+    int W[3] = {1, 1, 1};
+    int lo[3] = {0, 0, 0};
+    long long band_off = 0;
 };
 
 struct CgBuffers {
@@ -46,7 +70,11 @@ struct CgBuffers {
     const float* dinv32 = nullptr;
     float *r32 = nullptr, *z32 = nullptr, *p32 = nullptr, *t32 = nullptr, *dx32 = nullptr, *xhi = nullptr,
           *xlo = nullptr;
+    // if sdia.d is set, the inner FP32 products use the half-diagonal form instead of the CSR hi values
+    SdiaOp sdia;
 };
+
+struct df32;
 
 namespace launch {
 int cgPartials(int n);
@@ -70,5 +98,14 @@ void mixedSpmv(const CgBuffers& B, cudaStream_t s);
 void mixedRest(const CgBuffers& B, cudaStream_t s);
 void mixedIteration(const CgBuffers& B, cudaStream_t s);
 void mixedReplace(const CgBuffers& B, cudaStream_t s);  // x += dx, r = b - A x (df32), restart r32/z/rho
+// half-diagonal inner operator (sdia.cu): offsets stored, the builder from the df32 band (the hi
+// parts, as the CSR gather takes them) and the product t = A x with block partials of x.t
+int sdiaHalf(const int* p);
+void sdiaBuild(const SdiaOp& A, const SdiaBand& B, const df32* band, float* d, cudaStream_t s);
+int sdiaPartials(const SdiaOp& A);
+// encode the TMA tensor maps of A's diagonals and of the vector x into out2 (two CUtensorMap, 64-byte
+// aligned); false (and the reason in *why) if the driver or the shape does not allow them
+bool sdiaTensorMaps(const SdiaOp& A, const float* x, void* out2, std::string* why);
+void sdiaSpmv(const SdiaOp& A, const float* x, float* t, double* part, const CgState* st, cudaStream_t s);
 }  // namespace launch
 }  // namespace gsgpu

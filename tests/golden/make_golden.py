@@ -13,6 +13,7 @@ The fixtures are committed; the GPU tests only read them.
 from __future__ import annotations
 
 import argparse
+import hashlib
 import os
 import subprocess
 import sys
@@ -70,6 +71,25 @@ def cases():
     return out
 
 
+def large_cases():
+    """name -> Problem at the benchmark's sizes. The full matrices (87M non-zeros at 64^3) are too
+    large to commit: these fixtures keep the reference's scalars (sizes, CG iterations, residual,
+    L2 and H1 errors), every SAMPLE-th entry of its solution, rhs and diagonal, the norms of its
+    rhs and solution, and the SHA-256 of the problem's spec text."""
+    out = {}
+    # the headline shape (3D, p=3, 64^3) with kappa = 1 on the undisplaced unit cube
+    cube = P.Problem(3, [P.identity_patch(3, (64, 64, 64), (3, 3, 3))],
+                     dirichlet=[(0, s) for s in P.all_sides(3)], name="cube_p3_n64")
+    out["large_cube_p3_n64"] = cube
+    # the headline configuration itself (displacement 0.04, 16-mode kappa field), and at 32^3
+    out["large_vol_p3_n64_s1"] = P.volume_poisson(64, 3, seed=1)
+    out["large_vol_p3_n32_s1"] = P.volume_poisson(32, 3, seed=1)
+    return out
+
+
+SAMPLE = 97
+
+
 def run_reference(exe: str, prob, workdir: str) -> dict:
     spec = os.path.join(workdir, "spec.txt")
     P.write_spec(prob, spec)
@@ -105,6 +125,35 @@ def main():
             res = run_reference(exe, prob, td)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **res)
         print(name, "free", int(res["free"]), "nnz", int(res["nnz"]), "iters", int(res["iters"]), "l2", float(res["l2"]))
+    for name, prob in large_cases().items():
+        if args.only and name != args.only:
+            continue
+        with tempfile.TemporaryDirectory() as td:
+            res = run_reference(exe, prob, td)
+        keep = {k: res[k] for k in ("free", "nnz", "iters", "relres", "l2", "h1")}
+        # the spec text of a 64^3 displaced patch is tens of MB: keep its digest, the tests rebuild
+        # the problem with large_cases() and compare digests
+        keep["spec_sha256"] = np.array(hashlib.sha256(str(res["spec"]).encode()).hexdigest())
+        keep["sample"] = np.int64(SAMPLE)
+        keep["x_sample"] = res["x"][::SAMPLE]
+        keep["rhs_sample"] = res["rhs"][::SAMPLE]
+        keep["rhs_norm"] = np.float64(np.linalg.norm(res["rhs"]))
+        keep["x_norm"] = np.float64(np.linalg.norm(res["x"]))
+        keep["diag_sample"] = _csc_diagonal(res)[::SAMPLE]
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **keep)
+        print(name, "free", int(res["free"]), "nnz", int(res["nnz"]), "iters", int(res["iters"]), "l2", float(res["l2"]),
+              flush=True)
+
+
+def _csc_diagonal(res) -> np.ndarray:
+    """Diagonal of the reference's compressed ColMajor matrix."""
+    ptr, idx, val = res["csc_ptr"], res["csc_idx"], res["csc_val"]
+    n = len(ptr) - 1
+    colof = np.repeat(np.arange(n, dtype=np.int64), np.diff(ptr))
+    on = idx == colof
+    d = np.zeros(n)
+    d[colof[on]] = val[on]
+    return d
 
 
 if __name__ == "__main__":

@@ -10,9 +10,14 @@ def load_golden(name):
     return dict(np.load(os.path.join(HERE, name + ".npz")))
 
 
-def golden_problem(name):
+def golden_module():
+    """tests/golden/make_golden.py as a module (its case lists)."""
     import importlib.util
     spec = importlib.util.spec_from_file_location("make_golden", os.path.join(HERE, "make_golden.py"))
     mod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mod)
-    return mod.cases()[name]
+    return mod
+
+
+def golden_problem(name):
+    return golden_module().cases()[name]

@@ -173,3 +173,17 @@ def test_ctypes_structs_match_the_header(tmp_path):
         assert got[(cname, "size")] == C.sizeof(py), cname
         for fname, _ in py._fields_:
             assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
+@pytest.mark.parametrize("name", ["large_vol_p3_n32_s1", "large_cube_p3_n64"])
+def test_host_plan_sizes_match_large_reference_runs(lib, name):
+    """The reference's free-dof and non-zero counts at the benchmark's sizes, from the host plan of a
+    host-only context (no GPU)."""
+    from tests.golden_cases import golden_module, load_golden
+    g = load_golden(name)
+    prob = golden_module().large_cases()[name]
+    h, pk = _host_ctx(lib, prob)
+    nf, nnz, nb, nl = C.c_int(), C.c_longlong(), C.c_int(), C.c_int()
+    assert lib.gsgpu_sizes(h, C.byref(nf), C.byref(nnz), C.byref(nb), C.byref(nl)) == _lib.OK
+    assert (nf.value, nnz.value) == (int(g["free"]), int(g["nnz"]))
+    lib.gsgpu_destroy(h)

@@ -102,3 +102,74 @@ def test_stage31_tiles_are_bitwise_neutral(case):
         finally:
             os.environ.pop("GSGPU_NO_TILE31", None)
     assert np.array_equal(vals[0], vals[1])
+
+
+SDIA_CASES = {
+    "volume_p3_16": lambda: P.volume_poisson(16, 3, seed=2),
+    "disp2d_p4_40x33": lambda: P.displaced_single_patch(2, (40, 33), (4, 4), 9, 0.05, ufreq=3),
+    "disp3d_p232_5x6x7": lambda: P.displaced_single_patch(3, (5, 6, 7), (2, 3, 2), 8, 0.04),
+    "square_p2_64_neu": lambda: P.mixed_boundary(P.square_poisson(64, 2)),
+    "disp3d_p3_12_neu": lambda: P.mixed_boundary(P.volume_poisson(12, 3, seed=3)),
+}
+
+
+@pytest.mark.parametrize("case", sorted(SDIA_CASES))
+def test_half_diagonal_inner_operator(case, monkeypatch):
+    """Single patches whose free dofs form one box run the inner FP32 products on the half-diagonal
+    form (sdia.cu). Against the CSR form of the same FP32 values (GSGPU_NO_SDIA=1): both mixed
+    solutions within 1e-8 of the tight FP64 solution, iteration counts within a few of each other,
+    and the half-diagonal path is the one that ran (its per-product bytes)."""
+    from gismo_gb300.assembler import GpuPoissonAssembler
+    prob = SDIA_CASES[case]()
+    A = GpuPoissonAssembler(prob)
+    A.assemble("fp64")
+    x64, _ = A.solve(tol=1e-13, max_iters=20000)
+    A.close()
+    out = {}
+    for sdia in (True, False):
+        if sdia:
+            monkeypatch.delenv("GSGPU_NO_SDIA", raising=False)
+        else:
+            monkeypatch.setenv("GSGPU_NO_SDIA", "1")
+        A = GpuPoissonAssembler(prob)
+        A.assemble("mixed")
+        xm, im = A.solve(tol=1e-11, precision="mixed", max_iters=20000)
+        assert im["converged"], im
+        err = np.linalg.norm(xm - x64) / np.linalg.norm(x64)
+        assert err <= 1e-8, (case, sdia, err, im)
+        A.set_profiling(True)
+        A.solve(tol=1e-11, precision="mixed", max_iters=20000, download=False)
+        _, _, nbytes = A.spmv_stats()
+        A.set_profiling(False)
+        n = len(xm)
+        p = list(prob.patches[0].degree) + [0] * (3 - prob.dim)
+        nh = 1 + (np.prod([2 * q + 1 for q in p]) - 1) // 2
+        assert (nbytes == nh * n * 4 + 8 * n) == sdia, (case, sdia, nbytes, nh * n * 4 + 8 * n)
+        out[sdia] = im["iterations"]
+        A.close()
+    assert abs(out[True] - out[False]) <= max(3, out[False] // 20), out
+
+
+@pytest.mark.parametrize("case", ["volume_p3_16", "disp2d_p4_40x33", "disp3d_p3_12_neu"])
+def test_half_diagonal_tma_is_bitwise_neutral(case, monkeypatch):
+    """The TMA-fed half-diagonal product (GSGPU_SDIA_TMA=1: tiled bulk copies into a shared-memory
+    ring) and the default load-based one form the same products in the same order: the mixed solves
+    give the same bits."""
+    from gismo_gb300.assembler import GpuPoissonAssembler
+    prob = SDIA_CASES[case]()
+    xs = []
+    for tma in (True, False):
+        if tma:
+            monkeypatch.setenv("GSGPU_SDIA_TMA", "1")
+            monkeypatch.setenv("GSGPU_REQUIRE_TMA", "1")  # fail loudly if the tensor maps are refused
+        else:
+            monkeypatch.delenv("GSGPU_SDIA_TMA", raising=False)
+            monkeypatch.delenv("GSGPU_REQUIRE_TMA", raising=False)
+        A = GpuPoissonAssembler(prob)
+        A.assemble("mixed")
+        x, info = A.solve(tol=1e-11, precision="mixed", max_iters=20000)
+        assert info["converged"], info
+        xs.append((x, info["iterations"]))
+        A.close()
+    assert xs[0][1] == xs[1][1]
+    assert np.array_equal(xs[0][0], xs[1][0])
