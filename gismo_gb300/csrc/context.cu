@@ -395,7 +395,6 @@ void Context::setupSdia() {
     }
     sdiaOp.nh = launch::sdiaHalf(sdiaOp.p);
     sdiaOp.ns = (nfree + 255) / 256 * 256;
-    sdiaBand.band_off = D.band_off;
     sdiaOk = true;
 }
 
@@ -748,7 +747,8 @@ void Context::ensureSolveBuffers() {
     allocN(arena, dPart0, launch::cgPartials(n));
     allocN(arena, dPart1, launch::cgPartials(n));
     // SpMV partials: one per SpMV block; the most blocks are launched with 32 lanes per row
-    allocN(arena, dPart2, std::max(launch::cgPartials(n), launch::spmvPartials(n, 32)));
+    allocN(arena, dPart2, std::max({launch::cgPartials(n), launch::spmvPartials(n, 32),
+                                    sdiaOk ? launch::sdiaPartials(sdiaOp) : 0}));
     dCg = static_cast<CgState*>(arena.alloc(sizeof(CgState)));
     solveN = n;
 }
@@ -891,7 +891,17 @@ void Context::ensureMixedBuffers() {
     allocN(arena, dDinv32, n);
     allocN(arena, dR32, n);
     allocN(arena, dZ32, n);
-    allocN(arena, dP32, n);
+    if (sdiaOk) {
+        // the half-diagonal product reads x up to sdiaReach entries before and after the vector:
+        // the direction carries that many zeros on both sides (written once, never overwritten)
+        const int pad = (launch::sdiaReach(sdiaOp) + 63) / 64 * 64;
+        allocN(arena, dP32pad, (long long)n + 2LL * pad);
+        GSGPU_CUDA_TRY(cudaMemsetAsync(dP32pad, 0, (size_t(n) + 2 * size_t(pad)) * sizeof(float), stream));
+        dP32 = dP32pad + pad;
+        sdiaOp.xpad = pad;
+    } else {
+        allocN(arena, dP32, n);
+    }
     allocN(arena, dT32, n);
     allocN(arena, dDx32, n);
     allocN(arena, dXhi, n);

@@ -159,6 +159,7 @@ struct Context {
     SdiaOp sdiaOp;
     SdiaBand sdiaBand;
     float* dSdia = nullptr;
+    float* dP32pad = nullptr;         // allocation of the inner CG direction with its zero padding
     int* dSdiaErr = nullptr;          // set by the TMA-fed product's bounded waits when they expire
     alignas(64) unsigned char sdiaMaps[256] = {};  // two CUtensorMap (diagonals, x) when TMA is used
     void setupSdia();

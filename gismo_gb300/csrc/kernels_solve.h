@@ -32,6 +32,7 @@ struct SdiaOp {
     int n = 0, nh = 0, ns = 0;
     int m[3] = {1, 1, 1};
     int p[3] = {0, 0, 0};
+    int xpad = 0;  // zeros the vector x of the product carries before and after its n entries
     // if set: host copies of the two tensor maps (the diagonals, the vector x) of the TMA-fed product,
     // and the device word its bounded waits set when they expire
     const void* tmaps = nullptr;
@@ -101,6 +102,8 @@ void mixedReplace(const CgBuffers& B, cudaStream_t s);  // x += dx, r = b - A x 
 // half-diagonal inner operator (sdia.cu): offsets stored, the builder from the df32 band (the hi
 // parts, as the CSR gather takes them) and the product t = A x with block partials of x.t
 int sdiaHalf(const int* p);
+// the largest linear offset |L| of the neighbour box: the zero padding the product needs around x
+int sdiaReach(const SdiaOp& A);
 void sdiaBuild(const SdiaOp& A, const SdiaBand& B, const df32* band, float* d, cudaStream_t s);
 int sdiaPartials(const SdiaOp& A);
 // encode the TMA tensor maps of A's diagonals and of the vector x into out2 (two CUtensorMap, 64-byte

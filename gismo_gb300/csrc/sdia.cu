@@ -43,7 +43,12 @@ __host__ __device__ inline int halfCount(const int* p) {
 __global__ void __launch_bounds__(kB) k_sdia_build(SdiaOp A, SdiaBand B, const df32* __restrict__ band,
                                                   float* __restrict__ d) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= A.n) return;
+    const long long ns = A.ns;
+    if (r >= ns) return;
+    if (r >= A.n) {  // the padding of every diagonal holds zeros (the products read it times x = 0)
+        for (int h = 0; h < A.nh; ++h) d[h * ns + r] = 0.f;
+        return;
+    }
     int b[3];
     b[0] = r % A.m[0];
     b[1] = (r / A.m[0]) % A.m[1];
@@ -59,7 +64,6 @@ __global__ void __launch_bounds__(kB) k_sdia_build(SdiaOp A, SdiaBand B, const d
                              (long long)(o2 + A.p[2]) * n0W * n1W;
         return band[bi].hi;
     };
-    const long long ns = A.ns;
     int h = 0;
     for (int o0 = 0; o0 <= A.p[0]; ++o0, ++h) d[h * ns + r] = value(o0, 0, 0);
     for (int o2 = 0; o2 <= A.p[2]; ++o2)
@@ -67,78 +71,64 @@ __global__ void __launch_bounds__(kB) k_sdia_build(SdiaOp A, SdiaBand B, const d
             for (int o0 = -A.p[0]; o0 <= A.p[0]; ++o0, ++h) d[h * ns + r] = value(o0, o1, o2);
 }
 
-// L2 prefetch of `count` consecutive diagonals' segments [r0, r0 + kB) (kB floats = 1 KB each; the
-// diagonal stride is a multiple of kB floats, so every segment is 16-byte aligned and inside the
-// allocation)
-__device__ __forceinline__ void prefetchSegments(const float* seg, long long ns, int count) {
-    for (int k = 0; k < count; ++k)
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(seg + k * ns), "r"(kB * 4) : "memory");
-}
-
 __device__ __forceinline__ double warpSumD(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
 
+__device__ __forceinline__ void prefetchL2(const float* a) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+}
+
 // t = A x from the half diagonals (one thread per row, grid-stride) and block partial sums of x.t
-// (the p.Ap of the inner CG), in FP64 over FP32 products as in the CSR kernel
+// (the p.Ap of the inner CG), in FP64 over FP32 products as in the CSR kernel. x carries A.xpad >=
+// max L zeros before and after its n entries, and the diagonals' padding [n, ns) holds zeros, so
+// every index below stays in allocated memory and a term whose row or column leaves [0, n) is a
+// product with a zero: the mirrored index h ns + r - L with r - L < 0 falls into diagonal h - 1
+// (finite there) and meets x[r - L] = 0; an upper term with r + L >= n has d = 0 (the tensor point
+// r + o lies outside the box) and x[r + L] = 0. The row's own values d[h ns + r] are the only
+// ones read from HBM first (the mirrored ones were read by their own rows at about the same
+// time): each warp prefetches them into L2 two lines ahead.
 template <int P0>
 __global__ void __launch_bounds__(kB) k_sdia32_dot(SdiaOp A, const float* __restrict__ x, float* __restrict__ t,
                                                    double* __restrict__ part, const CgState* __restrict__ st) {
     if (st->done || st->pause) return;
+    constexpr int W0 = 2 * P0 + 1;
+    constexpr int kAhead = 2;
     const int n = A.n;
     const long long ns = A.ns;
-    constexpr int W0 = 2 * P0 + 1;
-    // lines of the half box after the centre line: (o2, o1) with o2 > 0 or (o2 = 0, o1 > 0)
     const int nlines = A.p[1] + A.p[2] * (2 * A.p[1] + 1);
-    constexpr int kAhead = 3;  // lines whose segments are prefetched ahead of their use
     double contrib = 0.0;
     for (int base = blockIdx.x * kB; base < n; base += gridDim.x * kB) {
         const int r = base + threadIdx.x;
-        // one thread streams this block's segments of the next lines into L2 (the first touch of
-        // a stored value, by its own row, then hits L2 instead of waiting on HBM)
-        if (threadIdx.x == 0) {
-            prefetchSegments(A.d + base, ns, P0 + 1);
-            for (int l = 0; l < kAhead && l < nlines; ++l)
-                prefetchSegments(A.d + (P0 + 1 + (long long)l * W0) * ns + base, ns, W0);
-        }
-        float acc = 0.f;
         if (r < n) {
-            // Every load below is in bounds: x indices are clamped to [0, n), and the mirrored
-            // value d[h ns + r - L] (h >= 1, 0 < L < n <= ns) lies in diagonal h or h - 1. A clamped
-            // x index pairs with a zero value: d[h ns + r] = 0 when r + L >= n (the tensor point
-            // r + o then lies outside the box), and the mirrored value is replaced by 0 when
-            // r - L < 0.
+            float acc = 0.f;
             const float* dh = A.d + r;
+            for (int l = 0; l < kAhead && l < nlines; ++l)
+#pragma unroll
+                for (int k = 0; k < W0; ++k) prefetchL2(dh + (P0 + 1 + l * W0 + k) * ns);
             // centre line: o = (0, 0, o0), o0 = 0..P0 (the diagonal first)
 #pragma unroll
             for (int o0 = 0; o0 <= P0; ++o0) {
-                const float vu = __ldcg(dh);
-                const float xu = __ldg(x + min(r + o0, n - 1));
-                acc = fmaf(vu, xu, acc);
-                if (o0 > 0) {
-                    const float vr = __ldcg(dh - o0);
-                    const float vd = r - o0 >= 0 ? vr : 0.f;
-                    const float xd = __ldg(x + max(r - o0, 0));
-                    acc = fmaf(vd, xd, acc);
-                }
+                acc = fmaf(__ldcg(dh), __ldg(x + r + o0), acc);
+                if (o0 > 0) acc = fmaf(__ldcg(dh - o0), __ldg(x + r - o0), acc);
                 dh += ns;
             }
             int line = 0;
             for (int o2 = 0; o2 <= A.p[2]; ++o2)
                 for (int o1 = o2 ? -A.p[1] : 1; o1 <= A.p[1]; ++o1, ++line) {
-                    if (threadIdx.x == 0 && line + kAhead < nlines)
-                        prefetchSegments(A.d + (P0 + 1 + (long long)(line + kAhead) * W0) * ns + base, ns, W0);
+                    if (line + kAhead < nlines)
+#pragma unroll
+                        for (int k = 0; k < W0; ++k) prefetchL2(dh + (kAhead * W0 + k) * ns);
                     const int L21 = (o2 * A.m[1] + o1) * A.m[0];
                     float vu[W0], xu[W0], vd[W0], xd[W0];
 #pragma unroll
                     for (int k = 0; k < W0; ++k) {
                         const int L = L21 + k - P0;
                         vu[k] = __ldcg(dh + k * ns);
-                        const float vr = __ldcg(dh + k * ns - L);
-                        vd[k] = r - L >= 0 ? vr : 0.f;
-                        xu[k] = __ldg(x + min(r + L, n - 1));
-                        xd[k] = __ldg(x + max(r - L, 0));
+                        vd[k] = __ldcg(dh + k * ns - L);
+                        xu[k] = __ldg(x + r + L);
+                        xd[k] = __ldg(x + r - L);
                     }
                     // a line's 2 (2 P0 + 1) products are summed first, then added to the row sum:
                     // two short FP32 chains instead of one of (2p+1)^3 terms
@@ -160,12 +150,11 @@ __global__ void __launch_bounds__(kB) k_sdia32_dot(SdiaOp A, const float* __rest
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = contrib;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int w = 0; w < kB / 32; ++w) s += ws[w];
-        part[blockIdx.x] = s;
+        double sum = 0.0;
+        for (int w = 0; w < kB / 32; ++w) sum += ws[w];
+        part[blockIdx.x] = sum;
     }
 }
-
 
 // ---------------------------------------------------------------------------------------------
 // The same product fed by the Tensor Memory Accelerator. A block owns tiles of kTmaT consecutive
@@ -379,8 +368,10 @@ namespace launch {
 int sdiaHalf(const int* p) { return halfCount(p); }
 
 void sdiaBuild(const SdiaOp& A, const SdiaBand& B, const df32* band, float* d, cudaStream_t s) {
-    if (A.n > 0) k_sdia_build<<<unsigned((A.n + kB - 1) / kB), kB, 0, s>>>(A, B, band, d);
+    if (A.n > 0) k_sdia_build<<<unsigned((A.ns + kB - 1) / kB), kB, 0, s>>>(A, B, band, d);
 }
+
+int sdiaReach(const SdiaOp& A) { return A.p[0] + A.m[0] * (A.p[1] + A.m[1] * A.p[2]); }
 
 int sdiaPartials(const SdiaOp& A) {
     if (A.tmaps) return std::max(1, std::min((A.n + kTmaT - 1) / kTmaT, 152 * kTmaBlocksPerSm));

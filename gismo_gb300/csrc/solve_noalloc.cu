@@ -4,7 +4,8 @@
 // array (kNoAllocScratchDoubles doubles = 8 MiB), which every GPU that loads the library keeps
 // until the process exits. The iteration is the one of gsgpu_solve (the same kernels, launched
 // one chunk at a time without a CUDA graph, so nothing is instantiated or allocated); only the
-// Jacobi diagonal is found on the device by a binary search in each sorted CSR row.
+// Jacobi diagonal is found on the device by a binary search in each sorted CSR row. Each call
+// reads the row-pointer end and the solver state back to the host and synchronises its stream.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -82,15 +83,27 @@ extern "C" int gsgpu_cg_jacobi_noalloc(int n, const int* ptr, const int* col, co
         scratch = g_scratch_addr[dev];
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    int nnz_end = 0;
-    if (cudaMemcpyAsync(&nnz_end, ptr + n, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
-        return GSGPU_ERR_CUDA;
-    const double avg = double(nnz_end) / n;
+    // an error the caller already had pending is reported as such and left pending, not taken
+    // for this call's
+    if (cudaPeekAtLastError() != cudaSuccess) return GSGPU_ERR_CUDA;
     const long long np = (n + 255) / 256;
-    const long long nb = (n + 7) / 8;
     CgState* st = reinterpret_cast<CgState*>(scratch);
     int* flag = reinterpret_cast<int*>(scratch + kStateDoubles - 1);
+    double* w = scratch + kStateDoubles;
+    double* dinv = w;
+    // the array keeps the previous call's contents: clear the error flag before use
+    if (cudaMemsetAsync(flag, 0, sizeof(int), s) != cudaSuccess) return GSGPU_ERR_CUDA;
+    k_dinv_search<<<unsigned((n + 255) / 256), 256, 0, s>>>(n, ptr, col, val, dinv, flag);
+    if (cudaGetLastError() != cudaSuccess) return GSGPU_ERR_CUDA;
+    // the row-pointer end (the average row length picks the lanes per row) and the diagonal flag in
+    // one round trip; a row without a non-zero diagonal is rejected before any iteration
+    int nnz_end = 0, hflag = 0;
+    if (cudaMemcpyAsync(&nnz_end, ptr + n, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return GSGPU_ERR_CUDA;
+    if (hflag) return GSGPU_ERR_INVALID;
+    const double avg = double(nnz_end) / n;
     CgBuffers B;
     B.n = n;
     B.lanes_per_row = avg > 48 ? 32 : (avg > 20 ? 16 : (avg > 10 ? 8 : 4));
@@ -99,8 +112,6 @@ extern "C" int gsgpu_cg_jacobi_noalloc(int n, const int* ptr, const int* col, co
     B.val = val;
     B.b = b;
     B.x = x;
-    double* w = scratch + kStateDoubles;
-    double* dinv = w;
     B.dinv = dinv;
     B.r = w + n;
     B.z = w + 2LL * n;
@@ -108,16 +119,12 @@ extern "C" int gsgpu_cg_jacobi_noalloc(int n, const int* ptr, const int* col, co
     B.t = w + 4LL * n;
     B.part0 = w + 5LL * n;
     B.part1 = B.part0 + np;
-    B.part2 = B.part1 + np;  // nb >= SpMV blocks for every lanes-per-row choice
-    (void)nb;
+    B.part2 = B.part1 + np;  // (n + 7) / 8 doubles: at least the SpMV blocks of every lanes-per-row choice
     B.st = st;
-    // the array keeps the previous call's contents: clear the error flag before use
-    if (cudaMemsetAsync(flag, 0, sizeof(int), s) != cudaSuccess) return GSGPU_ERR_CUDA;
-    k_dinv_search<<<unsigned((n + 255) / 256), 256, 0, s>>>(n, ptr, col, val, dinv, flag);
-    launch::cgInit(B, tol > 0 ? tol : 1e-10, max_iters > 0 ? max_iters : 1000, s);
     const int maxit = max_iters > 0 ? max_iters : 1000;
+    launch::cgInit(B, tol > 0 ? tol : 1e-10, maxit, s);
+    if (cudaGetLastError() != cudaSuccess) return GSGPU_ERR_CUDA;
     CgState hs{};
-    int hflag = 0;
     const int chunk = 16;
     for (int it = 0; it < maxit + chunk; it += chunk) {
         for (int k = 0; k < chunk; ++k) launch::cgIteration(B, s);
@@ -126,11 +133,8 @@ extern "C" int gsgpu_cg_jacobi_noalloc(int n, const int* ptr, const int* col, co
             return GSGPU_ERR_CUDA;
         if (hs.done) break;
     }
-    if (cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess)
-        return GSGPU_ERR_CUDA;
+    if (cudaGetLastError() != cudaSuccess) return GSGPU_ERR_CUDA;
     if (iterations) *iterations = hs.iters;
     if (relres) *relres = hs.relres;
-    if (hflag) return GSGPU_ERR_INVALID;  // a row without a non-zero diagonal
     return hs.done == 1 ? GSGPU_OK : GSGPU_ERR_NOT_CONVERGED;
 }

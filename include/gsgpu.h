@@ -233,20 +233,23 @@ int gsgpu_set_profiling(gsgpu_context* ctx, int on);
 int gsgpu_spmv_stats(gsgpu_context* ctx, long long* launches, double* total_ms, double* bytes_per_launch);
 /* Jacobi-preconditioned CG on a CSR system already in device memory, allocating no device
  * memory. No counterpart in the reference.
- * For callers that cannot call cudaMalloc: code that runs while a CUDA graph is being captured
- * in global mode (where cudaMalloc is an error), processes whose device memory is already handed
- * to a pool allocator sized to the GPU, and latency-bound loops that cannot afford the implicit
- * device synchronisation of an allocation. The caller passes the matrix (n rows, ptr/col/val
- * with sorted columns and a non-zero diagonal in every row), the right-hand side b and the
- * output x, all device pointers on the current device, and the stream to run on; x is
- * overwritten with the solution (the start vector is 0), and the stopping rule, iteration count
- * and relative residual are those of gsgpu_solve with GSGPU_SOLVER_CG_JACOBI. The working
- * vectors live in one fixed 8 MiB device array built into the library, which limits n to
- * 204,276 unknowns; a larger n returns GSGPU_ERR_INVALID before any device work. Every call
- * shares that array, so calls whose work overlaps on the GPU (other streams, other host
- * threads) race and must be serialised by the caller. The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture. */
+ * For callers that cannot call cudaMalloc: processes whose device memory is already handed to a
+ * pool allocator sized to the GPU (a further cudaMalloc fails or evicts the pool's blocks), and
+ * latency-bound loops that cannot afford the implicit device synchronisation of an allocation.
+ * The caller passes the matrix (n rows, ptr/col/val with sorted columns and a non-zero diagonal in
+ * every row), the right-hand side b and the output x, all device pointers on the current device,
+ * and the stream to run on; x is overwritten with the solution (the start vector is 0), and the
+ * stopping rule, iteration count and relative residual are those of gsgpu_solve with
+ * GSGPU_SOLVER_CG_JACOBI. Each call reads the row-pointer end and the solver state back to the
+ * host and synchronises `stream`, so it must not be called while that stream (or, in global
+ * capture mode, any stream) is being captured into a CUDA graph. A row without a non-zero
+ * diagonal returns GSGPU_ERR_INVALID before any iteration; an error already pending on entry
+ * returns GSGPU_ERR_CUDA and stays pending. The working vectors live in one fixed 8 MiB device
+ * array built into the library, which limits n to 204,276 unknowns; a larger n returns
+ * GSGPU_ERR_INVALID before any device work. Every call shares that array, so calls whose work
+ * overlaps on the GPU (other streams, other host threads) race and must be serialised by the
+ * caller. The first call on a device looks up the array's device address (cudaGetSymbolAddress)
+ * with that device current. */
 int gsgpu_cg_jacobi_noalloc(int n, const int* ptr, const int* col, const double* val, const double* b, double* x,
                             double tol, int max_iters, void* stream, int* iterations, double* relres);
 /* smallest det J over all quadrature points of the last assemble() */

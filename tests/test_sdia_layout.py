@@ -3,8 +3,8 @@
 The layout stores, for a symmetric matrix on a box of m0 x m1 x m2 unknowns numbered
 lexicographically with the neighbour box [-p, p]^3, only the diagonals of the lexicographically
 non-negative half offsets; the product reads every stored value twice (its own row and the mirrored
-one). This test restates the builder's offset order and the kernel's index arithmetic (clamped x
-indices, the mirrored value zeroed for a negative row) in numpy and checks the product against the
+one). This test restates the builder's offset order and the kernel's index arithmetic (zero padding
+around x and after every diagonal, unclamped indices) in numpy and checks the product against the
 full sparse matrix, on boxes down to the smallest width the library accepts (2p + 1)."""
 import itertools
 
@@ -54,18 +54,25 @@ def build_half(A, m, p):
     return d, H
 
 
-def half_product(d, H, m, x):
+def half_product(d, H, m, x, ns):
+    """The kernel's arithmetic: diagonals of stride ns whose padding [n, ns) holds zeros, x with
+    `reach` zeros before and after it, no clamping: the mirrored value of row r comes from flat index
+    h ns + r - L even when r - L < 0 (diagonal h - 1, multiplied by a padding zero of x)."""
     n = len(x)
     r = np.arange(n)
+    reach = max(abs(o[0] + m[0] * (o[1] + m[1] * o[2])) for o in H)
+    xp = np.concatenate([np.zeros(reach), x, np.zeros(reach)])
+    flat = np.zeros(len(H) * ns)
+    for h in range(len(H)):
+        flat[h * ns:h * ns + n] = d[h]
     y = np.zeros(n)
     for h, o in enumerate(H):
         L = o[0] + m[0] * (o[1] + m[1] * o[2])
-        y += d[h] * x[np.minimum(r + L, n - 1)]
+        y += flat[h * ns + r] * xp[reach + r + L]
         if L != 0:
-            flat = d.ravel()
-            vr = flat[h * n + r - L]  # in bounds for h >= 1 and 0 < L < n
-            vd = np.where(r - L >= 0, vr, 0.0)
-            y += vd * x[np.maximum(r - L, 0)]
+            idx = h * ns + r - L
+            assert idx.min() >= 0 and idx.max() < len(flat)
+            y += flat[idx] * xp[reach + r - L]
     return y
 
 
@@ -78,9 +85,10 @@ def test_half_diagonal_product_equals_full_product(m, p):
     assert len(H) == 1 + (np.prod([2 * pk + 1 for pk in p]) - 1) // 2
     # every non-zero of the half box is stored exactly once; the other half is its mirror
     assert np.count_nonzero(d) * 2 - np.count_nonzero(d[0]) == A.nnz
+    ns = (A.shape[0] + 255) // 256 * 256
     for _ in range(3):
         x = rng.standard_normal(A.shape[0])
-        assert np.allclose(half_product(d, H, m, x), A @ x, rtol=1e-13, atol=1e-12)
+        assert np.allclose(half_product(d, H, m, x, ns), A @ x, rtol=1e-13, atol=1e-12)
     # all mirrored reads stay inside the stored array (the kernel's unclamped value index)
     n = A.shape[0]
     for h, o in enumerate(H):
