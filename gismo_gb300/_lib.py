@@ -16,8 +16,13 @@ EXPORTS = [
     "gsgpu_set_profiling", "gsgpu_spmv_stats", "gsgpu_cg_jacobi_noalloc", "gsgpu_set_batch", "gsgpu_batch_info",
     "gsgpu_batch_l2_error", "gsgpu_server_create", "gsgpu_server_submit", "gsgpu_server_wait",
     "gsgpu_server_last_error", "gsgpu_server_destroy", "gsgpu_apply", "gsgpu_mg_apply", "gsgpu_set_fixed_dofs",
-    "gsgpu_h1_error", "gsgpu_batch_h1_error",
+    "gsgpu_h1_error", "gsgpu_batch_h1_error", "gsgpu_autotune", "gsgpu_tuned_variants", "gsgpu_tune_save",
+    "gsgpu_tune_load", "gsgpu_tune_clear",
 ]
+
+# the tuning table measured on GB300 (written by gsgpu_tune_save after gsgpu_autotune runs on the
+# benchmark configurations); loaded with the library, so contexts take their kernel variants from it
+TUNING_PATH = os.path.join(HERE, "tuning.txt")
 
 OK, ERR_INVALID, ERR_CUDA, ERR_BUDGET, ERR_NOT_CONVERGED, ERR_JACOBIAN, ERR_STATE, ERR_TIMEOUT = range(8)
 SOLVER_CG_JACOBI, SOLVER_CG_MG = 0, 1
@@ -111,8 +116,16 @@ def lib() -> C.CDLL:
         L.gsgpu_spmv_stats.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.gsgpu_cg_jacobi_noalloc.argtypes = [C.c_int, vp, vp, vp, vp, vp, C.c_double, C.c_int, vp,
                                                C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        L.gsgpu_autotune.argtypes = [vp, vp]
+        L.gsgpu_tuned_variants.argtypes = [vp, vp]
+        L.gsgpu_tune_save.argtypes = [C.c_char_p]
+        L.gsgpu_tune_load.argtypes = [C.c_char_p]
+        L.gsgpu_tune_clear.argtypes = []
         for name in EXPORTS:
             if name != "gsgpu_last_error":
                 getattr(L, name).restype = C.c_int
+        if os.path.exists(TUNING_PATH) and not os.environ.get("GSGPU_NO_TUNING_TABLE"):
+            if L.gsgpu_tune_load(TUNING_PATH.encode()) != OK:
+                raise ImportError(f"{TUNING_PATH} is not a valid tuning table")
         _LIB = L
     return _LIB

@@ -214,6 +214,20 @@ class GpuPoissonAssembler:
         self._check(self.L.gsgpu_stream(self.h, C.byref(v)))
         return v.value or 0
 
+    def autotune(self):
+        """Time every kernel variant on this problem, record the fastest in the process-wide tuning
+        table and apply it (gsgpu_autotune). Returns the measured milliseconds: six stiffness
+        combinations and two inner products (-1 where not applicable)."""
+        ms = np.empty(8, np.float64)
+        self._check(self.L.gsgpu_autotune(self.h, ms.ctypes.data))
+        return ms
+
+    def tuned_variants(self):
+        """(stage 1, stage 2, inner product) variants of this context (gsgpu_tuned_variants)."""
+        v = np.empty(3, np.int32)
+        self._check(self.L.gsgpu_tuned_variants(self.h, v.ctypes.data))
+        return tuple(int(a) for a in v)
+
     def set_profiling(self, on: bool):
         self._check(self.L.gsgpu_set_profiling(self.h, int(on)))
 
@@ -225,7 +239,10 @@ class GpuPoissonAssembler:
     # ---- gsConjugateGradient ----
     def solve(self, tol: float = 1e-10, max_iters: int = 1000, method: str = "jacobi", precision: str = "fp64",
               mg_levels: int = 4, mg_npre: int = 2, mg_npost: int = 2, mg_damping: float = 0.6,
-              inner_tol: float = 1e-4, download: bool = True, mg_cycles: int = 1, mg_cgc_damping: float = 1.0):
+              inner_tol: float = 1e-4, download: bool = True, mg_cycles: int = 1, mg_cgc_damping: float = 1.0,
+              out: Optional[np.ndarray] = None):
+        """`out`: a caller-owned contiguous float64 array of numDofs() entries (for instance a view of
+        pinned host memory) that receives the solution instead of a new array."""
         o = SolverOpts()
         o.method = _lib.SOLVER_CG_JACOBI if method == "jacobi" else _lib.SOLVER_CG_MG
         o.precision = _lib.PREC_FP64 if precision == "fp64" else _lib.PREC_MIXED
@@ -234,7 +251,12 @@ class GpuPoissonAssembler:
         o.mg_cycles, o.mg_cgc_damping = mg_cycles, mg_cgc_damping
         o.inner_tol = inner_tol
         info = SolveInfo()
-        x = np.empty(self.sizes()[0], np.float64) if download else None
+        if out is not None:
+            if out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"] or out.size != self.sizes()[0]:
+                raise ValueError("out must be a contiguous float64 array of numDofs() entries")
+            x, download = out, True
+        else:
+            x = np.empty(self.sizes()[0], np.float64) if download else None
         rc = self.L.gsgpu_solve(self.h, C.byref(o), x.ctypes.data if download else None, C.byref(info))
         if rc not in (_lib.OK, _lib.ERR_NOT_CONVERGED):
             self._check(rc)
@@ -342,3 +364,19 @@ class GpuPoissonServer:
             self.close()
         except Exception:
             pass
+
+
+def tune_save(path: str) -> None:
+    """Write the process-wide tuning table (gsgpu_tune_save)."""
+    if _lib.lib().gsgpu_tune_save(path.encode()) != _lib.OK:
+        raise GsGpuError(_lib.ERR_INVALID, f"could not write the tuning table {path}")
+
+
+def tune_load(path: str) -> None:
+    """Add the entries of a tuning table file to the process-wide table (gsgpu_tune_load)."""
+    if _lib.lib().gsgpu_tune_load(path.encode()) != _lib.OK:
+        raise GsGpuError(_lib.ERR_INVALID, f"could not read the tuning table {path}")
+
+
+def tune_clear() -> None:
+    _lib.lib().gsgpu_tune_clear()

@@ -114,7 +114,8 @@ def run_multigrid(args, sampler):
     from gismo_gb300.assembler import GpuPoissonAssembler
     from oracle import oracle as O
     damping = args.mg_damping
-    prob = P.cube_grid(n=8, n_elem=16, p=2, seed=3, amp=0.03, kappa_modes=32)
+    prob = P.cube_grid(n=getattr(args, "mg_grid", 8), n_elem=getattr(args, "mg_elems", 16), p=2, seed=3, amp=0.03,
+                       kappa_modes=32)
     A = GpuPoissonAssembler(prob, device=0)
     nfree, nnz, _, _ = A.sizes()
     tol = 1e-9
@@ -142,7 +143,9 @@ def run_multigrid(args, sampler):
                          err=float(np.linalg.norm(x - xref) / np.linalg.norm(xref)))
     mixed = nfree / (out["mixed"]["ms"] / 1e3)
     fp64 = nfree / (out["fp64"]["ms"] / 1e3)
-    cfg = {"workload": "cube_grid_8x8x8_p2_16^3", "patches": 512, "free_dofs": nfree, "nnz": nnz, "tol": tol,
+    ng, ne = getattr(args, "mg_grid", 8), getattr(args, "mg_elems", 16)
+    cfg = {"workload": f"cube_grid_{ng}x{ng}x{ng}_p2_{ne}^3", "patches": ng ** 3, "free_dofs": nfree, "nnz": nnz,
+           "tol": tol,
            "solver": f"CG + 4-level h-multigrid V-cycle, 2+2 damped Jacobi sweeps, omega={damping}",
            "omega_note": "omega=0.6 makes the Jacobi smoother divergent on these 16^3-element p=2 patches "
                          "(omega*lambda_max(D^-1 A) = 2.17 > 2): the reference's own gsMultiGridOp stalls there",

@@ -141,6 +141,8 @@ void Context::refresh() {
         nnz = (long long)pat.col.size();
     }
     if (batch) segRow = segmentRows(pd, map);
+    setupSdia();
+    applyTuning();
     if (device < 0) {  // host-only context: the plan, no device buffers
         refreshed = true;
         return;
@@ -149,7 +151,6 @@ void Context::refresh() {
     if (devPattern) patternOnDevice(rp);
     else patternFromHost();
     findBoxRows();
-    setupSdia();
     if (batch) batchSetup();
     allocN(arena, dVal, nnz);
     allocN(arena, dRhs, pat.n);
@@ -530,21 +531,23 @@ void Context::assemble(int precision) {
     // K3: sum-factorised stiffness contraction into the band
     if (mixed) {
         // row-blocked df32 contractions (all band offsets of a row function per work item), one
-        // launch per degree class along each stage axis
-        // output fields per launch: 4 (fewer input re-reads) or 2 (fewer registers, more warps)
-        const bool nh2 = rowGroup2();
+        // launch per degree class along each stage axis. Per degree the variant comes from the
+        // tuning table (autotune.cu): 3D stage 1 in shared-memory tiles or rows with 4 or 2 output
+        // fields per launch (4: fewer input re-reads, 2: fewer registers, more warps); 3D stage 2
+        // rows with 4 or 2 output fields. Every variant forms the same sums in the same order.
         for (int P = 1; P <= 4; ++P) {
             auto nb = [&](int st) { return (long long)tabRow[st][P].h.size(); };
             auto nbB = [&](int st) { return (long long)tabRowB[st][P].h.size(); };
-            if (pd.dim == 3 && nh2) {
+            const int v31 = tuned31[P];
+            if (pd.dim == 3 && v31 == kStage31RowsNh2) {
                 launch::contractRowDF<31, 0, 2>(P, dPatches, tabRow[0][P].d, nb(0), tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
                 launch::contractRowDF<31, 2, 2>(P, dPatches, tabRow[0][P].d, nb(0), tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
                 launch::contractRowDF<31, 4, 2>(P, dPatches, tabRow[0][P].d, nb(0), tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
                 launch::contractRowDF<31, 6, 2>(P, dPatches, tabRow[0][P].d, nb(0), tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
             } else if (pd.dim == 3) {
-                // interior rows: shared-memory tiles where the degree allows them (they cover the same
-                // patches as tabRow[0][P]), else the unrolled row kernel
-                const bool tiled = dev::tiledStage31(P) && std::getenv("GSGPU_NO_TILE31") == nullptr;
+                // interior rows in shared-memory tiles (they cover the same patches as tabRow[0][P]) or
+                // the unrolled row kernel; boundary rows always by rows
+                const bool tiled = v31 == kStage31Tiles && dev::tiledStage31(P);
                 const long long ni = tiled ? 0 : nb(0);
                 if (tiled)
                     launch::stage31Tile(P, dPatches, tabTile31[P].d, (long long)tabTile31[P].h.size(), cDf, sDf, pfDf, s);
@@ -557,7 +560,7 @@ void Context::assemble(int precision) {
         for (int P = 1; P <= 4; ++P) {
             auto nb = [&](int st) { return (long long)tabRow[st][P].h.size(); };
             auto nbB = [&](int st) { return (long long)tabRowB[st][P].h.size(); };
-            if (pd.dim == 3 && nh2) {
+            if (pd.dim == 3 && tuned32[P] == kStage32RowsNh2) {
                 launch::contractRowDF<32, 0, 2>(P, dPatches, tabRow[1][P].d, nb(1), tabRowB[1][P].d, nbB(1), sDf, uDf, dIbuf, pfDf, s);
                 launch::contractRowDF<32, 2, 2>(P, dPatches, tabRow[1][P].d, nb(1), tabRowB[1][P].d, nbB(1), sDf, uDf, dIbuf, pfDf, s);
             } else if (pd.dim == 3) {
@@ -744,19 +747,15 @@ void Context::ensureSolveBuffers() {
     allocN(arena, dP, n);
     allocN(arena, dT, n);
     allocN(arena, dDinv, n);
-    allocN(arena, dPart0, launch::cgPartials(n));
-    allocN(arena, dPart1, launch::cgPartials(n));
+    // partials: one per block of the widest grid that writes them (the persistent inner iteration
+    // runs up to kMaxSpmvBlocks blocks)
+    allocN(arena, dPart0, std::max(launch::cgPartials(n), launch::kMaxSpmvBlocks));
+    allocN(arena, dPart1, std::max(launch::cgPartials(n), launch::kMaxSpmvBlocks));
     // SpMV partials: one per SpMV block; the most blocks are launched with 32 lanes per row
-    allocN(arena, dPart2, std::max({launch::cgPartials(n), launch::spmvPartials(n, 32),
+    allocN(arena, dPart2, std::max({launch::cgPartials(n), launch::spmvPartials(n, 32), launch::kMaxSpmvBlocks,
                                     sdiaOk ? launch::sdiaPartials(sdiaOp) : 0}));
     dCg = static_cast<CgState*>(arena.alloc(sizeof(CgState)));
     solveN = n;
-}
-
-// df32 contraction output-group width (tuning override GSGPU_ROW_NH=2|4; measured default below)
-bool Context::rowGroup2() const {
-    if (const char* e = std::getenv("GSGPU_ROW_NH")) return std::atoi(e) == 2;
-    return false;
 }
 
 // lanes per CSR row of the SpMV kernels: long rows use 16 lanes for FP32 values (the load rate
@@ -912,16 +911,27 @@ void Context::ensureMixedBuffers() {
         allocN(arena, dSdiaErr, 1);
         GSGPU_CUDA_TRY(cudaMemsetAsync(dSdiaErr, 0, sizeof(int), stream));
         sdiaOp.err = dSdiaErr;
-        // the TMA-fed product on request (GSGPU_SDIA_TMA=1); the load-based one is the default: on
-        // GB300 it measured faster (C2 inner product 0.061 vs 0.087 ms)
-        sdiaOp.tmaps = nullptr;
-        if (std::getenv("GSGPU_SDIA_TMA")) {
-            std::string why;
-            if (launch::sdiaTensorMaps(sdiaOp, dP32, sdiaMaps, &why)) sdiaOp.tmaps = sdiaMaps;
-            else if (std::getenv("GSGPU_REQUIRE_TMA"))  // the tests' guard that the TMA product runs
-                throw std::runtime_error("TMA half-diagonal product unavailable: " + why);
-        }
+        setInnerVariant();
     }
+}
+
+// the half-diagonal inner product of the tuned variant: TMA-fed (tensor maps of the diagonals and of
+// the direction vector) or load-based, the default: on GB300 the load-based one measured faster
+// (C2 inner product 0.058 vs 0.087 ms). False when the TMA maps are refused (the load-based product
+// stays; GSGPU_REQUIRE_TMA=1 makes that an error, for the tests). The captured solver graph holds
+// the product's launch and is dropped.
+bool Context::setInnerVariant() {
+    if (!sdiaOk || !dSdia) return false;
+    if (gexecMixed) cudaGraphExecDestroy(gexecMixed), gexecMixed = nullptr;
+    sdiaOp.tmaps = nullptr;
+    if (tunedInner != kInnerSdiaTma) return true;
+    std::string why;
+    if (launch::sdiaTensorMaps(sdiaOp, dP32, sdiaMaps, &why)) {
+        sdiaOp.tmaps = sdiaMaps;
+        return true;
+    }
+    if (std::getenv("GSGPU_REQUIRE_TMA")) throw std::runtime_error("TMA half-diagonal product unavailable: " + why);
+    return false;
 }
 
 void Context::solveMixed(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
@@ -988,7 +998,8 @@ void Context::solveMixed(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
     } else {
         // chunks of FP32 iterations followed by one residual replacement, captured as a graph
         // (once per context)
-        if (!gexecMixed || gexecLpr[1] != B.lanes_per_row) {
+        const int graphKey = B.lanes_per_row;
+        if (!gexecMixed || gexecLpr[1] != graphKey) {
             if (gexecMixed) cudaGraphExecDestroy(gexecMixed);
             gexecMixed = nullptr;
             cudaGraph_t g;
@@ -998,7 +1009,7 @@ void Context::solveMixed(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
             GSGPU_CUDA_TRY(cudaStreamEndCapture(s, &g));
             GSGPU_CUDA_TRY(cudaGraphInstantiate(&gexecMixed, g, 0));
             cudaGraphDestroy(g);
-            gexecLpr[1] = B.lanes_per_row;
+            gexecLpr[1] = graphKey;
         }
         cudaGraphExec_t exec = gexecMixed;
         for (int c = 0; c < maxit / chunk + 2; ++c) {
@@ -1377,6 +1388,28 @@ int gsgpu_spmv_stats(gsgpu_context* ctx, long long* launches, double* total_ms, 
         if (total_ms) *total_ms = ctx->c.spmvMs;
         if (bytes_per_launch) *bytes_per_launch = ctx->c.spmvBytes;
     });
+}
+
+int gsgpu_autotune(gsgpu_context* ctx, double* ms8) {
+    return guarded(ctx, [&] { ctx->c.autotune(ms8); });
+}
+
+int gsgpu_tuned_variants(gsgpu_context* ctx, int* v3) {
+    return guarded(ctx, [&] {
+        if (!v3) throw std::invalid_argument("tuned_variants: null output");
+        if (!ctx->c.refreshed) throw gsgpu::StateError("tuned_variants() before refresh()");
+        const gsgpu::DevPatch& D = ctx->c.L.dev.at(0);
+        v3[0] = ctx->c.tuned31[std::min(4, std::max(1, D.p[0]))];
+        v3[1] = ctx->c.tuned32[std::min(4, std::max(1, D.p[1]))];
+        v3[2] = ctx->c.sdiaOk ? ctx->c.tunedInner : -1;
+    });
+}
+
+int gsgpu_tune_save(const char* path) { return path && gsgpu::tuneSave(path) ? GSGPU_OK : GSGPU_ERR_INVALID; }
+int gsgpu_tune_load(const char* path) { return path && gsgpu::tuneLoad(path) ? GSGPU_OK : GSGPU_ERR_INVALID; }
+int gsgpu_tune_clear(void) {
+    gsgpu::tuneClear();
+    return GSGPU_OK;
 }
 
 int gsgpu_min_jacobian(gsgpu_context* ctx, double* detmin) {

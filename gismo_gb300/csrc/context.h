@@ -16,6 +16,7 @@
 #include "kernels_solve.h"
 #include "mg_plan.h"
 #include "plan.h"
+#include "autotune.h"
 
 namespace gsgpu {
 
@@ -158,6 +159,13 @@ struct Context {
     bool sdiaOk = false;
     SdiaOp sdiaOp;
     SdiaBand sdiaBand;
+    // kernel variants of this problem from the tuning table (autotune.cu), per degree class
+    int tuned31[5] = {0, 0, 0, 0, 0}, tuned32[5] = {0, 0, 0, 0, 0}, tunedInner = 0;
+    void applyTuning();
+    bool setInnerVariant();
+    // time every variant on this problem, record the fastest in the table, apply it; ms[k]: the time
+    // of each stiffness combination (6) and each inner-product variant (2)
+    void autotune(double* ms);
     float* dSdia = nullptr;
     float* dP32pad = nullptr;         // allocation of the inner CG direction with its zero padding
     int* dSdiaErr = nullptr;          // set by the TMA-fed product's bounded waits when they expire
@@ -247,7 +255,6 @@ struct Context {
     void ensureMixedBuffers();
     void solveMixed(const gsgpu_solver_opts& o, gsgpu_solve_info& info);
     int lanesPerRow(bool fp64) const;
-    bool rowGroup2() const;
     static Context reset(Context&& c);
 };
 

@@ -109,6 +109,7 @@ int sdiaPartials(const SdiaOp& A);
 // encode the TMA tensor maps of A's diagonals and of the vector x into out2 (two CUtensorMap, 64-byte
 // aligned); false (and the reason in *why) if the driver or the shape does not allow them
 bool sdiaTensorMaps(const SdiaOp& A, const float* x, void* out2, std::string* why);
+// t = A x and the block partials of x.t
 void sdiaSpmv(const SdiaOp& A, const float* x, float* t, double* part, const CgState* st, cudaStream_t s);
 }  // namespace launch
 }  // namespace gsgpu

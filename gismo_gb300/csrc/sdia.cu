@@ -361,6 +361,7 @@ __global__ void __launch_bounds__(kTmaThreads) k_sdia32_tma(const __grid_constan
     }
 }
 
+
 }  // namespace
 
 namespace launch {
@@ -457,3 +458,4 @@ void sdiaSpmv(const SdiaOp& A, const float* x, float* t, double* part, const CgS
 
 }  // namespace launch
 }  // namespace gsgpu
+

@@ -21,11 +21,14 @@ def built():
 
 
 def _solve(prob, box, precision):
+    """Box rows belong to the CSR products: the half-diagonal inner operator of single patches is
+    switched off (GSGPU_NO_SDIA=1) so that the mixed path runs them."""
     from gismo_gb300.assembler import GpuPoissonAssembler
     if box:
         os.environ.pop("GSGPU_NO_BOX_ROWS", None)
     else:
         os.environ["GSGPU_NO_BOX_ROWS"] = "1"
+    os.environ["GSGPU_NO_SDIA"] = "1"
     try:
         A = GpuPoissonAssembler(prob, device=0)
         A.assemble(precision)
@@ -35,6 +38,7 @@ def _solve(prob, box, precision):
         A.close()
     finally:
         os.environ.pop("GSGPU_NO_BOX_ROWS", None)
+        os.environ.pop("GSGPU_NO_SDIA", None)
     return x, info, stats
 
 
