@@ -17,7 +17,7 @@ EXPORTS = [
     "gsgpu_batch_l2_error", "gsgpu_server_create", "gsgpu_server_submit", "gsgpu_server_wait",
     "gsgpu_server_last_error", "gsgpu_server_destroy", "gsgpu_apply", "gsgpu_mg_apply", "gsgpu_set_fixed_dofs",
     "gsgpu_h1_error", "gsgpu_batch_h1_error", "gsgpu_autotune", "gsgpu_tuned_variants", "gsgpu_tune_save",
-    "gsgpu_tune_load", "gsgpu_tune_clear",
+    "gsgpu_tune_load", "gsgpu_tune_clear", "gsgpu_server_set_resident",
 ]
 
 # the tuning table measured on GB300 (written by gsgpu_tune_save after gsgpu_autotune runs on the
@@ -61,7 +61,7 @@ class RequestInfo(C.Structure):
     _fields_ = [("status", C.c_int), ("nfree", C.c_int), ("iterations", C.c_int), ("relres", C.c_double),
                 ("t_submit", C.c_double), ("t_start", C.c_double), ("t_done", C.c_double), ("batch_size", C.c_int),
                 ("batch_id", C.c_longlong), ("est_bytes", C.c_double), ("ms_setup", C.c_double),
-                ("ms_assemble", C.c_double), ("ms_solve", C.c_double)]
+                ("ms_assemble", C.c_double), ("ms_solve", C.c_double), ("resident", C.c_int)]
 
 
 class GsGpuError(RuntimeError):
@@ -107,6 +107,7 @@ def lib() -> C.CDLL:
         L.gsgpu_server_last_error.argtypes = [vp]
         L.gsgpu_server_last_error.restype = C.c_char_p
         L.gsgpu_server_destroy.argtypes = [vp]
+        L.gsgpu_server_set_resident.argtypes = [vp, C.c_double]
         L.gsgpu_apply.argtypes = [vp, vp, vp]
         L.gsgpu_mg_apply.argtypes = [vp, C.POINTER(SolverOpts), vp, vp]
         L.gsgpu_min_jacobian.argtypes = [vp, C.POINTER(C.c_double)]

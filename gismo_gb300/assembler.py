@@ -354,6 +354,14 @@ class GpuPoissonServer:
             raise GsGpuError(rc, self.L.gsgpu_server_last_error(self.h).decode())
         return x[:info.nfree], d
 
+    def set_resident(self, gb: float):
+        """Device memory (GB) that resident batch contexts may hold (gsgpu_server_set_resident)."""
+        self._check_rc(self.L.gsgpu_server_set_resident(self.h, gb * 1e9))
+
+    def _check_rc(self, rc):
+        if rc != _lib.OK:
+            raise GsGpuError(rc, self.L.gsgpu_server_last_error(self.h).decode())
+
     def close(self):
         if getattr(self, "h", None) and self.h.value:
             self.L.gsgpu_server_destroy(self.h)

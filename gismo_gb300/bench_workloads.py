@@ -194,9 +194,17 @@ def _serve(reqs, precision, tol, slots=4, budget_gb=120.0, max_batch=64):
     last = max(r[1]["t_done"] for r in res)
     dofs = sum(r[1]["nfree"] for r in res)
     ok = all(r[1]["status"] == 0 for r in res)
+    batches = {}
+    for r in res:  # per batch: its set-up time and whether it ran on a resident context
+        batches[r[1]["batch_id"]] = (r[1]["ms_setup"], r[1]["resident"])
+    setup = np.array([v[0] for v in batches.values()])
+    resident = np.array([v[1] for v in batches.values()])
     return dict(p50_ms=float(np.percentile(lat, 50)) * 1e3, p99_ms=float(np.percentile(lat, 99)) * 1e3,
                 dofs_per_s=dofs / (last - first), makespan_s=last - first, all_converged=ok,
-                mean_batch=float(np.mean([r[1]["batch_size"] for r in res]))), res
+                mean_batch=float(np.mean([r[1]["batch_size"] for r in res])), batches=len(batches),
+                setup_ms_mean=float(setup.mean()), resident_batches=int(resident.sum()),
+                setup_ms_resident=float(setup[resident == 1].mean()) if resident.any() else None,
+                setup_ms_refresh=float(setup[resident == 0].mean()) if (resident == 0).any() else None), res
 
 
 def run_serving(args, sampler):
@@ -222,6 +230,17 @@ def run_serving(args, sampler):
         per_rate.append({"rate_req_s": rate, "requests": count, "mixed": m, "plain_fp64": f,
                          "max_rel_err_mixed_vs_fp64": worst(res_m), "max_rel_err_fp64_at_tol": worst(res_f),
                          "speedup_mixed_over_fp64": m["dofs_per_s"] / f["dofs_per_s"]})
+    # a stream on fixed meshes (8 recurring discretisations, every request its own geometry and
+    # kappa field): batches of a recurring structure run on resident contexts without refresh()
+    fixed = P.serving_requests(count, rate=rates[1], seed=13, n2d=(16, 256), n3d=(8, 48))
+    shapes = [pr for _, pr in P.serving_requests(8, rate=rates[1], seed=14)]
+    fixed_reqs = []
+    for j, (t, pr) in enumerate(fixed):
+        base = shapes[j % len(shapes)]
+        q = P.displaced_single_patch(base.dim, base.patches[0].nelems_dir, base.patches[0].degree, 1000 + j,
+                                     0.05 if base.dim == 2 else 0.04, check=False)
+        fixed_reqs.append((t, q))
+    fm, _ = _serve(fixed_reqs, "mixed", tol)
     clocks = clk.stop()
     top = per_rate[-1]
     cfg = {"workload": "serving_stream", "requests_per_rate": count, "slots": 4, "budget_gb": 120.0,
@@ -230,7 +249,7 @@ def run_serving(args, sampler):
     line = _line("serving", top["mixed"]["dofs_per_s"], "DoF/s", args, cfg, {
         "p50_ms": top["mixed"]["p50_ms"], "p99_ms": top["mixed"]["p99_ms"],
         "max_rel_err_mixed_vs_fp64": max(r["max_rel_err_mixed_vs_fp64"] for r in per_rate),
-        "rates": per_rate, "clocks": clocks})
+        "rates": per_rate, "fixed_meshes_200_req_s": fm, "clocks": clocks})
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = _cpu_batch([pr for _, pr in P.serving_requests(count, rate=rates[-1], seed=11)])
     print(json.dumps(line), flush=True)

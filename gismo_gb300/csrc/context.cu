@@ -1183,6 +1183,74 @@ int gsgpu::setBatchDescs(gsgpu_context* ctx, std::vector<gsgpu::ProblemDesc>& it
     });
 }
 
+// the structure of a batch (what refresh() derives its plan from): per problem the dimension,
+// quadrature rule, Dirichlet strategy, degrees and knot vectors of both bases, the control-point
+// count and the boundary sides; not the control points or the closed-form field constants
+std::string gsgpu::batchSignature(const std::vector<gsgpu::ProblemDesc>& items) {
+    std::string sig;
+    auto put = [&](const void* p, size_t n) { sig.append(static_cast<const char*>(p), n); };
+    for (const gsgpu::ProblemDesc& pd : items) {
+        put(&pd.dim, sizeof(int));
+        put(&pd.quA, sizeof(double));
+        put(&pd.quB, sizeof(int));
+        put(&pd.dirL2, sizeof(int));
+        for (const gsgpu::HostPatch& P : pd.patches) {
+            for (int k = 0; k < pd.dim; ++k)
+                for (const gsgpu::Basis1D* B : {&P.b[k], &P.g[k]}) {
+                    put(&B->p, sizeof(int));
+                    const size_t nt = B->t.size();
+                    put(&nt, sizeof(nt));
+                    put(B->t.data(), nt * sizeof(double));
+                }
+            const size_t nc = P.coefs.size();
+            put(&nc, sizeof(nc));
+        }
+        for (const std::vector<int>* v : {&pd.dsides, &pd.nsides, &pd.ifaces}) {
+            const size_t n = v->size();
+            put(&n, sizeof(n));
+            put(v->data(), n * sizeof(int));
+        }
+        put("|", 1);
+    }
+    return sig;
+}
+
+// new control points and field constants for a refreshed batch context whose batch has the
+// signature of `items` (the plan, pattern and device buffers stay resident): the next assemble()
+// uses them
+int gsgpu::updateBatchData(gsgpu_context* ctx, std::vector<gsgpu::ProblemDesc>& items) {
+    return guarded(ctx, [&] {
+        gsgpu::Context& c = ctx->c;
+        if (!c.batch || !c.refreshed || c.device < 0) throw gsgpu::StateError("update of a batch that is not resident");
+        if (items.size() != c.pd.patches.size()) throw std::invalid_argument("batch update: problem count differs");
+        std::vector<double> raw;
+        for (size_t j = 0; j < items.size(); ++j) {
+            gsgpu::HostPatch& P = c.pd.patches[j];
+            const gsgpu::HostPatch& Q = items[j].patches.at(0);
+            if (Q.coefs.size() != P.coefs.size()) throw std::invalid_argument("batch update: control points differ");
+            P.coefs = Q.coefs;
+            c.pd.pfields.at(j) = items[j].fields;
+            raw.insert(raw.end(), P.coefs.begin(), P.coefs.end());
+        }
+        std::vector<gsgpu::dev::FieldConst<double>> fc64;
+        std::vector<gsgpu::dev::FieldConst<gsgpu::df32>> fcdf;
+        for (const gsgpu::FieldParams& F : c.pd.fieldTable()) {
+            fc64.push_back(gsgpu::dev::fieldConst<double>(F));
+            fcdf.push_back(gsgpu::dev::fieldConst<gsgpu::df32>(F));
+        }
+        cudaStream_t s = c.stream;
+        GSGPU_CUDA_TRY(cudaMemcpyAsync(c.dFields, fc64.data(), fc64.size() * sizeof(fc64[0]), cudaMemcpyHostToDevice, s));
+        GSGPU_CUDA_TRY(cudaMemcpyAsync(c.dFieldsDf, fcdf.data(), fcdf.size() * sizeof(fcdf[0]), cudaMemcpyHostToDevice, s));
+        GSGPU_CUDA_TRY(cudaMemcpyAsync(c.dCoefRaw, raw.data(), raw.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+        gsgpu::launch::coefsToSoa(c.dPatches, c.tabCoef.d, (long long)c.tabCoef.h.size(), c.dCoefRaw, c.dCoefs, s);
+        GSGPU_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors above go out of scope
+        c.assembled = c.solved = false;
+    });
+}
+
+// device bytes a context holds
+double gsgpu::deviceBytes(const gsgpu_context* ctx) { return ctx ? double(ctx->c.arena.used) : 0.0; }
+
 void gsgpu::releaseDevice(gsgpu_context* ctx) {
     if (!ctx || ctx->c.device < 0) return;
     cudaSetDevice(ctx->c.device);

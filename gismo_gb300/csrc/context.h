@@ -107,6 +107,11 @@ std::vector<int> segmentRows(const ProblemDesc& pd, const DofMap& map);
 int setBatchDescs(gsgpu_context* ctx, std::vector<ProblemDesc>& items);
 // free every device buffer of the context (it keeps its stream and problem)
 void releaseDevice(gsgpu_context* ctx);
+// the structure of a batch of problems (all that refresh() derives the plan from)
+std::string batchSignature(const std::vector<ProblemDesc>& items);
+// new control points and field constants for a resident batch of the same signature (no refresh)
+int updateBatchData(gsgpu_context* ctx, std::vector<ProblemDesc>& items);
+double deviceBytes(const gsgpu_context* ctx);
 
 struct Context {
     int device = -1;

@@ -6,6 +6,13 @@
 // the batch stays within max_batch requests and the estimated device memory of all running batches
 // stays within the budget; it assembles and solves them as one batch (segmented CG). Batches of
 // different slots run concurrently on their own streams.
+//
+// Residency: a slot keeps the contexts of its recent batches (plan, pattern, gather maps and device
+// buffers) in a least-recently-used list keyed by the batch's structure (batchSignature). A batch
+// whose structure is resident skips refresh(): only its control points and field constants are
+// uploaded. Resident contexts count against the budget (admission sees running batches plus
+// resident bytes); when the queue head does not fit, the taking slot evicts its own resident
+// contexts, and if that is not enough every slot is asked to evict its list.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -31,6 +38,7 @@ namespace {
 struct Request {
     long long id = 0;
     ProblemDesc pd;
+    std::string sig;  // batchSignature of the request alone
     double tol = 1e-8;
     double est = 0.0;
     bool done = false;
@@ -58,9 +66,20 @@ double estimateBytes(const ProblemDesc& pd) {
 
 }  // namespace
 
+struct Resident {
+    std::string sig;
+    gsgpu_context* ctx = nullptr;
+    double bytes = 0.0;
+    unsigned long long used = 0;
+};
+
 struct Server {
     int device = 0, maxBatch = 64, precision = GSGPU_PREC_MIXED, nslots = 1;
     double budget = 0.0, reserved = 0.0;
+    double residentCap = 0.0;   // the most device memory resident contexts may hold (0: none kept)
+    double residentBytes = 0.0; // held by resident contexts of all slots
+    unsigned long long evictEpoch = 0;  // bumped to ask every slot to evict its resident contexts
+    unsigned long long useClock = 0;
     std::mutex m;
     std::condition_variable cvWork, cvDone;
     std::deque<Request*> queue;
@@ -85,7 +104,7 @@ struct Server {
             r->done = true;
             cvDone.notify_all();
         }
-        if (queue.empty() || reserved + queue.front()->est > budget) return batch;
+        if (queue.empty() || reserved + residentBytes + queue.front()->est > budget) return batch;
         const Request* head = queue.front();
         const int dim = head->pd.dim;
         const double tol = head->tol, quA = head->pd.quA;
@@ -95,7 +114,7 @@ struct Server {
             Request* r = *it;
             const bool same = r->pd.dim == dim && r->tol == tol && r->pd.quA == quA && r->pd.quB == quB &&
                               r->pd.dirL2 == head->pd.dirL2;
-            if (same && reserved + sum + r->est <= budget) {
+            if (same && reserved + residentBytes + sum + r->est <= budget) {
                 sum += r->est;
                 batch.push_back(r);
                 it = queue.erase(it);
@@ -108,10 +127,11 @@ struct Server {
     }
 
     void work();
-    void run(gsgpu_context* ctx, std::vector<Request*>& batch);
+    // run the batch on ctx; resident: ctx already holds a refreshed batch of the same structure
+    void run(gsgpu_context* ctx, std::vector<Request*>& batch, bool resident);
 };
 
-void Server::run(gsgpu_context* ctx, std::vector<Request*>& batch) {
+void Server::run(gsgpu_context* ctx, std::vector<Request*>& batch, bool resident) {
     const size_t nb = batch.size();
     std::vector<ProblemDesc> items;
     items.reserve(nb);
@@ -121,8 +141,13 @@ void Server::run(gsgpu_context* ctx, std::vector<Request*>& batch) {
         return std::chrono::duration<double, std::milli>(b - a).count();
     };
     const auto t0 = clock();
-    int rc = setBatchDescs(ctx, items);
-    if (rc == GSGPU_OK) rc = gsgpu_refresh(ctx);
+    int rc = GSGPU_OK;
+    if (resident) {
+        rc = updateBatchData(ctx, items);
+    } else {
+        rc = setBatchDescs(ctx, items);
+        if (rc == GSGPU_OK) rc = gsgpu_refresh(ctx);
+    }
     const auto t1 = clock();
     if (rc == GSGPU_OK) rc = gsgpu_assemble(ctx, precision);
     const auto t2 = clock();
@@ -150,6 +175,7 @@ void Server::run(gsgpu_context* ctx, std::vector<Request*>& batch) {
     for (size_t j = 0; j < nb; ++j) {
         Request* r = batch[j];
         r->info.batch_size = int(nb);
+        r->info.resident = resident ? 1 : 0;
         r->info.ms_setup = ms(t0, t1);
         r->info.ms_assemble = ms(t1, t2);
         r->info.ms_solve = ms(t2, t3);
@@ -165,7 +191,6 @@ void Server::run(gsgpu_context* ctx, std::vector<Request*>& batch) {
         r->info.status = rr[j] < r->tol ? GSGPU_OK : GSGPU_ERR_NOT_CONVERGED;
         if (r->info.status != GSGPU_OK) r->err = "maximum number of iterations reached";
     }
-    releaseDevice(ctx);  // an idle slot holds no device memory: the budget counts running batches
 }
 
 void Server::work() {
@@ -173,15 +198,43 @@ void Server::work() {
     // the slots' host set-up runs concurrently: each gets an equal share of the host threads
     omp_set_num_threads(std::max(1, omp_get_num_procs() / std::max(1, nslots)));
 #endif
-    gsgpu_context* ctx = nullptr;
-    const int crc = gsgpu_create(&ctx, device);
+    std::vector<Resident> mine;  // this slot's resident contexts (least recently used first)
+    std::vector<gsgpu_context*> spare;  // contexts without device memory, ready for a new batch
+    unsigned long long seenEpoch = 0;
+    auto evict = [&](size_t k, std::unique_lock<std::mutex>& lk) {  // lock held on entry and exit
+        Resident r = mine[k];
+        mine.erase(mine.begin() + long(k));
+        residentBytes -= r.bytes;
+        lk.unlock();
+        releaseDevice(r.ctx);
+        spare.push_back(r.ctx);
+        lk.lock();
+    };
     for (;;) {
         std::vector<Request*> batch;
+        gsgpu_context* ctx = nullptr;
+        bool resident = false;
         {
             std::unique_lock<std::mutex> lk(m);
             for (;;) {
+                if (evictEpoch != seenEpoch) {  // another slot needs the memory of resident contexts
+                    seenEpoch = evictEpoch;
+                    while (!mine.empty()) evict(0, lk);
+                    cvWork.notify_all();
+                }
                 batch = takeBatch();
                 if (!batch.empty() || (stop && queue.empty())) break;
+                // the head does not fit: free this slot's resident contexts first, then ask the others
+                if (!queue.empty() && reserved + queue.front()->est <= budget &&
+                    reserved + residentBytes + queue.front()->est > budget && residentBytes > 0.0) {
+                    if (!mine.empty()) {
+                        while (!mine.empty()) evict(0, lk);
+                        continue;
+                    }
+                    ++evictEpoch;
+                    seenEpoch = evictEpoch;
+                    cvWork.notify_all();
+                }
                 cvWork.wait(lk);
             }
             if (batch.empty()) break;
@@ -191,14 +244,61 @@ void Server::work() {
                 r->info.t_start = t;
                 r->info.batch_id = bid;
             }
+            // a resident context of the same structure takes the batch (its bytes move from the
+            // resident count to the batch's reservation)
+            std::string sig;
+            for (Request* r : batch) sig += r->sig;
+            for (size_t k = 0; k < mine.size(); ++k)
+                if (mine[k].sig == sig) {
+                    ctx = mine[k].ctx;
+                    residentBytes -= mine[k].bytes;
+                    mine.erase(mine.begin() + long(k));
+                    resident = true;
+                    break;
+                }
+            if (!ctx && !spare.empty()) {
+                ctx = spare.back();
+                spare.pop_back();
+            }
+            if (!ctx && int(mine.size()) >= 4) {
+                // at most four resident contexts per slot before a new handle is made: the least
+                // recently used one gives up its memory and its handle takes the batch
+                Resident r = mine.front();
+                mine.erase(mine.begin());
+                residentBytes -= r.bytes;
+                lk.unlock();
+                releaseDevice(r.ctx);
+                lk.lock();
+                ctx = r.ctx;
+            }
         }
+        int crc = GSGPU_OK;
+        if (!ctx) crc = gsgpu_create(&ctx, device);
         if (crc != GSGPU_OK) {
             for (Request* r : batch) {
                 r->info.status = crc;
                 r->err = "could not create a CUDA context for the server slot";
             }
+            ctx = nullptr;
         } else {
-            run(ctx, batch);
+            std::string sig;
+            for (Request* r : batch) sig += r->sig;
+            run(ctx, batch, resident);
+            // keep the context resident when its memory fits the resident cap, else release it
+            const double bytes = deviceBytes(ctx);
+            std::unique_lock<std::mutex> lk(m);
+            bool keep = residentCap > 0.0 && bytes <= residentCap && batch[0]->info.status == GSGPU_OK;
+            while (keep && residentBytes + bytes > residentCap && !mine.empty()) evict(0, lk);
+            keep = keep && residentBytes + bytes <= residentCap;
+            if (keep) {
+                mine.push_back(Resident{sig, ctx, bytes, ++useClock});
+                residentBytes += bytes;
+                ctx = nullptr;
+            }
+        }
+        if (ctx) {
+            releaseDevice(ctx);  // not kept: an idle slot holds no device memory for it
+            spare.push_back(ctx);
         }
         {
             std::lock_guard<std::mutex> lk(m);
@@ -214,7 +314,11 @@ void Server::work() {
         cvDone.notify_all();
         cvWork.notify_all();
     }
-    if (ctx) gsgpu_destroy(ctx);
+    {
+        std::unique_lock<std::mutex> lk(m);
+        while (!mine.empty()) evict(0, lk);
+    }
+    for (gsgpu_context* c : spare) gsgpu_destroy(c);
 }
 
 }  // namespace gsgpu
@@ -235,6 +339,7 @@ int gsgpu_server_create(gsgpu_server** out, int device, int slots, double budget
     p->s.maxBatch = max_batch;
     p->s.precision = precision;
     p->s.nslots = slots;
+    p->s.residentCap = 0.25 * budget_bytes;  // default: a quarter of the budget for resident batches
     for (int i = 0; i < slots; ++i) p->s.workers.emplace_back([p] { p->s.work(); });
     *out = p;
     return GSGPU_OK;
@@ -249,6 +354,7 @@ int gsgpu_server_submit(gsgpu_server* srv, const gsgpu_problem* prob, double tol
         if (r->pd.patches.size() != 1 || !r->pd.ifaces.empty())
             throw std::invalid_argument("server requests must be single patches without interfaces");
         r->est = gsgpu::estimateBytes(r->pd);
+        r->sig = gsgpu::batchSignature(std::vector<gsgpu::ProblemDesc>(1, r->pd));
     } catch (const std::exception& e) {
         std::lock_guard<std::mutex> lk(S.m);
         S.lastError = e.what();
@@ -290,6 +396,16 @@ int gsgpu_server_wait(gsgpu_server* srv, long long id, double* x, int capacity, 
     if (status != GSGPU_OK) S.lastError = r->err;
     S.reqs.erase(it);
     return status;
+}
+
+int gsgpu_server_set_resident(gsgpu_server* srv, double bytes) {
+    if (!srv || bytes < 0.0) return GSGPU_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(srv->s.m);
+    if (bytes > srv->s.budget) return GSGPU_ERR_INVALID;
+    srv->s.residentCap = bytes;
+    if (srv->s.residentBytes > bytes) ++srv->s.evictEpoch;  // slots give up their lists
+    srv->s.cvWork.notify_all();
+    return GSGPU_OK;
 }
 
 const char* gsgpu_server_last_error(const gsgpu_server* srv) { return srv ? srv->s.lastError.c_str() : "null server"; }

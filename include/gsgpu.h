@@ -209,6 +209,7 @@ typedef struct {
     long long batch_id;
     double est_bytes; /* device-memory estimate the admission used */
     double ms_setup, ms_assemble, ms_solve;  /* wall time of the batch's refresh, assemble and solve */
+    int resident;     /* 1: the batch ran on a resident context of the same structure (no refresh) */
 } gsgpu_request_info;
 int gsgpu_server_create(gsgpu_server** srv, int device, int slots, double budget_bytes, int max_batch,
                         int precision);
@@ -218,6 +219,15 @@ int gsgpu_server_submit(gsgpu_server* srv, const gsgpu_problem* prob, double tol
  * request is forgotten afterwards. Returns the request's status (GSGPU_ERR_INVALID for an unknown
  * id or a too small x). */
 int gsgpu_server_wait(gsgpu_server* srv, long long id, double* x, int capacity, gsgpu_request_info* info);
+/* Residency: each slot keeps the contexts of its recent batches (plan, sparsity pattern, gather
+ * maps, device buffers) in a least-recently-used list keyed by the batch's structure (per problem:
+ * dimension, quadrature rule, Dirichlet strategy, degrees and knots, control-point count, boundary
+ * sides). A later batch of the same structure reuses one without refresh(): only its control points
+ * and field constants are uploaded (gsgpu_request_info.resident = 1, ms_setup the upload time).
+ * Resident contexts hold at most `bytes` of device memory in total (default: a quarter of the
+ * budget; 0 keeps none) and count against the budget: when a queued request does not fit beside
+ * them, resident contexts are released first. */
+int gsgpu_server_set_resident(gsgpu_server* srv, double bytes);
 /* message of the last failed request taken by gsgpu_server_wait */
 const char* gsgpu_server_last_error(const gsgpu_server* srv);
 /* finishes the queued requests, then stops the workers and frees everything */
