@@ -1458,6 +1458,25 @@ int gsgpu_spmv_stats(gsgpu_context* ctx, long long* launches, double* total_ms, 
     });
 }
 
+int gsgpu_eval_fields(const gsgpu_problem* prob, int npts, const double* x, double* kappa, double* f, double* u) {
+    if (!prob || npts < 0 || (npts > 0 && !x)) return GSGPU_ERR_INVALID;
+    try {
+        gsgpu::ProblemDesc pd;
+        gsgpu::problemFromC(prob, pd);
+        const int d = pd.dim;
+        for (int i = 0; i < npts; ++i) {
+            double k = 0, ff = 0, uu = 0;
+            gsgpu::evalFields(pd.fields, x + size_t(i) * d, k, ff, uu);
+            if (kappa) kappa[i] = k;
+            if (f) f[i] = ff;
+            if (u) u[i] = uu;
+        }
+    } catch (...) {
+        return GSGPU_ERR_INVALID;
+    }
+    return GSGPU_OK;
+}
+
 int gsgpu_autotune(gsgpu_context* ctx, double* ms8) {
     return guarded(ctx, [&] { ctx->c.autotune(ms8); });
 }

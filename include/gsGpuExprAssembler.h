@@ -199,21 +199,26 @@ private:
         int n = 0, nb = 0, nl = 0;
         long long nnz = 0;
         check(gsgpu_sizes(m_ctx, &n, &nnz, &nb, &nl));
-        std::vector<int> ptr(n + 1), col(nnz);
-        std::vector<double> val(nnz);
-        check(gsgpu_matrix_csr(m_ctx, ptr.data(), col.data(), val.data()));
-        // symmetric: the CSR arrays are the compressed ColMajor arrays
+        // symmetric: the CSR arrays are the compressed ColMajor arrays, copied straight into the
+        // matrix's storage (no per-entry insertion)
         m_matrix.resize(n, n);
-        gsVector<index_t> per(n);
-        for (int c = 0; c < n; ++c) per[c] = ptr[c + 1] - ptr[c];
-        m_matrix.reserve(per);
-        for (int c = 0; c < n; ++c)
-            for (int k = ptr[c]; k < ptr[c + 1]; ++k) m_matrix.insert(col[k], c) = val[k];
-        m_matrix.makeCompressed();
+        m_matrix.resizeNonZeros(index_t(nnz));
+        fillCompressed(m_matrix.outerIndexPtr(), m_matrix.innerIndexPtr(), m_matrix.valuePtr(), n, nnz);
         std::vector<double> b(n);
         check(gsgpu_rhs(m_ctx, b.data()));
         m_rhs.resize(n, 1);
         for (int i = 0; i < n; ++i) m_rhs(i, 0) = b[i];
+    }
+    void fillCompressed(int* outer, int* inner, double* values, int, long long) {
+        check(gsgpu_matrix_csr(m_ctx, outer, inner, values));
+    }
+    template <class I, class U>
+    void fillCompressed(I* outer, I* inner, U* values, int n, long long nnz) {
+        std::vector<int> p(static_cast<size_t>(n) + 1), c(static_cast<size_t>(nnz));
+        std::vector<double> v(static_cast<size_t>(nnz));
+        check(gsgpu_matrix_csr(m_ctx, p.data(), c.data(), v.data()));
+        for (size_t i = 0; i < p.size(); ++i) outer[i] = I(p[i]);
+        for (size_t i = 0; i < c.size(); ++i) inner[i] = I(c[i]), values[i] = U(v[i]);
     }
 
     gsgpu_context* m_ctx = nullptr;

@@ -6,12 +6,22 @@
  *  (gsMultiPatch, gsMultiBasis, gsBoundaryConditions, rhs), call assemble(), then matrix(),
  *  rhs(), fixedDofs(), numDofs(), constructSolution() as usual. refresh() builds the dof map and
  *  the sparsity pattern on the host and uploads the patch data; assemble() runs the device
- *  kernels and fills m_system (an Eigen compressed ColMajor matrix with int indices, as G+Smo's).
+ *  kernels and brings back the rhs and the eliminated-dof values; matrix() materialises the
+ *  system matrix on first access after an assemble(), straight into the compressed ColMajor
+ *  storage of m_system (one copy of the device CSR arrays, no per-entry insertion). Call matrix(),
+ *  rhs() and fixedDofs() on the gsGpuPoissonAssembler itself: they hide the base class's
+ *  (non-virtual) accessors; through a gsPoissonAssembler reference call matrix() on the derived
+ *  object once first.
  *
  *  Functions: the device evaluates closed forms, so the coefficient, the source and the
  *  Dirichlet data are passed as gsGpuFields parameters (kappa = exp(alpha g) with a Fourier
- *  field g, or a constant; f = -div(kappa grad u) for u = prod sin(freq pi x_i)); the gsFunction
- *  given to the constructor is kept for G+Smo-side post-processing (e.g. distanceL2).
+ *  field g, or a constant; f = -div(kappa grad u) for u = prod sin(freq pi x_i)). refresh()
+ *  checks the caller's own functions against them: the rhs function given to the constructor
+ *  at points of every patch, each Dirichlet side's function (u) and each Neumann side's function
+ *  (the flux kappa grad u . n of the closed forms on the box side) at points of the side; a
+ *  mismatch beyond 1e-8 relative throws std::invalid_argument instead of silently computing
+ *  another problem. The coefficient has no caller-side function in gsPoissonAssembler's
+ *  constructor and comes from gsGpuFields alone.
  *  Supported inputs: gsTensorBSpline patches of dimension 2 or 3, tensor B-spline bases,
  *  conforming interfaces with identity orientation (iFace::glue), Dirichlet sides eliminated
  *  with values by interpolation or L2 projection ("DirichletValues"), Neumann sides with the
@@ -30,6 +40,7 @@
 #include <vector>
 
 #include "gsgpu.h"
+#include "gsgpu.hpp"
 
 namespace gismo {
 
@@ -131,45 +142,37 @@ public:
     gsGpuPoissonAssembler(const gsMultiPatch<T>& patches, const gsMultiBasis<T>& basis,
                           const gsBoundaryConditions<T>& bconditions, const gsFunction<T>& rhs,
                           const gsGpuFields& fields, int device = 0)
-        : Base(patches, basis, bconditions, rhs, dirichlet::elimination, iFace::glue), m_fields(fields) {
-        check(gsgpu_create(&m_ctx, device));
+        : Base(patches, basis, bconditions, rhs, dirichlet::elimination, iFace::glue), m_sys(device), m_fields(fields) {
         upload();
-    }
-
-    ~gsGpuPoissonAssembler() {
-        if (m_ctx) gsgpu_destroy(m_ctx);
     }
 
     /// gsAssembler::refresh(): dof map, sparsity pattern and device buffers
     void refresh() override {
         Base::refresh();
-        if (m_ctx) upload();
+        if (m_ready) upload();
     }
 
-    /// gsPoissonAssembler::assemble() on the device
+    /// gsPoissonAssembler::assemble() on the device: the rhs and the eliminated-dof values come back
+    /// at once, the matrix on first access (matrix())
     void assemble() override {
-        check(gsgpu_assemble(m_ctx, GSGPU_PREC_FP64));
-        int n = 0, nb = 0, nl = 0;
-        long long nnz = 0;
-        check(gsgpu_sizes(m_ctx, &n, &nnz, &nb, &nl));
-        std::vector<int> ptr(n + 1), col(nnz);
-        std::vector<double> val(nnz);
-        check(gsgpu_matrix_csr(m_ctx, ptr.data(), col.data(), val.data()));
-        // the system is symmetric: the CSR arrays are the compressed ColMajor arrays
-        gsSparseMatrix<T>& K = this->m_system.matrix();
-        K.resize(n, n);
-        K.reserve(gsVector<index_t>::Map(std::vector<index_t>(ptr.begin() + 1, ptr.end()).data(), n) -
-                  gsVector<index_t>::Map(std::vector<index_t>(ptr.begin(), ptr.end() - 1).data(), n));
-        for (int c = 0; c < n; ++c)
-            for (int k = ptr[c]; k < ptr[c + 1]; ++k) K.insert(col[k], c) = val[k];
-        K.makeCompressed();
+        m_sys.assemble(GSGPU_PREC_FP64);
+        const gsgpu::Sizes sz = m_sys.sizes();
         gsMatrix<T>& b = this->m_system.rhs();
-        b.resize(n, 1);
-        check(gsgpu_rhs(m_ctx, b.data()));
+        b.resize(sz.nfree, 1);
+        readInto(b.data(), sz.nfree, [&](double* p) { m_sys.rhs(p); });
         this->m_ddof.resize(1);
-        this->m_ddof[0].resize(nb, 1);
-        if (nb) check(gsgpu_fixed_dofs(m_ctx, this->m_ddof[0].data()));
+        this->m_ddof[0].resize(sz.nfixed, 1);
+        if (sz.nfixed) readInto(this->m_ddof[0].data(), sz.nfixed, [&](double* p) { m_sys.fixedDofs(p); });
+        m_matrixStale = true;
     }
+
+    /// gsAssembler::matrix(), materialised from the device on the first access after assemble()
+    const gsSparseMatrix<T>& matrix() const {
+        if (m_matrixStale) const_cast<gsGpuPoissonAssembler*>(this)->materializeMatrix();
+        return Base::matrix();
+    }
+    const gsMatrix<T>& rhs() const { return Base::rhs(); }
+    const gsMatrix<T>& fixedDofs(short_t unk = 0) const { return Base::fixedDofs(unk); }
 
     /// CG (+ Jacobi) on the device-resident system (gsConjugateGradient(matrix(), gsJacobiOp))
     int solve(gsMatrix<T>& x, double tol = 1e-10, int maxIter = 1000) {
@@ -197,9 +200,12 @@ public:
         o.mg_cycles = opt.askInt("NumCycles", 1);
         o.mg_cgc_damping = opt.askReal("CoarseGridCorrectionDamping", 1.0);
         o.inner_tol = 1e-4;
-        if (o.precision == GSGPU_PREC_MIXED) check(gsgpu_assemble(m_ctx, GSGPU_PREC_MIXED));
+        if (o.precision == GSGPU_PREC_MIXED) {
+            if (m_matrixStale) materializeMatrix();  // matrix() keeps the FP64 system
+            m_sys.assemble(GSGPU_PREC_MIXED);
+        }
         const int its = run(o, x);
-        if (o.precision == GSGPU_PREC_MIXED) check(gsgpu_assemble(m_ctx, GSGPU_PREC_FP64));
+        if (o.precision == GSGPU_PREC_MIXED) m_sys.assemble(GSGPU_PREC_FP64);
         return its;
     }
 
@@ -207,34 +213,123 @@ public:
     double error() const { return m_error; }
 
     /// gsField::distanceL2 of the last device solution against the manufactured solution
-    double distanceL2() const {
-        double e = 0.0;
-        check(gsgpu_l2_error(m_ctx, &e));
-        return e;
-    }
+    double distanceL2() const { return m_sys.l2Error(); }
 
     /// gsField::distanceH1 (H1 seminorm of the error) of the last device solution
-    double distanceH1() const {
-        double e = 0.0;
-        check(gsgpu_h1_error(m_ctx, &e));
-        return e;
-    }
+    double distanceH1() const { return m_sys.h1Error(); }
 
-    gsgpu_context* context() const { return m_ctx; }
+    gsgpu_context* context() const { return m_sys.context(); }
 
 private:
     int run(const gsgpu_solver_opts& o, gsMatrix<T>& x) {
         gsgpu_solve_info info;
         x.resize(this->numDofs(), 1);
-        const int rc = gsgpu_solve(m_ctx, &o, x.data(), &info);
-        if (rc != GSGPU_OK && rc != GSGPU_ERR_NOT_CONVERGED) check(rc);
+        readInto(x.data(), int(x.rows()), [&](double* p) { m_sys.solve(o, p, &info); });
         m_error = info.relres;
         return info.iterations;
     }
 
-    void check(int rc) const {
-        if (rc != GSGPU_OK)
-            throw std::runtime_error(std::string("gsgpu: ") + (m_ctx ? gsgpu_last_error(m_ctx) : "no context"));
+    // a device read into T storage (directly when T is double)
+    template <class F>
+    static void readInto(double* out, int, F&& read) { read(out); }
+    template <class U, class F>
+    static void readInto(U* out, int n, F&& read) {
+        std::vector<double> tmp(size_t(n > 0 ? n : 0));
+        read(tmp.data());
+        for (int i = 0; i < n; ++i) out[i] = U(tmp[size_t(i)]);
+    }
+
+    // the compressed ColMajor storage of m_system's matrix filled with one copy of the device CSR
+    // arrays (the system is symmetric: the CSR row arrays are the column arrays)
+    void materializeMatrix() {
+        const gsgpu::Sizes sz = m_sys.sizes();
+        gsSparseMatrix<T>& K = this->m_system.matrix();
+        K.resize(sz.nfree, sz.nfree);
+        K.resizeNonZeros(index_t(sz.nnz));
+        fillCompressed(K.outerIndexPtr(), K.innerIndexPtr(), K.valuePtr(), sz);
+        m_matrixStale = false;
+    }
+    void fillCompressed(int* outer, int* inner, double* values, const gsgpu::Sizes&) { m_sys.csrInto(outer, inner, values); }
+    template <class I, class U>
+    void fillCompressed(I* outer, I* inner, U* values, const gsgpu::Sizes& sz) {
+        std::vector<int> p(static_cast<size_t>(sz.nfree) + 1), c(static_cast<size_t>(sz.nnz));
+        std::vector<double> v(static_cast<size_t>(sz.nnz));
+        m_sys.csr(p.data(), c.data(), v.data());
+        for (size_t i = 0; i < p.size(); ++i) outer[i] = I(p[i]);
+        for (size_t i = 0; i < c.size(); ++i) inner[i] = I(c[i]), values[i] = U(v[i]);
+    }
+
+    // the caller's functions against the device closed forms, at points of every patch (rhs) and of
+    // every Dirichlet / Neumann side (u / the flux kappa grad u . n)
+    void checkFunctions(const std::vector<int>& dsides, const std::vector<int>& nsides) const {
+        const gsMultiPatch<T>& mp = this->patches();
+        const short_t d = mp.parDim();
+        const T tcs[3] = {T(0.17), T(0.5), T(0.83)};
+        auto params = [&](int fixdir, T fixval) {  // 3^(d-1) or 3^d parametric points
+            std::vector<gsVector<T> > pts;
+            const int m = fixdir < 0 ? d : d - 1;
+            int count = 1;
+            for (int i = 0; i < m; ++i) count *= 3;
+            for (int c = 0; c < count; ++c) {
+                gsVector<T> u(d);
+                int r = c;
+                for (int i = 0, j = 0; i < d; ++i) {
+                    if (i == fixdir) { u[i] = fixval; continue; }
+                    u[i] = tcs[r % 3];
+                    r /= 3;
+                    ++j;
+                }
+                pts.push_back(u);
+            }
+            return pts;
+        };
+        auto compare = [&](const gsFunctionSet<T>& fn, bool parametric, index_t patch, int fixdir, T fixval, int what,
+                           int side) {
+            const gsGeometry<T>& G = mp.patch(patch);
+            const std::vector<gsVector<T> > us = params(fixdir, fixval);
+            gsMatrix<T> u(d, index_t(us.size()));
+            for (size_t i = 0; i < us.size(); ++i) u.col(index_t(i)) = us[i];
+            gsMatrix<T> x, got;
+            G.eval_into(u, x);
+            fn.eval_into(parametric ? u : x, got);  // a parametric condition takes the parameters
+            const int n = int(x.cols());
+            std::vector<double> xs(static_cast<size_t>(n) * d), kap(static_cast<size_t>(n)), ff(static_cast<size_t>(n)),
+                uu(static_cast<size_t>(n));
+            for (int i = 0; i < n; ++i)
+                for (int k = 0; k < d; ++k) xs[size_t(i) * d + k] = double(x(k, i));
+            gsgpu::evalFields(m_pack.prob, n, xs.data(), kap.data(), ff.data(), uu.data());
+            for (int i = 0; i < n; ++i) {
+                double want = what == 0 ? ff[size_t(i)] : uu[size_t(i)];
+                if (what == 2) {  // flux sgn kappa du/dx_k on side s of direction k = (s-1)/2
+                    const int k = (side - 1) / 2;
+                    const double w = m_fields.ufreq * 3.14159265358979323846;
+                    double g = w * std::cos(w * xs[size_t(i) * d + k]);
+                    for (int j = 0; j < d; ++j)
+                        if (j != k) g *= std::sin(w * xs[size_t(i) * d + j]);
+                    want = ((side - 1) % 2 ? 1.0 : -1.0) * kap[size_t(i)] * g;
+                }
+                const double have = double(got(0, i));
+                if (std::abs(have - want) > 1e-8 * std::max(1.0, std::abs(want)))
+                    throw std::invalid_argument(
+                        std::string("gsGpuPoissonAssembler: the caller's ") +
+                        (what == 0 ? "rhs function" : what == 1 ? "Dirichlet function" : "Neumann function") +
+                        " differs from the device's closed form (gsGpuFields) on patch " + std::to_string(patch) +
+                        ": " + std::to_string(have) + " vs " + std::to_string(want));
+            }
+        };
+        if (const gsFunctionSet<T>* f = static_cast<const gsPoissonPde<T>&>(this->pde()).rhs())
+            for (index_t k = 0; k < index_t(mp.nPatches()); ++k) compare(*f, false, k, -1, T(0), 0, 0);
+        const gsBoundaryConditions<T>& bc = this->pde().bc();
+        for (typename gsBoundaryConditions<T>::const_iterator it = bc.dirichletBegin(); it != bc.dirichletEnd(); ++it)
+            if (it->function())
+                compare(*it->function(), it->parametric(), it->patch(), it->side().direction(), T(it->side().parameter()),
+                        1, it->side().index());
+        for (typename gsBoundaryConditions<T>::const_iterator it = bc.neumannBegin(); it != bc.neumannEnd(); ++it)
+            if (it->function())
+                compare(*it->function(), it->parametric(), it->patch(), it->side().direction(), T(it->side().parameter()),
+                        2, it->side().index());
+        (void)dsides;
+        (void)nsides;
     }
 
     void upload() {
@@ -258,14 +353,19 @@ private:
         m_pack.pack(this->patches(), this->m_bases[0], dsides, m_fields, this->m_options.getReal("quA"),
                     this->m_options.getInt("quB"),
                     dv == dirichlet::l2Projection ? GSGPU_DIRICHLET_L2 : GSGPU_DIRICHLET_INTERPOLATION, nsides);
-        check(gsgpu_set_problem(m_ctx, &m_pack.prob));
-        check(gsgpu_refresh(m_ctx));
+        checkFunctions(dsides, nsides);
+        m_sys.setProblem(m_pack.prob);
+        m_sys.refresh();
+        m_ready = true;
+        m_matrixStale = false;
     }
 
-    gsgpu_context* m_ctx = nullptr;
+    gsgpu::System m_sys;
     double m_error = 0.0;
     gsGpuFields m_fields;
     gsGpuProblemPack<T> m_pack;
+    bool m_ready = false;
+    bool m_matrixStale = false;
 };
 
 /// The assembled device matrix as a gsLinearOperator (gsMatrixOp semantics: x = K input, column

@@ -233,6 +233,12 @@ const char* gsgpu_server_last_error(const gsgpu_server* srv);
 /* finishes the queued requests, then stops the workers and frees everything */
 int gsgpu_server_destroy(gsgpu_server* srv);
 
+/* The closed-form fields of the problem's description (kappa, f = -div(kappa grad u) and u; the
+ * formulas in the gsgpu_problem comment) at npts physical points x (npts x dim, row-major), as the
+ * device evaluates them. No counterpart in the reference, where these are the caller's gsFunction
+ * objects: the C++ drop-in compares the caller's functions with these values. Outputs may be NULL. */
+int gsgpu_eval_fields(const gsgpu_problem* prob, int npts, const double* x, double* kappa, double* f, double* u);
+
 /* Utilities with no counterpart in the reference. */
 /* the CUDA stream (cudaStream_t) all device work of the context is issued on */
 int gsgpu_stream(gsgpu_context* ctx, void** stream);

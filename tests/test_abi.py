@@ -187,3 +187,20 @@ def test_host_plan_sizes_match_large_reference_runs(lib, name):
     assert lib.gsgpu_sizes(h, C.byref(nf), C.byref(nnz), C.byref(nb), C.byref(nl)) == _lib.OK
     assert (nf.value, nnz.value) == (int(g["free"]), int(g["nnz"]))
     lib.gsgpu_destroy(h)
+
+
+def test_dropin_checks_caller_functions(lib):
+    """The C++ drop-in compares the caller's rhs, Dirichlet and Neumann functions with the closed
+    forms the device evaluates and throws on a mismatch (oracle/ref/dropin_check.cpp, host-only
+    contexts, no GPU). Needs the G+Smo source tree; skipped where it is absent."""
+    import shutil
+    import subprocess
+    mk = os.path.join(ROOT, "oracle", "ref")
+    if shutil.which("make") is None or shutil.which("g++") is None:
+        pytest.skip("no make / g++")
+    ref = subprocess.run(["make", "-s", "-C", mk, "print-ref"], capture_output=True, text=True).stdout.strip()
+    if not ref or not os.path.isdir(os.path.join(ref, "src", "gsAssembler")):
+        pytest.skip("G+Smo source tree not available")
+    r = subprocess.run(["make", "-s", "-C", mk, "dropincheck"], capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, (r.stdout[-2000:], r.stderr[-3000:])
+    assert r.stdout.strip().endswith("ok")
