@@ -17,7 +17,7 @@ EXPORTS = [
     "gsgpu_batch_l2_error", "gsgpu_server_create", "gsgpu_server_submit", "gsgpu_server_wait",
     "gsgpu_server_last_error", "gsgpu_server_destroy", "gsgpu_apply", "gsgpu_mg_apply", "gsgpu_set_fixed_dofs",
     "gsgpu_h1_error", "gsgpu_batch_h1_error", "gsgpu_autotune", "gsgpu_tuned_variants", "gsgpu_tune_save",
-    "gsgpu_tune_load", "gsgpu_tune_clear", "gsgpu_server_set_resident", "gsgpu_eval_fields",
+    "gsgpu_tune_load", "gsgpu_tune_clear", "gsgpu_server_set_resident", "gsgpu_eval_fields", "gsgpu_mass_csr",
 ]
 
 # the tuning table measured on GB300 (written by gsgpu_tune_save after gsgpu_autotune runs on the
@@ -123,6 +123,7 @@ def lib() -> C.CDLL:
         L.gsgpu_tune_load.argtypes = [C.c_char_p]
         L.gsgpu_tune_clear.argtypes = []
         L.gsgpu_eval_fields.argtypes = [C.POINTER(Problem), C.c_int, vp, vp, vp, vp]
+        L.gsgpu_mass_csr.argtypes = [vp, vp]
         for name in EXPORTS:
             if name != "gsgpu_last_error":
                 getattr(L, name).restype = C.c_int

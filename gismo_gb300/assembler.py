@@ -134,6 +134,13 @@ class GpuPoissonAssembler:
         n = len(ptr) - 1
         return sp.csr_matrix((val, col, ptr), shape=(n, n))
 
+    def mass_csr(self) -> np.ndarray:
+        """gsGenericAssembler::assembleMass on the device: the mass matrix's values in the CSR
+        pattern of csr() (gsgpu_mass_csr); the next solve or matrix read needs a new assemble()."""
+        val = np.empty(self.sizes()[1], np.float64)
+        self._check(self.L.gsgpu_mass_csr(self.h, val.ctypes.data))
+        return val
+
     def diagonal(self) -> np.ndarray:
         """matrix().diagonal() (gsSparseMatrix::diagonal), from the downloaded CSR arrays."""
         ptr, col, val = self.csr()

@@ -630,6 +630,38 @@ void Context::assemble(int precision) {
     if (!(detMin > 0.0)) throw JacobianError("geometry map has det J <= 0 at a quadrature point");
 }
 
+// gsGenericAssembler::assembleMass (gsGenericAssembler.h:103): M_ij = int phi_i phi_j |det J| on
+// the free dofs, in FP64, by the stiffness path's kernels with one field (w |det J|) and the
+// value-value pair factors: basis tables, geometry stages, the field, three (two) sum-factorised
+// contractions into the band and the gather over the same slot -> band map into the CSR pattern
+// of matrix(). It reuses the assembly's intermediate buffers (the stiffness CSR values, rhs and
+// solver state are untouched); the next assemble() recomputes them.
+void Context::assembleMass() {
+    if (!refreshed) throw StateError("mass() before refresh()");
+    if (device < 0) throw StateError("mass() needs a CUDA device (host-only context)");
+    cudaStream_t s = stream;
+    if (!dMass) allocN(arena, dMass, nnz);
+    launch::basisTables(dTabJobs, (long long)L.tabjobs.size(), dKnots, dTab, s);
+    launch::basisTables(dGtabJobs, (long long)L.gtabjobs.size(), dGknots, dGtab, s);
+    launch::pairFactors<double>(dPfJobs, tabPf.d, (long long)tabPf.h.size(), dTab, dPf, s);
+    launch::geoStage1<double>(dPatches, tabGeo1.d, (long long)tabGeo1.h.size(), dCoefs, dGtab, dIbuf, dY1, s);
+    if (pd.dim == 3) launch::geoStage2<double>(dPatches, tabGeo2.d, (long long)tabGeo2.h.size(), dY1, dGtab, dIbuf, dY2, s);
+    launch::massField(dPatches, tabPoint.d, (long long)tabPoint.h.size(), dY1, dY2, dGtab, dIbuf, dWq, dFieldL, s);
+    if (pd.dim == 3) {
+        launch::contract<double, 41>(dPatches, tabSt[0].d, (long long)tabSt[0].h.size(), dFieldL, dS, dIbuf, dPf, s);
+        launch::contract<double, 42>(dPatches, tabSt[1].d, (long long)tabSt[1].h.size(), dS, dU, dIbuf, dPf, s);
+        launch::contract<double, 43>(dPatches, tabSt[2].d, (long long)tabSt[2].h.size(), dU, dBand, dIbuf, dPf, s);
+    } else {
+        launch::contract<double, 51>(dPatches, tabSt[0].d, (long long)tabSt[0].h.size(), dFieldL, dS, dIbuf, dPf, s);
+        launch::contract<double, 52>(dPatches, tabSt[1].d, (long long)tabSt[1].h.size(), dS, dBand, dIbuf, dPf, s);
+    }
+    launch::gatherCsr<double>(nnz, dSrc, dBand, dOvfPtr, dOvfIdx, dMass, s);
+    GSGPU_CUDA_TRY(cudaGetLastError());
+    GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    assembled = false;  // the intermediate buffers now hold the mass matrix's
+    solved = false;
+}
+
 // y = K x with the assembled FP64 matrix (the CG SpMV kernel); x, y on the host
 void Context::applyMatrix(const double* x, double* y) {
     if (!assembled || assembledPrecision != kFP64) throw StateError("apply() needs assemble(GSGPU_PREC_FP64)");
@@ -1455,6 +1487,14 @@ int gsgpu_spmv_stats(gsgpu_context* ctx, long long* launches, double* total_ms, 
         if (launches) *launches = ctx->c.spmvLaunches;
         if (total_ms) *total_ms = ctx->c.spmvMs;
         if (bytes_per_launch) *bytes_per_launch = ctx->c.spmvBytes;
+    });
+}
+
+int gsgpu_mass_csr(gsgpu_context* ctx, double* val) {
+    return guarded(ctx, [&] {
+        ctx->c.assembleMass();
+        if (val && ctx->c.nnz > 0)
+            GSGPU_CUDA_TRY(cudaMemcpy(val, ctx->c.dMass, size_t(ctx->c.nnz) * sizeof(double), cudaMemcpyDeviceToHost));
     });
 }
 

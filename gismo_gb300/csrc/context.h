@@ -252,6 +252,8 @@ struct Context {
     }
     void setCoefs(const double* coefs);
     void assemble(int precision);
+    double* dMass = nullptr;  // mass matrix values in the CSR pattern (gsgpu_mass_csr)
+    void assembleMass();
     void solve(const gsgpu_solver_opts& o, gsgpu_solve_info& info);
     void times(double* ms);
     void freeAssembly();

@@ -450,12 +450,47 @@ struct Stage<22> {
     }
 };
 
+// the mass matrix (gsGenericAssembler::assembleMass): one field M = w |det J| (stored in the load
+// field's slot), one output, the value-value pair factors along every axis; the stages have the
+// geometry of the stiffness stages 31 / 32 / 33 (3D) and 21 / 22 (2D)
+template <>
+struct Stage<41> {
+    static constexpr int AX = 0, NIN = 1, NOUT = 1, NT = 1;
+    GS_HD static Term term(int) { return {0, 0, 0}; }
+};
+template <>
+struct Stage<42> {
+    static constexpr int AX = 1, NIN = 1, NOUT = 1, NT = 1;
+    GS_HD static Term term(int) { return {0, 0, 0}; }
+};
+template <>
+struct Stage<43> {
+    static constexpr int AX = 2, NIN = 1, NOUT = 1, NT = 1;
+    GS_HD static Term term(int) { return {0, 0, 0}; }
+};
+template <>
+struct Stage<51> {
+    static constexpr int AX = 0, NIN = 1, NOUT = 1, NT = 1;
+    GS_HD static Term term(int) { return {0, 0, 0}; }
+};
+template <>
+struct Stage<52> {
+    static constexpr int AX = 1, NIN = 1, NOUT = 1, NT = 1;
+    GS_HD static Term term(int) { return {0, 0, 0}; }
+};
+
 // geometry of a stage for one patch: outer / inner extents, field strides and base offsets
 struct StageGeom {
     long long outer, inner, in_fs, out_fs, in_base, out_base;
 };
 template <int KIND>
 GS_HD StageGeom stageGeom(const DevPatch& D) {
+    // the mass stages: the stiffness stages' geometry, input from the load field's slot
+    if (KIND == 41 || KIND == 42 || KIND == 43 || KIND == 51 || KIND == 52) {
+        StageGeom g = stageGeom<KIND == 41 ? 31 : KIND == 42 ? 32 : KIND == 43 ? 33 : KIND == 51 ? 21 : 22>(D);
+        if (KIND == 41 || KIND == 51) g.in_base = D.lfield_off;
+        return g;
+    }
     StageGeom g{};
     const long long n0W = (long long)D.n[0] * D.W[0], n1W = (long long)D.n[1] * D.W[1];
     if (KIND == 31) {

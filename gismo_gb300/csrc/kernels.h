@@ -23,6 +23,9 @@ void geoStage1(const DevPatch* P, const BlkEnt* tab, long long nblk, const R* co
 template <typename R>
 void geoStage2(const DevPatch* P, const BlkEnt* tab, long long nblk, const R* Y1, const R* gtab, const int* ibuf,
                R* Y2, cudaStream_t s);
+// M = w |det J| per quadrature point into the load field's slot (the mass matrix's field)
+void massField(const DevPatch* P, const BlkEnt* tab, long long nblk, const double* Y1, const double* Y2,
+               const double* gtab, const int* ibuf, const double* wq, double* M, cudaStream_t s);
 template <typename R>
 void pointStep(const DevPatch* P, const BlkEnt* tab, long long nblk, const dev::FieldConst<R>* F, const R* Y1,
                const R* Y2, const R* gtab, const int* ibuf, const R* wq, R* C, R* Lf, unsigned long long* detkey,

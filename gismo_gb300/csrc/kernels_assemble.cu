@@ -62,6 +62,33 @@ __device__ __forceinline__ unsigned long long detKey(double v) {
     return (b & 0x8000000000000000ULL) ? ~b : (b | 0x8000000000000000ULL);
 }
 
+// the mass field M = w |det J| at every quadrature point, into the load field's slot (FP64)
+__global__ void __launch_bounds__(kBlock) k_mass_field(const DevPatch* __restrict__ P, const BlkEnt* __restrict__ tab,
+                                                       const double* __restrict__ Y1, const double* __restrict__ Y2,
+                                                       const double* __restrict__ gtab, const int* __restrict__ ibuf,
+                                                       const double* __restrict__ wq, double* __restrict__ M) {
+    const BlkEnt be = tab[blockIdx.x];
+    const DevPatch& D = P[be.patch];
+    const long long item = be.base + threadIdx.x;
+    if (item >= D.nq) return;
+    const int Q0 = D.Q[0], Q1 = D.Q[1];
+    const int g0 = int(item % Q0);
+    const long long r = item / Q0;
+    const int g1 = int(r % Q1), g2 = int(r / Q1);
+    double x[3], J[3][3];
+    dev::pointMap<double>(D, item, Y1, Y2, gtab, ibuf, x, J);
+    double w = wq[D.qoff[0] + g0] * wq[D.qoff[1] + g1];
+    double det;
+    if (D.dim == 3) {
+        w *= wq[D.qoff[2] + g2];
+        det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) + J[0][1] * (J[1][2] * J[2][0] - J[1][0] * J[2][2]) +
+              J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    } else {
+        det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    }
+    M[D.lfield_off + item] = w * fabs(det);
+}
+
 template <typename R>
 __global__ void __launch_bounds__(kBlock) k_point(const DevPatch* __restrict__ P, const BlkEnt* __restrict__ tab,
                                                   const dev::FieldConst<R>* __restrict__ F, const R* __restrict__ Y1,
@@ -434,6 +461,11 @@ void contract(const DevPatch* P, const BlkEnt* tab, long long nblk, const T* in,
 }
 #define INST_CONTRACT(T, K) \
     template void contract<T, K>(const DevPatch*, const BlkEnt*, long long, const T*, T*, const int*, const T*, cudaStream_t);
+INST_CONTRACT(double, 41)
+INST_CONTRACT(double, 42)
+INST_CONTRACT(double, 43)
+INST_CONTRACT(double, 51)
+INST_CONTRACT(double, 52)
 INST_CONTRACT(double, 31)
 INST_CONTRACT(double, 32)
 INST_CONTRACT(double, 33)
@@ -479,6 +511,11 @@ template void rhsRows<double>(int, const double*, const uint32_t*, const uint32_
                               const uint32_t*, const uint32_t*, const double*, double*, cudaStream_t);
 template void rhsRows<df32>(int, const double*, const uint32_t*, const uint32_t*, const df32*, const uint32_t*,
                             const uint32_t*, const uint32_t*, const double*, double*, cudaStream_t);
+
+void massField(const DevPatch* P, const BlkEnt* tab, long long nblk, const double* Y1, const double* Y2,
+               const double* gtab, const int* ibuf, const double* wq, double* M, cudaStream_t s) {
+    if (nblk > 0) k_mass_field<<<unsigned(nblk), kBlock, 0, s>>>(P, tab, Y1, Y2, gtab, ibuf, wq, M);
+}
 
 void coefsToSoa(const DevPatch* P, const BlkEnt* tab, long long nblk, const double* raw, double* soa, cudaStream_t s) {
     if (nblk > 0) k_coef_soa<<<unsigned(nblk), kBlock, 0, s>>>(P, tab, raw, soa);

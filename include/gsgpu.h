@@ -135,6 +135,13 @@ int gsgpu_sizes(gsgpu_context* ctx, int* nfree, long long* nnz, int* nfixed, int
  * the compressed ColMajor arrays outerIndexPtr / innerIndexPtr / valuePtr). Any of the three
  * pointers may be NULL; ptr/col are available after refresh(), val after assemble(). */
 int gsgpu_matrix_csr(gsgpu_context* ctx, int* ptr, int* col, double* val);
+/* gsGenericAssembler::assembleMass() (src/gsAssembler/gsGenericAssembler.h:103) with the
+ * context's boundary conditions (gsGenericAssembler(patches, bases, opt, &bc)): the mass matrix
+ * M_ij = int phi_i phi_j |det J| over all patches on the free dofs of the same dof map, in the
+ * CSR pattern of gsgpu_matrix_csr (val: nnz values). Runs on the device in FP64; it reuses the
+ * assembly's intermediate buffers, so it invalidates the last assemble() (assemble again before
+ * matrix values, rhs or a solve are needed). */
+int gsgpu_mass_csr(gsgpu_context* ctx, double* val);
 /* gsAssembler::rhs() (gsAssembler.h:618) */
 int gsgpu_rhs(gsgpu_context* ctx, double* rhs);
 /* gsAssembler::fixedDofs() (gsAssembler.h:538); on a host-only context (device -1) computed on

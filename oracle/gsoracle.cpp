@@ -973,6 +973,42 @@ struct Oracle {
         return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
 
+    // gsGenericAssembler::assembleMass (src/gsAssembler/gsGenericAssembler.h:103, its mass visitor
+    // integrating phi_i phi_j |det J| with the assembler's Gauss rule) on the free dofs, in the CSR
+    // pattern of the stiffness matrix; element loop in element order (serial)
+    void mass(double* val) {
+        if (A.ptr.empty()) buildPattern();
+        Csr M = A;
+        std::fill(M.val.begin(), M.val.end(), 0.0);
+        std::vector<double> pts, wts, N, dN;
+        std::vector<int> act;
+        const long long ne = totalElems();
+        for (long long ge = 0; ge < ne; ++ge) {
+            const Elem E = elemAt(ge);
+            const PatchData& P = patches[E.patch];
+            int q[3];
+            elementRule(P, E, pts, wts, q);
+            const int nqt = int(wts.size());
+            elementBasis(P, E, pts, nqt, act, N, dN);
+            const int na = int(act.size());
+            for (int qi = 0; qi < nqt; ++qi) {
+                double x[3], J[9];
+                geoEval(P, &pts[size_t(qi) * dim], x, J);
+                const double w = wts[qi] * std::fabs(det(dim, J));
+                for (int a = 0; a < na; ++a) {
+                    const int ii = map.index[P.offset + act[a]];
+                    if (ii >= map.freeSize) continue;
+                    for (int b = 0; b < na; ++b) {
+                        const int jj = map.index[P.offset + act[b]];
+                        if (jj < map.freeSize)
+                            M.at(ii, jj) += w * N[size_t(a) * nqt + qi] * N[size_t(b) * nqt + qi];
+                    }
+                }
+            }
+        }
+        std::copy(M.val.begin(), M.val.end(), val);
+    }
+
     // gsConjugateGradient with gsJacobiOp (gsConjugateGradient.hpp:19-84,
     // gsIterativeSolver.h:114-202, gsSimplePreconditioners.h:145-244)
     template <class Precond>
@@ -1444,6 +1480,7 @@ double orc_solve_mg(void* h, double tol, int maxit, int levels, int npre, int np
     return static_cast<Oracle*>(h)->solveMG(tol, maxit, levels, npre, npost, damping, cycles, cgc, x, *iters,
                                             *relres);
 }
+void orc_mass(void* h, double* val) { static_cast<Oracle*>(h)->mass(val); }
 double orc_l2_error(void* h, const double* x) { return static_cast<Oracle*>(h)->l2error(x); }
 double orc_h1_error(void* h, const double* x) { return static_cast<Oracle*>(h)->h1error(x); }
 double orc_error_evaluator_rule(void* h, const double* x, int h1) {

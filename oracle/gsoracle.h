@@ -60,6 +60,8 @@ double orc_solve_cg(void* h, double tol, int maxit, double* x, int* iters, doubl
  * cgc = CoarseGridCorrectionDamping */
 double orc_solve_mg(void* h, double tol, int maxit, int levels, int npre, int npost, double damping,
                     int cycles, double cgc, double* x, int* iters, double* relres);
+// gsGenericAssembler::assembleMass on the free dofs, in the CSR pattern of orc_csr (nnz values)
+void orc_mass(void* h, double* val);
 double orc_l2_error(void* h, const double* x);
 /* gsField::distanceH1: H1 seminorm of u_h - u */
 double orc_h1_error(void* h, const double* x);

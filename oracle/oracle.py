@@ -58,6 +58,8 @@ def _lib():
                                  C.c_double, C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)]
     lib.orc_l2_error.restype = C.c_double
     lib.orc_l2_error.argtypes = [vp, C.c_void_p]
+    lib.orc_mass.restype = None
+    lib.orc_mass.argtypes = [vp, C.c_void_p]
     lib.orc_h1_error.restype = C.c_double
     lib.orc_h1_error.argtypes = [vp, C.c_void_p]
     lib.orc_error_evaluator_rule.restype = C.c_double
@@ -172,6 +174,12 @@ class OracleProblem:
         t = lib().orc_solve_mg(self.h, tol, maxit, levels, npre, npost, damping, cycles, cgc_damping, x.ctypes.data,
                                C.byref(it), C.byref(rr))
         return x, it.value, rr.value, t
+
+    def mass(self):
+        """gsGenericAssembler::assembleMass on the free dofs: values in the CSR pattern of csr()."""
+        val = np.empty(self.sizes()[1], np.float64)
+        lib().orc_mass(self.h, val.ctypes.data)
+        return val
 
     def l2_error(self, x):
         x = np.ascontiguousarray(x, np.float64)

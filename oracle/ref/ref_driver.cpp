@@ -23,6 +23,7 @@
 #include <gsPde/gsBoundaryConditions.h>
 #include <gsAssembler/gsPoissonAssembler.h>
 #include <gsAssembler/gsCDRAssembler.h>
+#include <gsAssembler/gsGenericAssembler.h>
 #include <gsSolver/gsConjugateGradient.h>
 #include <gsSolver/gsSimplePreconditioners.h>
 #include <gsSolver/gsMatrixOp.h>
@@ -321,6 +322,19 @@ int main(int argc, char** argv) {
     dump(out + "/csc_val.f64", K.valuePtr(), size_t(K.nonZeros()));
     dump(out + "/rhs.f64", A->rhs().data(), size_t(A->rhs().rows()));
     dump(out + "/ddof.f64", A->fixedDofs().data(), size_t(A->fixedDofs().rows()));
+    {
+        // gsGenericAssembler::assembleMass with the same boundary conditions (the same dof map)
+        gsOptionList gopt = gsGenericAssembler<>::defaultOptions();
+        gopt.setReal("quA", s.quA);
+        gopt.setInt("quB", s.quB);
+        gopt.setInt("DirichletStrategy", dirichlet::elimination);
+        gopt.setInt("InterfaceStrategy", iFace::glue);
+        gsGenericAssembler<> G(mp, mb, gopt, &bc);
+        const gsSparseMatrix<>& M = G.assembleMass();
+        dump(out + "/mass_ptr.i32", M.outerIndexPtr(), size_t(M.cols()) + 1);
+        dump(out + "/mass_idx.i32", M.innerIndexPtr(), size_t(M.nonZeros()));
+        dump(out + "/mass_val.f64", M.valuePtr(), size_t(M.nonZeros()));
+    }
 
     int iters = 0;
     double err = 0, l2 = 0, h1 = 0;

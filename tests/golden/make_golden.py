@@ -2,7 +2,8 @@
 
 Builds the reference's own FP64 assembler/solver from its sources (oracle/ref/Makefile, output in
 oracle/_ref/), runs it on seeded problems from gismo_gb300.problems and stores what it returns
-(dof map, CSC matrix, rhs, eliminated-dof values, solution, iterations, L2 error, H1 seminorm error) as compressed
+(dof map, CSC matrix, rhs, eliminated-dof values, solution, iterations, L2 error, H1 seminorm error, and the
+mass matrix of gsGenericAssembler::assembleMass with the same boundary conditions) as compressed
 .npz files next to this script. Run from the repository root, in a container that has the G+Smo
 source tree:
 
@@ -98,7 +99,11 @@ def run_reference(exe: str, prob, workdir: str) -> dict:
     info = dict(line.split() for line in open(os.path.join(workdir, "info.txt")))
     with open(spec) as fh:
         spec_text = fh.read()
-    return dict(
+    extra = {}
+    if os.path.exists(os.path.join(workdir, "mass_val.f64")):  # gsGenericAssembler::assembleMass
+        extra = dict(mass_ptr=ld("mass_ptr.i32", np.int32), mass_idx=ld("mass_idx.i32", np.int32),
+                     mass_val=ld("mass_val.f64", np.float64))
+    return dict(**extra,
         dofmap=ld("dofmap.i32", np.int32), csc_ptr=ld("csc_ptr.i32", np.int32), csc_idx=ld("csc_idx.i32", np.int32),
         csc_val=ld("csc_val.f64", np.float64), rhs=ld("rhs.f64", np.float64), ddof=ld("ddof.f64", np.float64),
         x=ld("x.f64", np.float64), free=np.int64(info["free"]), nnz=np.int64(info["nnz"]),
@@ -131,6 +136,7 @@ def main():
         with tempfile.TemporaryDirectory() as td:
             res = run_reference(exe, prob, td)
         keep = {k: res[k] for k in ("free", "nnz", "iters", "relres", "l2", "h1")}
+        res.pop("mass_ptr", None), res.pop("mass_idx", None), res.pop("mass_val", None)
         # the spec text of a 64^3 displaced patch is tens of MB: keep its digest, the tests rebuild
         # the problem with large_cases() and compare digests
         keep["spec_sha256"] = np.array(hashlib.sha256(str(res["spec"]).encode()).hexdigest())

@@ -59,6 +59,26 @@ def test_oracle_matches_reference(path):
     assert abs(h1 - float(g["h1"])) <= 1e-10 * float(g["h1"])
 
 
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_oracle_mass_matches_reference(path):
+    """gsGenericAssembler::assembleMass with the fixture's boundary conditions: the reference's mass
+    matrix has the stiffness matrix's pattern, and the oracle's restatement matches its values to
+    1e-12 relative."""
+    name = os.path.basename(path)[:-4]
+    g = load_golden(name)
+    assert "mass_val" in g, name
+    n = int(g["free"])
+    M = sp.csc_matrix((g["mass_val"], g["mass_idx"], g["mass_ptr"]), shape=(n, n)).tocsr()
+    M.sort_indices()
+    K = _csr_from_csc(g)
+    assert np.array_equal(M.indptr, K.indptr) and np.array_equal(M.indices, K.indices)
+    o = O.OracleProblem(golden_problem(name))
+    o.assemble()
+    m = o.mass()
+    assert np.abs(m - M.data).max() <= 1e-12 * np.abs(M.data).max()
+    assert np.all(M.diagonal() > 0)
+
+
 def test_generator_reproduces_fixture_specs():
     """The seeded generator must still produce exactly the inputs the fixtures were made from."""
     import tempfile
