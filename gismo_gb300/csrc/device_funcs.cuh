@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cmath>
+#include <type_traits>
 
 #include "df32.cuh"
 #include "gsgpu_internal.h"
@@ -105,6 +106,23 @@ struct Real<df32> {
     GS_HD static df32 mulInt(df32 a, int k) { return a * float(k); }
 };
 
+// sum of products: FP64 accumulates in place (acc += a * b); double-float accumulates compensated
+// (Dot2: the exact FP32 products and the rounding errors of the running sum kept in one FP32
+// correction), about half the FP32 operations of a chain of double-float multiplies and adds at
+// an error of a few 2^-48 of the sum of |products|
+template <typename R>
+struct Acc {
+    R s = Real<R>::zero();
+    GS_HD void mac(R a, R b) { s += a * b; }
+    GS_HD R result() const { return s; }
+};
+template <>
+struct Acc<df32> {
+    Dot2 d;
+    GS_HD void mac(df32 a, df32 b) { d.mac(a, b); }
+    GS_HD df32 result() const { return d.result(); }
+};
+
 // the closed-form field constants in the arithmetic of R (built on the host)
 template <typename R>
 struct FieldConst {
@@ -162,9 +180,9 @@ GS_HD R geoStage1(const DevPatch& D, long long item, const R* __restrict__ coefs
     const int f0 = ibuf[D.gqoff[0] + g0];
     const R* tb = gtab + D.gtoff[0] + (long long)g0 * 2 * (gp + 1) + tau * (gp + 1);
     const R* c = coefs + D.coef_off + m * D.ngeo + rest * D.gn[0] + f0;
-    R acc = Real<R>::zero();
-    for (int s = 0; s <= gp; ++s) acc += tb[s] * c[s];
-    return acc;
+    Acc<R> acc;
+    for (int s = 0; s <= gp; ++s) acc.mac(tb[s], c[s]);
+    return acc.result();
 }
 
 // 3D stage 2 (direction 1): Y2[m][tau][i2][g1][g0], tau: 0 vv, 1 dv (d/dxi0), 2 vd (d/dxi1)
@@ -186,9 +204,9 @@ GS_HD R geoStage2(const DevPatch& D, long long item, const R* __restrict__ Y1, c
     const int f1 = ibuf[D.gqoff[1] + g1];
     const R* tb = gtab + D.gtoff[1] + (long long)g1 * 2 * (gp + 1) + t2 * (gp + 1);
     const R* y = Y1 + D.y1_off + ((((long long)m * 2 + t1) * D.gn[2] + i2) * D.gn[1] + f1) * Q0 + g0;
-    R acc = Real<R>::zero();
-    for (int s = 0; s <= gp; ++s) acc += tb[s] * y[(long long)s * Q0];
-    return acc;
+    Acc<R> acc;
+    for (int s = 0; s <= gp; ++s) acc.mac(tb[s], y[(long long)s * Q0]);
+    return acc.result();
 }
 
 // closed-form fields at a physical point: kappa and f = -div(kappa grad u)
@@ -201,6 +219,15 @@ struct Cplx {
 template <typename R>
 GS_HD Cplx<R> cmul(const Cplx<R>& a, const Cplx<R>& b) {
     return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+// the same product with each component rounded once (double-float: dot2Terms), the form of the
+// mode sums below
+template <typename R>
+GS_HD Cplx<R> cmulFused(const Cplx<R>& a, const Cplx<R>& b) {
+    if constexpr (std::is_same<R, df32>::value)
+        return {dot2Terms(a.re, b.re, a.im, b.im, -1.f), dot2Terms(a.re, b.im, a.im, b.re, 1.f)};
+    else
+        return cmul(a, b);
 }
 
 // sum over the Fourier modes of g = sum_m amp_m cos(pi k_m.x + phase_m) and of
@@ -270,7 +297,7 @@ GS_HD void fields(const FieldConst<R>& F, const R* x, R& kappa, R& f) {
         zp[i][0].re += R(1);
         zp[i][0].im = Real<R>::zero();
         const Cplx<R> z{c, s};
-        for (int k = 1; k <= F.kmax; ++k) zp[i][k] = cmul(zp[i][k - 1], z);
+        for (int k = 1; k <= F.kmax; ++k) zp[i][k] = cmulFused(zp[i][k - 1], z);
     }
     R g, gg[3];
     modeSums<R>(F, zp, d, g, gg);
@@ -302,19 +329,19 @@ GS_HD void pointMap(const DevPatch& D, long long item, const R* __restrict__ Y1,
             const R* yvv = Y2 + D.y2_off + (((long long)m * 3 + 0) * D.gn[2] + f2) * plane + (long long)g1 * Q0 + g0;
             const R* ydv = yvv + (long long)D.gn[2] * plane;
             const R* yvd = ydv + (long long)D.gn[2] * plane;
-            R a = Real<R>::zero(), b = Real<R>::zero(), c = Real<R>::zero(), e = Real<R>::zero();
+            Acc<R> a, b, c, e;
             for (int s = 0; s <= gp; ++s) {
                 const R v = tb[s], dv = tb[gp + 1 + s];
                 const long long o = (long long)s * plane;
-                a += v * yvv[o];
-                b += v * ydv[o];
-                c += v * yvd[o];
-                e += dv * yvv[o];
+                a.mac(v, yvv[o]);
+                b.mac(v, ydv[o]);
+                c.mac(v, yvd[o]);
+                e.mac(dv, yvv[o]);
             }
-            x[m] = a;
-            J[m][0] = b;
-            J[m][1] = c;
-            J[m][2] = e;
+            x[m] = a.result();
+            J[m][0] = b.result();
+            J[m][1] = c.result();
+            J[m][2] = e.result();
         }
     } else {
         const int gp = D.gp[1];
@@ -323,17 +350,17 @@ GS_HD void pointMap(const DevPatch& D, long long item, const R* __restrict__ Y1,
         for (int m = 0; m < 2; ++m) {
             const R* yv = Y1 + D.y1_off + (((long long)m * 2 + 0) * D.gn[1] + f1) * Q0 + g0;
             const R* yd = yv + (long long)D.gn[1] * Q0;
-            R a = Real<R>::zero(), b = Real<R>::zero(), c = Real<R>::zero();
+            Acc<R> a, b, c;
             for (int s = 0; s <= gp; ++s) {
                 const R v = tb[s], dv = tb[gp + 1 + s];
                 const long long o = (long long)s * Q0;
-                a += v * yv[o];
-                b += v * yd[o];
-                c += dv * yv[o];
+                a.mac(v, yv[o]);
+                b.mac(v, yd[o]);
+                c.mac(dv, yv[o]);
             }
-            x[m] = a;
-            J[m][0] = b;
-            J[m][1] = c;
+            x[m] = a.result();
+            J[m][0] = b.result();
+            J[m][1] = c.result();
         }
     }
 }
@@ -360,6 +387,49 @@ GS_HD double pointStep(const DevPatch& D, const FieldConst<R>& F, long long item
     fields(F, x, kappa, f);
     const long long nq = D.nq;
     R det;
+    if constexpr (std::is_same<R, df32>::value) {
+        // double-float: every cofactor, the determinant and every metric component as one
+        // compensated sum of exact products (same formulas as the FP64 branch below)
+        if (d == 3) {
+            df32 cof[3][3];
+            auto cf = [&](int a, int b, int c, int e) { return dot2Terms(J[a][b], J[c][e], J[a][e], J[c][b], -1.f); };
+            cof[0][0] = cf(1, 1, 2, 2);
+            cof[0][1] = cf(1, 2, 2, 0);
+            cof[0][2] = cf(1, 0, 2, 1);
+            cof[1][0] = cf(0, 2, 2, 1);
+            cof[1][1] = cf(0, 0, 2, 2);
+            cof[1][2] = cf(0, 1, 2, 0);
+            cof[2][0] = cf(0, 1, 1, 2);
+            cof[2][1] = cf(0, 2, 1, 0);
+            cof[2][2] = cf(0, 0, 1, 1);
+            Dot2 dt;
+            dt.mac(J[0][0], cof[0][0]);
+            dt.mac(J[0][1], cof[0][1]);
+            dt.mac(J[0][2], cof[0][2]);
+            det = dt.result();
+            const df32 sc = w * kappa / Real<R>::abs(det);
+            df32* c = C + D.field_off + item;
+            int k = 0;
+            for (int a = 0; a < 3; ++a)
+                for (int b = a; b < 3; ++b, ++k) {
+                    Dot2 q;
+                    q.mac(cof[0][a], cof[0][b]);
+                    q.mac(cof[1][a], cof[1][b]);
+                    q.mac(cof[2][a], cof[2][b]);
+                    c[k * nq] = sc * q.result();
+                }
+        } else {
+            det = dot2Terms(J[0][0], J[1][1], J[0][1], J[1][0], -1.f);
+            const df32 c00 = J[1][1], c01 = -J[1][0], c10 = -J[0][1], c11 = J[0][0];
+            const df32 sc = w * kappa / Real<R>::abs(det);
+            df32* c = C + D.field_off + item;
+            c[0] = sc * dot2Terms(c00, c00, c10, c10, 1.f);
+            c[nq] = sc * dot2Terms(c00, c01, c10, c11, 1.f);
+            c[2 * nq] = sc * dot2Terms(c01, c01, c11, c11, 1.f);
+        }
+        Lf[D.lfield_off + item] = w * Real<R>::abs(det) * f;
+        return Real<R>::toD(det);
+    }
     if (d == 3) {
         R cof[3][3];
         cof[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
