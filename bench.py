@@ -310,15 +310,21 @@ def main():
         g1 = torch.cuda.Event(enable_timing=True)
         g0.record(stream)
         fp_infos = []
+        fp_asm = []
         for _ in range(args.steps):
             A.assemble("fp64")
+            fp_asm.append(A.assemble_times())
             _, fi = A.solve(tol=args.tol, download=False)
             fp_infos.append(fi)
         g1.record(stream)
         g1.synchronize()
         t64 = g0.elapsed_time(g1) / args.steps
+        fa = np.mean(np.array(fp_asm), axis=0)
         fp64_line = {"value": ws * nfree / (t64 * 1e-3), "unit": "DoF/s", "ms_per_step": t64,
-                     "iterations": fp_infos[-1]["iterations"], "speedup_mixed_over_fp64": t64 / ms_per_step}
+                     "iterations": fp_infos[-1]["iterations"], "speedup_mixed_over_fp64": t64 / ms_per_step,
+                     "t_solve_ms": float(np.mean([f["t_solve_ms"] for f in fp_infos])),
+                     "assemble_ms": {"geometry_fields": fa[2], "stiffness": fa[3], "load": fa[4],
+                                     "scatter": fa[5], "total": fa[6]}}
         for _ in range(2):
             step()
 
@@ -364,10 +370,13 @@ def main():
     achieved = sp_bytes / (sp_ms / nl * 1e-3) / 1e9 if nl else None
     nh = 1 + ((2 * args.p + 1) ** 3 - 1) // 2
     if args.mode == "mixed" and sp_bytes == nh * nfree * 4 + 8 * nfree:
-        traffic = profiled_traffic("k_sdia32_dot_volume_p3_64")
-        kname = ("k_sdia32_dot (FP32 inner operator in half-diagonal storage: the lexicographically "
+        inner = A.tuned_variants()[2]
+        kbase = {0: "k_sdia32_dot", 1: "k_sdia32_tma", 2: "k_sdia32_g4"}.get(inner, "k_sdia32_dot")
+        traffic = profiled_traffic(kbase + "_volume_p3_64")
+        kname = (kbase + " (FP32 inner operator in half-diagonal storage: the lexicographically "
                  "non-negative half of the 7^3 neighbour box as 172 diagonals, each stored value read by "
-                 "its row and by its mirror row; + block partials of p.Ap)")
+                 "its row and by its mirror row; " + ("four rows per thread, 16-byte loads; " if inner == 2 else "")
+                 + "+ block partials of p.Ap)")
     elif args.mode == "mixed":
         traffic = profiled_traffic("k_spmv32_dot_volume_p3_64")
         kname = ("k_spmv32_dot (CSR SpMV + p.Ap of the FP32 inner operator; box rows take their column "
@@ -383,7 +392,7 @@ def main():
 
     it = infos[-1]["iterations"]
     chunks = math.ceil(it / 16) + 1 if it else 1
-    if args.mode == "mixed" and "k_sdia32_dot" in kname:
+    if args.mode == "mixed" and kname.startswith("k_sdia32"):
         # counted in the launch list of one step (profiles/launches_volume_p3_64_mixed.md): assemble 23
         # (basis 2, pair 1, to_df 2, geo 2, point 1, contraction 9 with the tuned stage-2 width, load 3,
         # gather 1, half-diagonal build 1, rhs 1); solve: dinv 1, init 2, per graph chunk 16 x 4 iteration

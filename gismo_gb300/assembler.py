@@ -224,8 +224,8 @@ class GpuPoissonAssembler:
     def autotune(self):
         """Time every kernel variant on this problem, record the fastest in the process-wide tuning
         table and apply it (gsgpu_autotune). Returns the measured milliseconds: six stiffness
-        combinations and two inner products (-1 where not applicable)."""
-        ms = np.empty(8, np.float64)
+        combinations and three inner products (-1 where not applicable)."""
+        ms = np.empty(9, np.float64)
         self._check(self.L.gsgpu_autotune(self.h, ms.ctypes.data))
         return ms
 

@@ -72,7 +72,7 @@ bool tuneLoad(const char* path) {
         double ms;
         if (!(is >> kind >> dim >> p >> q >> v >> ms)) return false;
         const bool ok = (kind == kTuneStage31 && v >= 0 && v <= 2) || (kind == kTuneStage32 && v >= 0 && v <= 1) ||
-                        (kind == kTuneInner && v >= 0 && v <= 1);
+                        (kind == kTuneInner && v >= kInnerSdiaLoads && v <= kInnerSdiaRows4);
         if (!ok || dim < 2 || dim > 3 || p < 1 || p > 4 || q < 1) return false;
         add[std::make_tuple(kind, dim, p, q)] = Entry{v, ms};
     }
@@ -91,8 +91,9 @@ int gaussPoints(const ProblemDesc& pd, int p) { return int(pd.quA * p + pd.quB +
 }  // namespace
 
 // variants of this problem: the table, else the defaults (measured on GB300: stage-1 tiles where the
-// degree has them, 4 output fields, the load-based inner product); the environment overrides
-// (GSGPU_NO_TILE31, GSGPU_ROW_NH=2|4, GSGPU_SDIA_TMA) come last
+// degree has them, 4 output fields, the load-based inner product with four rows per thread); the
+// environment overrides (GSGPU_NO_TILE31, GSGPU_ROW_NH=2|4, GSGPU_SDIA_INNER=0|1|2, GSGPU_SDIA_TMA)
+// come last
 void Context::applyTuning() {
     const int dim = pd.dim;
     for (int P = 1; P <= 4; ++P) {
@@ -110,10 +111,14 @@ void Context::applyTuning() {
         tuned31[P] = v31;
         tuned32[P] = v32;
     }
-    tunedInner = kInnerSdiaLoads;
+    tunedInner = kInnerSdiaRows4;
     if (sdiaOk) {
         const int v = tuneLookup({kTuneInner, dim, sdiaOp.p[0], gaussPoints(pd, sdiaOp.p[0])});
         if (v >= 0) tunedInner = v;
+    }
+    if (const char* e = std::getenv("GSGPU_SDIA_INNER")) {
+        const int v = std::atoi(e);
+        if (v >= kInnerSdiaLoads && v <= kInnerSdiaRows4) tunedInner = v;
     }
     if (std::getenv("GSGPU_SDIA_TMA")) tunedInner = kInnerSdiaTma;
 }
@@ -121,8 +126,8 @@ void Context::applyTuning() {
 void Context::autotune(double* ms) {
     if (!refreshed) throw StateError("autotune() before refresh()");
     if (device < 0) throw StateError("autotune() needs a CUDA device (host-only context)");
-    double out[8];
-    std::fill(out, out + 8, -1.0);
+    double out[9];
+    std::fill(out, out + 9, -1.0);
     const int dim = pd.dim;
     // degrees present along the stage axes
     std::vector<int> deg0, deg1;
@@ -179,7 +184,7 @@ void Context::autotune(double* ms) {
         const double m0 = spmvMs;
         double best = std::numeric_limits<double>::infinity();
         int bv = kInnerSdiaLoads;
-        for (int v : {kInnerSdiaLoads, kInnerSdiaTma}) {
+        for (int v : {kInnerSdiaLoads, kInnerSdiaTma, kInnerSdiaRows4}) {
             tunedInner = v;
             if (!setInnerVariant()) continue;
             profiling = true;
@@ -200,7 +205,7 @@ void Context::autotune(double* ms) {
     applyTuning();
     if (sdiaOk && dValHi) setInnerVariant();
     assemble(kMixed);  // leave the context assembled with the chosen variants
-    if (ms) std::copy(out, out + 8, ms);
+    if (ms) std::copy(out, out + 9, ms);
 }
 
 }  // namespace gsgpu

@@ -11,8 +11,9 @@ namespace gsgpu {
 enum : int { kStage31Tiles = 0, kStage31RowsNh4 = 1, kStage31RowsNh2 = 2 };
 // 3D stiffness stage 2 (axis 1): rows with 4 / 2 output fields per launch
 enum : int { kStage32RowsNh4 = 0, kStage32RowsNh2 = 1 };
-// inner FP32 product of the mixed solve on the half-diagonal operator: load-based or TMA-fed
-enum : int { kInnerSdiaLoads = 0, kInnerSdiaTma = 1 };
+// inner FP32 product of the mixed solve on the half-diagonal operator: load-based with one row per
+// thread, TMA-fed, or load-based with four rows per thread and 16-byte loads
+enum : int { kInnerSdiaLoads = 0, kInnerSdiaTma = 1, kInnerSdiaRows4 = 2 };
 
 enum TuneKind : int { kTuneInner = 1, kTuneStage31 = 31, kTuneStage32 = 32 };
 struct TuneKey {

@@ -6,6 +6,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
@@ -923,9 +924,10 @@ void Context::ensureMixedBuffers() {
     allocN(arena, dR32, n);
     allocN(arena, dZ32, n);
     if (sdiaOk) {
-        // the half-diagonal product reads x up to sdiaReach entries before and after the vector:
-        // the direction carries that many zeros on both sides (written once, never overwritten)
-        const int pad = (launch::sdiaReach(sdiaOp) + 63) / 64 * 64;
+        // the half-diagonal product reads x up to sdiaReach entries (plus the 16-float windows of the
+        // four-row product) before and after the vector: the direction carries that many zeros on
+        // both sides (written once, never overwritten)
+        const int pad = (launch::sdiaReach(sdiaOp) + 16 + 63) / 64 * 64;
         allocN(arena, dP32pad, (long long)n + 2LL * pad);
         GSGPU_CUDA_TRY(cudaMemsetAsync(dP32pad, 0, (size_t(n) + 2 * size_t(pad)) * sizeof(float), stream));
         dP32 = dP32pad + pad;
@@ -948,14 +950,22 @@ void Context::ensureMixedBuffers() {
 }
 
 // the half-diagonal inner product of the tuned variant: TMA-fed (tensor maps of the diagonals and of
-// the direction vector) or load-based, the default: on GB300 the load-based one measured faster
-// (C2 inner product 0.058 vs 0.087 ms). False when the TMA maps are refused (the load-based product
-// stays; GSGPU_REQUIRE_TMA=1 makes that an error, for the tests). The captured solver graph holds
-// the product's launch and is dropped.
+// the direction vector), or load-based with one or four rows per thread. False when the variant
+// cannot run on these buffers (the one-row load-based product stays; GSGPU_REQUIRE_TMA=1 makes a
+// refused TMA map an error, for the tests). The captured solver graph holds the product's launch
+// and is dropped.
 bool Context::setInnerVariant() {
     if (!sdiaOk || !dSdia) return false;
     if (gexecMixed) cudaGraphExecDestroy(gexecMixed), gexecMixed = nullptr;
     sdiaOp.tmaps = nullptr;
+    sdiaOp.group = 1;
+    if (tunedInner == kInnerSdiaRows4) {
+        // 16-byte loads of the diagonals and of x, 16-byte stores of t
+        auto a16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
+        if (!a16(dSdia) || !a16(dP32) || !a16(dT32) || sdiaOp.ns % 4 != 0) return false;
+        sdiaOp.group = 4;
+        return true;
+    }
     if (tunedInner != kInnerSdiaTma) return true;
     std::string why;
     if (launch::sdiaTensorMaps(sdiaOp, dP32, sdiaMaps, &why)) {
@@ -1517,8 +1527,8 @@ int gsgpu_eval_fields(const gsgpu_problem* prob, int npts, const double* x, doub
     return GSGPU_OK;
 }
 
-int gsgpu_autotune(gsgpu_context* ctx, double* ms8) {
-    return guarded(ctx, [&] { ctx->c.autotune(ms8); });
+int gsgpu_autotune(gsgpu_context* ctx, double* ms9) {
+    return guarded(ctx, [&] { ctx->c.autotune(ms9); });
 }
 
 int gsgpu_tuned_variants(gsgpu_context* ctx, int* v3) {

@@ -165,7 +165,7 @@ struct Context {
     SdiaOp sdiaOp;
     SdiaBand sdiaBand;
     // kernel variants of this problem from the tuning table (autotune.cu), per degree class
-    int tuned31[5] = {0, 0, 0, 0, 0}, tuned32[5] = {0, 0, 0, 0, 0}, tunedInner = 0;
+    int tuned31[5] = {0, 0, 0, 0, 0}, tuned32[5] = {0, 0, 0, 0, 0}, tunedInner = kInnerSdiaRows4;
     void applyTuning();
     bool setInnerVariant();
     // time every variant on this problem, record the fastest in the table, apply it; ms[k]: the time

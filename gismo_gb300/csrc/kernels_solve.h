@@ -33,6 +33,7 @@ struct SdiaOp {
     int m[3] = {1, 1, 1};
     int p[3] = {0, 0, 0};
     int xpad = 0;  // zeros the vector x of the product carries before and after its n entries
+    int group = 1;  // rows per thread of the load-based product: 1 (scalar loads) or 4 (16-byte loads)
     // if set: host copies of the two tensor maps (the diagonals, the vector x) of the TMA-fed product,
     // and the device word its bounded waits set when they expire
     const void* tmaps = nullptr;

@@ -157,6 +157,156 @@ __global__ void __launch_bounds__(kB) k_sdia32_dot(SdiaOp A, const float* __rest
 }
 
 // ---------------------------------------------------------------------------------------------
+// The same product with four consecutive rows r0 .. r0 + 3 (r0 = 4 g) per thread. The row's own
+// values of a diagonal are one 16-byte load; x is read as aligned windows of 16-byte loads that
+// the four rows and the 2 P0 + 1 offsets of a line share (x[r0 + L + j] for every offset L of the
+// line and row j); the mirrored values d[h ns + r0 + j - L] of diagonal h as the two aligned
+// 16-byte loads around them. Where a window starts inside its first 16 bytes depends only on the
+// line offset L21 modulo 4, so the line body is instantiated per residue and every pick from a
+// window is a register move. Each row sums its terms in the order of k_sdia32_dot: both products
+// give the same bits. Compared with one row per thread this issues a quarter of the load
+// instructions and reads x with a fraction of the L1 wavefronts (one pass over each window
+// instead of one unaligned load per offset). Blocks take equal contiguous shares of the row
+// groups (kG4Blocks per SM, all resident), so no SM gets a block more than another.
+constexpr int kG = 4;           // rows per thread
+constexpr int kBG = 128;        // threads per block
+constexpr int kG4BlocksPerSm = 4;
+
+constexpr int mod4(int a) { return ((a % 4) + 4) % 4; }
+
+template <int NV>
+__device__ __forceinline__ void loadWin(const float* p, float (&w)[4 * NV]) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        const float4 q = __ldg(reinterpret_cast<const float4*>(p) + v);
+        w[4 * v] = q.x;
+        w[4 * v + 1] = q.y;
+        w[4 * v + 2] = q.z;
+        w[4 * v + 3] = q.w;
+    }
+}
+__device__ __forceinline__ void loadD2(const float* p, float (&w)[8]) {
+    const float4 a = __ldcg(reinterpret_cast<const float4*>(p));
+    const float4 b = __ldcg(reinterpret_cast<const float4*>(p) + 1);
+    w[0] = a.x, w[1] = a.y, w[2] = a.z, w[3] = a.w;
+    w[4] = b.x, w[5] = b.y, w[6] = b.z, w[7] = b.w;
+}
+
+// one (o2, o1) line for rows r0 .. r0 + 3: dh = d + h_l ns + r0, L21 = (o2 m1 + o1) m0 = C mod 4
+template <int P0, int C>
+__device__ __forceinline__ void lineG4(const float* __restrict__ dh, long long ns, const float* __restrict__ x, int r0,
+                                       int L21, float (&acc)[kG]) {
+    constexpr int W0 = 2 * P0 + 1;
+    constexpr int SU = mod4(C - P0);         // x[r0 + L21 - P0 + i] = xu[SU + i]
+    constexpr int SD = mod4(-C - P0);        // x[r0 - L21 - P0 + i] = xd[SD + i]
+    constexpr int NU = (SU + W0 + 2) / 4 + 1;  // 16-byte loads covering indices 0 .. SU + W0 + 2
+    constexpr int ND = (SD + W0 + 2) / 4 + 1;
+    float xu[4 * NU], xd[4 * ND];
+    loadWin<NU>(x + r0 + L21 - P0 - SU, xu);
+    loadWin<ND>(x + r0 - L21 - P0 - SD, xd);
+    float lsum[kG] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < W0; ++k) {
+        // own: d[(h_l + k) ns + r0 + j]; mirrored: d[(h_l + k) ns + r0 + j - L], L = L21 + k - P0,
+        // read from the aligned pair starting SM floats before r0 - L
+        const float4 v = __ldcg(reinterpret_cast<const float4*>(dh + k * ns));
+        const int SM = mod4(P0 - C - k);
+        float m[8];
+        loadD2(dh + k * ns - L21 + P0 - k - SM, m);
+        const float vu[kG] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int j = 0; j < kG; ++j) {
+            lsum[j] = fmaf(vu[j], xu[SU + k + j], lsum[j]);
+            lsum[j] = fmaf(m[SM + j], xd[SD + 2 * P0 - k + j], lsum[j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < kG; ++j) acc[j] += lsum[j];
+}
+
+template <int P0>
+__global__ void __launch_bounds__(kBG, kG4BlocksPerSm) k_sdia32_g4(SdiaOp A, const float* __restrict__ x,
+                                                                   float* __restrict__ t, double* __restrict__ part,
+                                                                   const CgState* __restrict__ st) {
+    if (st->done || st->pause) return;
+    constexpr int W0 = 2 * P0 + 1;
+    constexpr int kAhead = 2;
+    const int n = A.n;
+    const long long ns = A.ns;
+    const int nlines = A.p[1] + A.p[2] * (2 * A.p[1] + 1);
+    const int ngroups = (n + kG - 1) / kG;
+    const int share = (ngroups + int(gridDim.x) - 1) / int(gridDim.x);
+    const int gEnd = min(ngroups, (int(blockIdx.x) + 1) * share);
+    double contrib = 0.0;
+    for (int g = int(blockIdx.x) * share + int(threadIdx.x); g < gEnd; g += kBG) {
+        const int r0 = g * kG;
+        const float* dh = A.d + r0;
+        for (int l = 0; l < kAhead && l < nlines; ++l)
+#pragma unroll
+            for (int k = 0; k < W0; ++k) prefetchL2(dh + (P0 + 1 + l * W0 + k) * ns);
+        // centre line: x[r0 - 4 .. r0 + 8) covers r0 + j +- o0; the mirrored values of diagonal o0
+        // (d[o0 ns + r0 + j - o0]) lie in the aligned pair starting at r0 - 4
+        float xc[12];
+        loadWin<3>(x + r0 - 4, xc);
+        float acc[kG];
+        {
+            const float4 v = __ldcg(reinterpret_cast<const float4*>(dh));
+            const float v0[kG] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int j = 0; j < kG; ++j) acc[j] = fmaf(v0[j], xc[4 + j], 0.f);
+        }
+#pragma unroll
+        for (int o0 = 1; o0 <= P0; ++o0) {
+            dh += ns;
+            const float4 v = __ldcg(reinterpret_cast<const float4*>(dh));
+            const float vu[kG] = {v.x, v.y, v.z, v.w};
+            float m[8];
+            loadD2(dh - 4, m);
+#pragma unroll
+            for (int j = 0; j < kG; ++j) {
+                acc[j] = fmaf(vu[j], xc[4 + j + o0], acc[j]);
+                acc[j] = fmaf(m[4 + j - o0], xc[4 + j - o0], acc[j]);
+            }
+        }
+        dh += ns;
+        int line = 0;
+        for (int o2 = 0; o2 <= A.p[2]; ++o2)
+            for (int o1 = o2 ? -A.p[1] : 1; o1 <= A.p[1]; ++o1, ++line) {
+                if (line + kAhead < nlines)
+#pragma unroll
+                    for (int k = 0; k < W0; ++k) prefetchL2(dh + (kAhead * W0 + k) * ns);
+                const int L21 = (o2 * A.m[1] + o1) * A.m[0];
+                switch (L21 & 3) {
+                    case 0: lineG4<P0, 0>(dh, ns, x, r0, L21, acc); break;
+                    case 1: lineG4<P0, 1>(dh, ns, x, r0, L21, acc); break;
+                    case 2: lineG4<P0, 2>(dh, ns, x, r0, L21, acc); break;
+                    default: lineG4<P0, 3>(dh, ns, x, r0, L21, acc); break;
+                }
+                dh += W0 * ns;
+            }
+        if (r0 + kG <= n) {
+            *reinterpret_cast<float4*>(t + r0) = make_float4(acc[0], acc[1], acc[2], acc[3]);
+#pragma unroll
+            for (int j = 0; j < kG; ++j) contrib += double(acc[j]) * double(xc[4 + j]);
+        } else {
+            for (int j = 0; j < kG && r0 + j < n; ++j) {
+                t[r0 + j] = acc[j];
+                contrib += double(acc[j]) * double(xc[4 + j]);
+            }
+        }
+    }
+    __shared__ double ws[kBG / 32];
+    contrib = warpSumD(contrib);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = contrib;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sum = 0.0;
+        for (int w = 0; w < kBG / 32; ++w) sum += ws[w];
+        part[blockIdx.x] = sum;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
 // The same product fed by the Tensor Memory Accelerator. A block owns tiles of kTmaT consecutive
 // rows [r0, r0 + kTmaT); per tile it walks the lines of the half box (the centre line, then the
 // (o2, o1) lines), and per line one elected thread issues four tiled bulk copies into a
@@ -376,6 +526,7 @@ int sdiaReach(const SdiaOp& A) { return A.p[0] + A.m[0] * (A.p[1] + A.m[1] * A.p
 
 int sdiaPartials(const SdiaOp& A) {
     if (A.tmaps) return std::max(1, std::min((A.n + kTmaT - 1) / kTmaT, 152 * kTmaBlocksPerSm));
+    if (A.group == kG) return std::max(1, std::min((A.n + kG * kBG - 1) / (kG * kBG), 152 * kG4BlocksPerSm));
     const int nb = (A.n + kB - 1) / kB;
     return std::max(1, std::min(nb, kMaxSpmvBlocks));
 }
@@ -448,6 +599,15 @@ void sdiaSpmv(const SdiaOp& A, const float* x, float* t, double* part, const CgS
         return;
     }
     const int nb = sdiaPartials(A);
+    if (A.group == kG) {
+        switch (A.p[0]) {
+            case 1: k_sdia32_g4<1><<<nb, kBG, 0, s>>>(A, x, t, part, st); break;
+            case 2: k_sdia32_g4<2><<<nb, kBG, 0, s>>>(A, x, t, part, st); break;
+            case 3: k_sdia32_g4<3><<<nb, kBG, 0, s>>>(A, x, t, part, st); break;
+            default: k_sdia32_g4<4><<<nb, kBG, 0, s>>>(A, x, t, part, st); break;
+        }
+        return;
+    }
     switch (A.p[0]) {
         case 1: k_sdia32_dot<1><<<nb, kB, 0, s>>>(A, x, t, part, st); break;
         case 2: k_sdia32_dot<2><<<nb, kB, 0, s>>>(A, x, t, part, st); break;

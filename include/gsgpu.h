@@ -278,17 +278,18 @@ int gsgpu_cg_jacobi_noalloc(int n, const int* ptr, const int* col, const double*
 /* Autotuner of the kernel variants. No counterpart in the reference, whose element loop has no
  * variants. The tuned choices are the 3D stiffness stage 1 (interior rows in shared-memory tiles, or
  * rows with 4 or 2 output fields per launch), the 3D stage 2 (4 or 2 output fields) and the inner
- * FP32 product of single-patch mixed solves (load-based or TMA-fed half-diagonal operator); every
- * variant forms the same sums in the same order, so results do not depend on the choice.
+ * FP32 product of single-patch mixed solves on the half-diagonal operator (load-based with one row
+ * per thread, TMA-fed, or load-based with four rows per thread); every variant forms the same sums
+ * in the same order, so results do not depend on the choice.
  * gsgpu_autotune times each variant on the context's problem with CUDA events (six stiffness
- * combinations and two inner products: ms8[0..5], ms8[6..7], -1 where not applicable; ms8 may be
+ * combinations and three inner products: ms9[0..5], ms9[6..8], -1 where not applicable; ms9 may be
  * NULL), records the fastest per (kernel group, dimension, degree, Gauss points) in a process-wide
  * table, applies it and leaves the context assembled in mixed precision. Contexts refreshed later
  * take their variants from the table. gsgpu_tuned_variants returns a context's variants for the
  * degrees of its first patch: stage 1, stage 2, inner product (-1 when the problem has no
  * half-diagonal operator). The table is saved to and loaded from a text file (lines "kind dim
  * degree gauss_points variant ms"); loading adds to or replaces the entries in memory. */
-int gsgpu_autotune(gsgpu_context* ctx, double* ms8);
+int gsgpu_autotune(gsgpu_context* ctx, double* ms9);
 int gsgpu_tuned_variants(gsgpu_context* ctx, int* v3);
 int gsgpu_tune_save(const char* path);
 int gsgpu_tune_load(const char* path);

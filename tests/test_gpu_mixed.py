@@ -110,6 +110,7 @@ SDIA_CASES = {
     "disp3d_p232_5x6x7": lambda: P.displaced_single_patch(3, (5, 6, 7), (2, 3, 2), 8, 0.04),
     "square_p2_64_neu": lambda: P.mixed_boundary(P.square_poisson(64, 2)),
     "disp3d_p3_12_neu": lambda: P.mixed_boundary(P.volume_poisson(12, 3, seed=3)),
+    "disp3d_p1_14x9x11": lambda: P.displaced_single_patch(3, (14, 9, 11), (1, 1, 1), 6, 0.04),
 }
 
 
@@ -150,23 +151,31 @@ def test_half_diagonal_inner_operator(case, monkeypatch):
     assert abs(out[True] - out[False]) <= max(3, out[False] // 20), out
 
 
-@pytest.mark.parametrize("case", ["volume_p3_16", "disp2d_p4_40x33", "disp3d_p3_12_neu"])
-def test_half_diagonal_tma_is_bitwise_neutral(case, monkeypatch):
-    """The TMA-fed half-diagonal product (GSGPU_SDIA_TMA=1: tiled bulk copies into a shared-memory
-    ring) and the default load-based one form the same products in the same order: the mixed solves
-    give the same bits."""
+@pytest.mark.parametrize("variant", ["tma", "rows4"])
+@pytest.mark.parametrize("case", sorted(SDIA_CASES))
+def test_half_diagonal_variants_are_bitwise_neutral(case, variant, monkeypatch):
+    """The variants of the half-diagonal product form the same products in the same order as the
+    default one-row load-based product: the TMA-fed one (GSGPU_SDIA_TMA=1, tiled bulk copies into a
+    shared-memory ring) and the four-rows-per-thread one (GSGPU_SDIA_INNER=2, 16-byte loads, the
+    window shifts instantiated per line residue); the mixed solves give the same bits. The cases
+    cover odd and even box widths (every residue of the line offsets modulo 4), degrees 2 to 4 per
+    direction, and row counts that are not a multiple of 4."""
     from gismo_gb300.assembler import GpuPoissonAssembler
     prob = SDIA_CASES[case]()
     xs = []
-    for tma in (True, False):
-        if tma:
+    for on in (True, False):
+        for k in ("GSGPU_SDIA_TMA", "GSGPU_REQUIRE_TMA", "GSGPU_SDIA_INNER"):
+            monkeypatch.delenv(k, raising=False)
+        if on and variant == "tma":
             monkeypatch.setenv("GSGPU_SDIA_TMA", "1")
             monkeypatch.setenv("GSGPU_REQUIRE_TMA", "1")  # fail loudly if the tensor maps are refused
+        elif on:
+            monkeypatch.setenv("GSGPU_SDIA_INNER", "2")
         else:
-            monkeypatch.delenv("GSGPU_SDIA_TMA", raising=False)
-            monkeypatch.delenv("GSGPU_REQUIRE_TMA", raising=False)
+            monkeypatch.setenv("GSGPU_SDIA_INNER", "0")
         A = GpuPoissonAssembler(prob)
         A.assemble("mixed")
+        assert A.tuned_variants()[2] == ({"tma": 1, "rows4": 2}[variant] if on else 0)
         x, info = A.solve(tol=1e-11, precision="mixed", max_iters=20000)
         assert info["converged"], info
         xs.append((x, info["iterations"]))

@@ -48,7 +48,7 @@ def test_autotune_chooses_bitwise_neutral_variants(case, table):
         assert (ms[0] > 0) == (prob.patches[0].degree[0] in (2, 3))  # tiles only for degrees 2, 3
     else:
         assert np.all(ms[:6] == -1)                         # nothing to tune in the 2D stiffness
-    assert v[2] in (0, 1) and ms[6] > 0
+    assert v[2] in (0, 1, 2) and ms[6] > 0 and ms[8] > 0
     x1, i1 = A.solve(tol=1e-11, precision="mixed", max_iters=20000)
     assert i1["iterations"] == i0["iterations"]
     assert np.array_equal(x1, x0), (v0, v)

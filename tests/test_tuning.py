@@ -39,8 +39,9 @@ def _variants(L, prob):
 
 
 def test_defaults_without_a_table(lib):
-    # degree 3: stage-1 tiles (0), stage 2 with 4 output fields (0), load-based inner product (0)
-    assert _variants(lib, P.volume_poisson(8, 3, seed=1, check=False)) == (0, 0, 0)
+    # degree 3: stage-1 tiles (0), stage 2 with 4 output fields (0), load-based inner product with
+    # four rows per thread (2)
+    assert _variants(lib, P.volume_poisson(8, 3, seed=1, check=False)) == (0, 0, 2)
     # degree 4 has no stage-1 tiles: rows with 4 output fields (1); a glued grid has no half-diagonal
     # inner operator (-1)
     assert _variants(lib, P.displaced_single_patch(3, (9, 9, 9), (4, 4, 4), 2, 0.04, check=False))[0] == 1
@@ -54,7 +55,7 @@ def test_table_round_trip_and_lookup(lib, tmp_path):
     assert lib.gsgpu_tune_load(str(f).encode()) == _lib.OK
     assert _variants(lib, P.volume_poisson(8, 3, seed=1, check=False)) == (2, 1, 1)
     # other degrees keep their defaults
-    assert _variants(lib, P.displaced_single_patch(3, (9, 9, 9), (4, 4, 4), 2, 0.04, check=False)) == (1, 0, 0)
+    assert _variants(lib, P.displaced_single_patch(3, (9, 9, 9), (4, 4, 4), 2, 0.04, check=False)) == (1, 0, 2)
     g = tmp_path / "u.txt"
     assert lib.gsgpu_tune_save(str(g).encode()) == _lib.OK
     rows = sorted(tuple(ln.split()) for ln in g.read_text().splitlines() if ln and not ln.startswith("#"))
@@ -69,4 +70,4 @@ def test_invalid_tables_are_rejected(lib, tmp_path, bad):
     f = tmp_path / "bad.txt"
     f.write_text(bad)
     assert lib.gsgpu_tune_load(str(f).encode()) == _lib.ERR_INVALID
-    assert _variants(lib, P.volume_poisson(8, 3, seed=1, check=False)) == (0, 0, 0)  # nothing was taken
+    assert _variants(lib, P.volume_poisson(8, 3, seed=1, check=False)) == (0, 0, 2)  # nothing was taken
