@@ -393,13 +393,13 @@ def main():
     it = infos[-1]["iterations"]
     chunks = math.ceil(it / 16) + 1 if it else 1
     if args.mode == "mixed" and kname.startswith("k_sdia32"):
-        # counted in the launch list of one step (profiles/launches_volume_p3_64_mixed.md): assemble 23
-        # (basis 2, pair 1, to_df 2, geo 2, point 1, contraction 9 with the tuned stage-2 width, load 3,
+        # counted in the launch list of one step (profiles/launches_volume_p3_64_mixed.md): assemble 24
+        # (basis 2, pair 1, to_df 3, geo 2, point 1, contraction 9 with the tuned stage-2 width, load 3,
         # gather 1, half-diagonal build 1, rhs 1); solve: dinv 1, init 2, per graph chunk 16 x 4 iteration
         # kernels (product, alpha, update with beta, direction) + 5 replacement kernels; 12 chunks for
         # 155 iterations with 5 replacements
         chunks = math.ceil(it / 16) + 2 if it else 1
-        launches_per_step = 23 + 3 + (16 * 4 + 5) * chunks
+        launches_per_step = 24 + 3 + (16 * 4 + 5) * chunks
     elif args.mode == "mixed":
         # assemble: basis 2, pair 1, to_df 2, geo 2, point 1, contraction 7 (stage 1: two tile
         # launches + two boundary-row launches; stage 2: interior + boundary rows; stage 3), load 3,

@@ -426,6 +426,7 @@ void Context::refreshUploads() {
     upload(arena, dIbuf, L.ibuf, stream);
     upload(arena, dWq, L.wq, stream);
     allocN(arena, dTab, L.ntab);
+    allocN(arena, dTabDf, L.ntab);
     allocN(arena, dGtab, L.ngtab);
     allocN(arena, dPf, L.npf);
     allocN(arena, dCoefRaw, L.coefs);
@@ -499,6 +500,7 @@ void Context::assemble(int precision) {
     df32* pfDf = reinterpret_cast<df32*>(dPf);
     if (mixed) {
         launch::toDF(L.ngtab, dGtab, gtabDf, s);  // element-wise in place
+        launch::toDF(L.ntab, dTab, dTabDf, s);    // the load contraction's table (dTab stays FP64)
         launch::pairFactors<df32>(dPfJobs, tabPf.d, (long long)tabPf.h.size(), dTab, pfDf, s);
         launch::toDF(L.coefs, dCoefs, dCoefsDf, s);
     } else {
@@ -584,17 +586,18 @@ void Context::assemble(int precision) {
         launch::contract<double, 22>(dPatches, tabSt[1].d, (long long)tabSt[1].h.size(), dS, dBand, dIbuf, dPf, s);
     }
     GSGPU_CUDA_TRY(cudaEventRecord(ev[4], s));
-    // load vector (FP64 contraction of the load field)
+    // load vector (first stage: compensated df32 sums of the df32 load field on the mixed path;
+    // FP64 contraction otherwise and for the later stages)
     if (pd.dim == 3) {
         if (mixed)
-            launch::loadContract<31, df32>(dPatches, tabLd[0].d, (long long)tabLd[0].h.size(), lDf, dLv1, dTab, dIbuf, s);
+            launch::loadContractDF<31>(dPatches, tabLd[0].d, (long long)tabLd[0].h.size(), lDf, dLv1, dTabDf, dIbuf, s);
         else
             launch::loadContract<31, double>(dPatches, tabLd[0].d, (long long)tabLd[0].h.size(), dFieldL, dLv1, dTab, dIbuf, s);
         launch::loadContract<32, double>(dPatches, tabLd[1].d, (long long)tabLd[1].h.size(), dLv1, dLv2, dTab, dIbuf, s);
         launch::loadContract<33, double>(dPatches, tabLd[2].d, (long long)tabLd[2].h.size(), dLv2, dLvec, dTab, dIbuf, s);
     } else {
         if (mixed)
-            launch::loadContract<21, df32>(dPatches, tabLd[0].d, (long long)tabLd[0].h.size(), lDf, dLv1, dTab, dIbuf, s);
+            launch::loadContractDF<21>(dPatches, tabLd[0].d, (long long)tabLd[0].h.size(), lDf, dLv1, dTabDf, dIbuf, s);
         else
             launch::loadContract<21, double>(dPatches, tabLd[0].d, (long long)tabLd[0].h.size(), dFieldL, dLv1, dTab, dIbuf, s);
         launch::loadContract<22, double>(dPatches, tabLd[1].d, (long long)tabLd[1].h.size(), dLv1, dLvec, dTab, dIbuf, s);

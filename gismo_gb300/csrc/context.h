@@ -134,6 +134,7 @@ struct Context {
     dev::FieldConst<double>* dFields = nullptr;
     dev::FieldConst<df32>* dFieldsDf = nullptr;
     double *dKnots = nullptr, *dGknots = nullptr, *dTab = nullptr, *dGtab = nullptr, *dPf = nullptr, *dWq = nullptr;
+    df32* dTabDf = nullptr;  // the basis table as double-float values (the mixed path's load contraction)
     TabJob *dTabJobs = nullptr, *dGtabJobs = nullptr;
     PfJob* dPfJobs = nullptr;
     int* dIbuf = nullptr;

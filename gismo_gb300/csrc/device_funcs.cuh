@@ -939,6 +939,35 @@ GS_HD double loadItem(const DevPatch& D, long long item, const Tin* __restrict__
     return acc;
 }
 
+// the same contraction for a double-float load field and basis table: the products summed by a
+// compensated dot product on the FP32 pipe, the sum rounded to FP64 once per output (no FP64
+// arithmetic and no conversion per term)
+template <int KIND>
+GS_HD double loadItemDF(const DevPatch& D, long long item, const df32* __restrict__ in, const df32* __restrict__ tab,
+                        const int* __restrict__ ibuf) {
+    const int ax = Stage<KIND>::AX;
+    const LoadGeom G = loadGeom<KIND>(D);
+    const int n = D.n[ax], q = D.q[ax], p = D.p[ax], Qa = D.Q[ax];
+    const long long c = item % G.inner;
+    long long r = item / G.inner;
+    const int i = int(r % n);
+    const long long o = r / n;
+    const int* first = ibuf + D.eoff[ax];
+    const int* elo = ibuf + D.doff[ax];
+    const int* ehi = elo + n;
+    const df32* tb = tab + D.toff[ax];
+    Dot2 acc;
+    for (int e = elo[i]; e <= ehi[i]; ++e) {
+        const int s = i - first[e];
+        for (int rr = 0; rr < q; ++rr) {
+            const int g = e * q + rr;
+            acc.mac(tb[(long long)g * 2 * (p + 1) + s], in[G.in_base + (o * Qa + g) * G.inner + c]);
+        }
+    }
+    const df32 v = acc.result();
+    return double(v.hi) + double(v.lo);
+}
+
 // -------------------------------------------------------------------------------------------
 // CSR values: segmented reduction of band entries over the precomputed slot map
 template <typename T>

@@ -48,6 +48,10 @@ void contractRowDF(int P, const DevPatch* Pd, const BlkEnt* tabInt, long long nI
 template <int KIND, typename Tin>
 void loadContract(const DevPatch* P, const BlkEnt* tab, long long nblk, const Tin* in, double* out,
                   const double* basis, const int* ibuf, cudaStream_t s);
+// the first load stage of the double-float path: df32 field and basis table, compensated sums
+template <int KIND>
+void loadContractDF(const DevPatch* P, const BlkEnt* tab, long long nblk, const df32* in, double* out,
+                    const df32* basis, const int* ibuf, cudaStream_t s);
 void gatherCsrDF(long long nnz, const uint32_t* src, const df32* band, const uint32_t* ovf_ptr, const uint32_t* ovf_idx,
                  float* hi, float* lo, cudaStream_t s);
 void toDF(long long n, const double* in, df32* out, cudaStream_t s);

@@ -281,6 +281,17 @@ __global__ void __launch_bounds__(kBlock) k_load(const DevPatch* __restrict__ P,
     out[dev::loadGeom<KIND>(D).out_base + item] = dev::loadItem<KIND, Tin>(D, item, in, basis, ibuf);
 }
 
+template <int KIND>
+__global__ void __launch_bounds__(kBlock) k_load_df(const DevPatch* __restrict__ P, const BlkEnt* __restrict__ tab,
+                                                    const df32* __restrict__ in, double* __restrict__ out,
+                                                    const df32* __restrict__ basis, const int* __restrict__ ibuf) {
+    const BlkEnt be = tab[blockIdx.x];
+    const DevPatch& D = P[be.patch];
+    const long long item = be.base + threadIdx.x;
+    if (item >= dev::loadWork<KIND>(D)) return;
+    out[dev::loadGeom<KIND>(D).out_base + item] = dev::loadItemDF<KIND>(D, item, in, basis, ibuf);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kBlock) k_gather(long long nnz, const uint32_t* __restrict__ src,
                                                    const T* __restrict__ band, const uint32_t* __restrict__ ovf_ptr,
@@ -490,8 +501,16 @@ INST_LOAD(32, double)
 INST_LOAD(33, double)
 INST_LOAD(21, double)
 INST_LOAD(22, double)
-INST_LOAD(31, df32)
-INST_LOAD(21, df32)
+
+template <int KIND>
+void loadContractDF(const DevPatch* P, const BlkEnt* tab, long long nblk, const df32* in, double* out,
+                    const df32* basis, const int* ibuf, cudaStream_t s) {
+    if (nblk > 0) k_load_df<KIND><<<unsigned(nblk), kBlock, 0, s>>>(P, tab, in, out, basis, ibuf);
+}
+template void loadContractDF<31>(const DevPatch*, const BlkEnt*, long long, const df32*, double*, const df32*, const int*,
+                                 cudaStream_t);
+template void loadContractDF<21>(const DevPatch*, const BlkEnt*, long long, const df32*, double*, const df32*, const int*,
+                                 cudaStream_t);
 
 template <typename T>
 void gatherCsr(long long nnz, const uint32_t* src, const T* band, const uint32_t* ovf_ptr, const uint32_t* ovf_idx,
