@@ -552,8 +552,14 @@ void Context::assemble(int precision) {
                 // the unrolled row kernel; boundary rows always by rows
                 const bool tiled = v31 == kStage31Tiles && dev::tiledStage31(P);
                 const long long ni = tiled ? 0 : nb(0);
-                if (tiled)
-                    launch::stage31Tile(P, dPatches, tabTile31[P].d, (long long)tabTile31[P].h.size(), cDf, sDf, pfDf, s);
+                if (tiled) {
+                    // one patch: its row segments per line (the persistent tile kernel's grid stride)
+                    int nseg = 0;
+                    if (L.dev.size() == 1)
+                        nseg = (L.dev[0].n[0] - 2 * P + dev::kTileRows - 1) / dev::kTileRows;
+                    launch::stage31Tile(P, dPatches, tabTile31[P].d, (long long)tabTile31[P].h.size(), cDf, sDf, pfDf,
+                                        nseg, s);
+                }
                 launch::contractRowDF<31, 0, 4>(P, dPatches, tabRow[0][P].d, ni, tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
                 launch::contractRowDF<31, 4, 4>(P, dPatches, tabRow[0][P].d, ni, tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
             } else {

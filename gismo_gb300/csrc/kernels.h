@@ -37,8 +37,10 @@ template <int KIND>
 void contractDF(const DevPatch* P, const BlkEnt* tab, long long nblk, const df32* in, df32* out, const int* ibuf,
                 const df32* pf, cudaStream_t s);
 // 3D stage 1 interior rows in shared-memory tiles (degrees with dev::tiledStage31)
+// nseg: the row segments per line when every tile belongs to one patch (the persistent kernel's
+// grid is a multiple of it), else 0 (one block per tile)
 void stage31Tile(int P, const DevPatch* Pd, const BlkEnt* tab, long long ntiles, const df32* in, df32* out,
-                 const df32* pf, cudaStream_t s);
+                 const df32* pf, int nseg, cudaStream_t s);
 // degree-P specialisation over the patches whose degree along the stage axis is P
 // (degrees 1..4; the context checks the range)
 // interior rows (unrolled fixed-shape kernel, tabInt) and the remaining rows (tabBnd)

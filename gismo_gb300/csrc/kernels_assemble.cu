@@ -1,6 +1,7 @@
 // sm_103a assembly kernels: basis tables (K1), geometry map and coefficient fields (K2),
 // sum-factorised stiffness / load contractions (K3) and the atomic-free CSR gather with the
 // Dirichlet lift (K4). Thread -> item mapping only; the arithmetic lives in device_funcs.cuh.
+#include <cstdlib>
 #include <cstring>
 
 #include "device_funcs.cuh"
@@ -252,6 +253,154 @@ __global__ void __launch_bounds__(dev::kTileLines * dev::kTileRows, 2)
         for (int h = 0; h < 4; ++h) op[(H0 + h) * G.out_fs + w] = acc[w][h].result();
 }
 
+// 8-byte asynchronous copy global -> shared (no register round trip; completes with the group)
+__device__ __forceinline__ void cpAsync8(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(dst))),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cpAsyncCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpAsyncWait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// k_stage31_tile as a persistent kernel: each block walks the tiles blockIdx.x, blockIdx.x + G, ...
+// (G = gridDim.x, a multiple of the row segments per line of a single patch, so that a block's
+// tiles share their elements and pair factors, which it stages once), and double-buffers the
+// coefficient fields: while it forms the outputs of one tile, the fields of its next tile arrive
+// by asynchronous copies into the other buffer. Same products and Dot2 order per output as
+// k_stage31_tile (the same bits); the staging overlaps the arithmetic instead of preceding it.
+template <int P, int H0>
+__global__ void __launch_bounds__(dev::kTileLines * dev::kTileRows, 2)
+    k_stage31_tilep(const DevPatch* __restrict__ Pd, const BlkEnt* __restrict__ tab, long long ntiles,
+                    const df32* __restrict__ in, df32* __restrict__ out, const df32* __restrict__ pf) {
+    using S = dev::Stage<31>;
+    constexpr int P1 = P + 1, Q = P + 1, W = 2 * P + 1, LB = dev::kTileLines, RB = dev::kTileRows;
+    constexpr int NE = dev::tileElems(P);
+    constexpr int F0 = dev::tileField0(H0), NF = dev::tileNField(H0);
+    constexpr int T0 = dev::tileTau0(H0), NTAU = dev::tileNTau(H0);
+    constexpr int NX = dev::tileFieldCount(P, H0);
+    extern __shared__ df32 smem[];
+    df32* sPF = smem;
+    df32* sXb = smem + dev::tilePfCount(P, H0);  // two field buffers of NX values
+    struct TileInfo {
+        int patch, seg, i0, e0, ne, nl, n;
+        long long o0;
+    };
+    auto info = [&](long long j) {
+        const BlkEnt be = tab[j];
+        const DevPatch& D = Pd[be.patch];
+        const int n = D.n[0], E = D.E[0];
+        const int m = n - 2 * P;
+        const int nseg = (m + RB - 1) / RB;
+        const long long tile = be.base / kBlock;
+        TileInfo t;
+        t.patch = be.patch;
+        t.n = n;
+        t.o0 = tile / nseg * LB;
+        t.seg = int(tile % nseg);
+        t.i0 = P + t.seg * RB;
+        t.e0 = t.i0 - P;
+        t.ne = min(NE, E - t.e0);
+        t.nl = int(min((long long)LB, dev::stageGeom<31>(D).outer - t.o0));
+        return t;
+    };
+    auto issueFields = [&](const TileInfo& t, df32* sX) {
+        const DevPatch& D = Pd[t.patch];
+        const dev::StageGeom G = dev::stageGeom<31>(D);
+        const int Qa = D.Q[0];
+        const int perl = t.ne * Q;
+        for (int idx = threadIdx.x; idx < NF * t.nl * perl; idx += blockDim.x) {
+            const int f = idx / (t.nl * perl);
+            int r = idx - f * t.nl * perl;
+            const int l = r / perl;
+            r -= l * perl;
+            const int rr = r % Q;
+            const int ee = r / Q;
+            cpAsync8(&sX[((f * Q + rr) * LB + l) * NE + ee],
+                     &in[G.in_base + (F0 + f) * G.in_fs + (t.o0 + l) * Qa + (long long)t.e0 * Q + r]);
+        }
+    };
+    const long long stride = gridDim.x;
+    long long j = blockIdx.x;
+    if (j >= ntiles) return;
+    TileInfo cur = info(j);
+    issueFields(cur, sXb);
+    cpAsyncCommit();
+    int pfPatch = -1, pfSeg = -1;
+    for (int it = 0; j < ntiles; j += stride, ++it) {
+        df32* sX = sXb + (it & 1) * NX;
+        // the next tile's fields into the other buffer (every thread passed the previous tile's
+        // closing barrier, so nobody reads that buffer any more)
+        TileInfo nxt{};
+        const bool more = j + stride < ntiles;
+        if (more) {
+            nxt = info(j + stride);
+            issueFields(nxt, sXb + ((it + 1) & 1) * NX);
+        }
+        cpAsyncCommit();
+        if (cur.patch != pfPatch || cur.seg != pfSeg) {
+            // pair factors of elements e0 .. e0+ne-1, types T0 .. T0+NTAU-1
+            const DevPatch& D = Pd[cur.patch];
+            const int E = D.E[0];
+            const long long tstride = (long long)E * Q * P1 * P1;
+            const df32* pfa = pf + D.pfoff[0] + T0 * tstride + (long long)cur.e0 * Q * P1 * P1;
+            const int per = cur.ne * Q * P1 * P1;
+            for (int idx = threadIdx.x; idx < NTAU * per; idx += blockDim.x) {
+                const int tau = idx / per;
+                const int jj = idx - tau * per;
+                int r = jj;
+                const int t = r % P1;
+                r /= P1;
+                const int si = r % P1;
+                r /= P1;
+                const int rr = r % Q;
+                const int ee = r / Q;
+                sPF[(((si * Q + rr) * P1 + t) * NTAU + tau) * NE + ee] = pfa[tau * tstride + jj];
+            }
+            pfPatch = cur.patch;
+            pfSeg = cur.seg;
+        }
+        cpAsyncWait<1>();  // this thread's copies of the current tile have landed
+        __syncthreads();   // everyone's, and the pair factors
+        const int l = threadIdx.x / RB, rw = threadIdx.x % RB;
+        const int i = cur.i0 + rw;
+        if (l < cur.nl && i < cur.n - P) {
+            const df32* sx = sX + l * NE + rw;
+            const df32* spf = sPF + rw;
+            Dot2 acc[W][4];
+#pragma unroll
+            for (int k = 0; k <= P; ++k) {
+#pragma unroll
+                for (int rr = 0; rr < Q; ++rr) {
+                    df32 x[NF];
+#pragma unroll
+                    for (int f = 0; f < NF; ++f) x[f] = sx[(f * Q + rr) * LB * NE + k];
+                    const df32* prow = spf + ((P - k) * Q + rr) * P1 * NTAU * NE + k;
+#pragma unroll
+                    for (int t = 0; t < P1; ++t) {
+#pragma unroll
+                        for (int kk = 0; kk < S::NT; ++kk) {
+                            const dev::Term tm = S::term(kk);
+                            if (tm.h >= H0 && tm.h < H0 + 4)
+                                acc[k + t][tm.h - H0].mac(prow[(t * NTAU + tm.tau - T0) * NE], x[tm.f - F0]);
+                        }
+                    }
+                }
+            }
+            const DevPatch& D = Pd[cur.patch];
+            const dev::StageGeom G = dev::stageGeom<31>(D);
+            df32* op = out + G.out_base + ((cur.o0 + l) * cur.n + i) * W;
+#pragma unroll
+            for (int w = 0; w < W; ++w)
+#pragma unroll
+                for (int h = 0; h < 4; ++h) op[(H0 + h) * G.out_fs + w] = acc[w][h].result();
+        }
+        __syncthreads();  // the current buffer (and the pair factors) are free again
+        if (more) cur = nxt;
+    }
+    cpAsyncWait<0>();
+}
+
 // the remaining (boundary) rows with the general element loop
 template <int KIND, int DEG, int H0, int NH>
 __global__ void __launch_bounds__(kBlock) k_contract_row_df_bnd(const DevPatch* __restrict__ P,
@@ -418,22 +567,34 @@ void contractRowDF(int P, const DevPatch* Pd, const BlkEnt* tabInt, long long nI
 }
 template <int P, int H0>
 void stage31TileLaunch(const DevPatch* Pd, const BlkEnt* tab, long long ntiles, const df32* in, df32* out,
-                       const df32* pf, cudaStream_t s) {
+                       const df32* pf, int nseg, cudaStream_t s) {
+    constexpr int threads = dev::kTileLines * dev::kTileRows;
+    if (nseg > 0 && !std::getenv("GSGPU_TILE31_ONESHOT")) {
+        // persistent: two blocks per SM, the grid a multiple of the row segments per line
+        constexpr size_t bytes = size_t(dev::tilePfCount(P, H0) + 2 * dev::tileFieldCount(P, H0)) * sizeof(df32);
+        cudaFuncSetAttribute(k_stage31_tilep<P, H0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+        long long g = 2 * 152;
+        g = g / nseg * nseg;
+        if (g < nseg) g = nseg;
+        if (g > ntiles) g = ntiles;
+        k_stage31_tilep<P, H0><<<unsigned(g), threads, bytes, s>>>(Pd, tab, ntiles, in, out, pf);
+        return;
+    }
     constexpr size_t bytes = size_t(dev::tilePfCount(P, H0) + dev::tileFieldCount(P, H0)) * sizeof(df32);
     // a failure here shows as the launch error the caller checks
     cudaFuncSetAttribute(k_stage31_tile<P, H0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
-    k_stage31_tile<P, H0><<<unsigned(ntiles), dev::kTileLines * dev::kTileRows, bytes, s>>>(Pd, tab, in, out, pf);
+    k_stage31_tile<P, H0><<<unsigned(ntiles), threads, bytes, s>>>(Pd, tab, in, out, pf);
 }
 
 void stage31Tile(int P, const DevPatch* Pd, const BlkEnt* tab, long long ntiles, const df32* in, df32* out,
-                 const df32* pf, cudaStream_t s) {
+                 const df32* pf, int nseg, cudaStream_t s) {
     if (ntiles <= 0) return;
     if (P == 2) {
-        stage31TileLaunch<2, 0>(Pd, tab, ntiles, in, out, pf, s);
-        stage31TileLaunch<2, 4>(Pd, tab, ntiles, in, out, pf, s);
+        stage31TileLaunch<2, 0>(Pd, tab, ntiles, in, out, pf, nseg, s);
+        stage31TileLaunch<2, 4>(Pd, tab, ntiles, in, out, pf, nseg, s);
     } else if (P == 3) {
-        stage31TileLaunch<3, 0>(Pd, tab, ntiles, in, out, pf, s);
-        stage31TileLaunch<3, 4>(Pd, tab, ntiles, in, out, pf, s);
+        stage31TileLaunch<3, 0>(Pd, tab, ntiles, in, out, pf, nseg, s);
+        stage31TileLaunch<3, 4>(Pd, tab, ntiles, in, out, pf, nseg, s);
     }
 }
 
