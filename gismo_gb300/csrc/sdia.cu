@@ -171,6 +171,7 @@ __global__ void __launch_bounds__(kB) k_sdia32_dot(SdiaOp A, const float* __rest
 constexpr int kG = 4;           // rows per thread
 constexpr int kBG = 128;        // threads per block
 constexpr int kG4BlocksPerSm = 4;
+constexpr int kG4Ahead = 1;     // lines of own values prefetched into L2 ahead of their use (swept: 0-4)
 
 constexpr int mod4(int a) { return ((a % 4) + 4) % 4; }
 
@@ -230,7 +231,7 @@ __global__ void __launch_bounds__(kBG, kG4BlocksPerSm) k_sdia32_g4(SdiaOp A, con
                                                                    const CgState* __restrict__ st) {
     if (st->done || st->pause) return;
     constexpr int W0 = 2 * P0 + 1;
-    constexpr int kAhead = 2;
+    constexpr int kAhead = kG4Ahead;
     const int n = A.n;
     const long long ns = A.ns;
     const int nlines = A.p[1] + A.p[2] * (2 * A.p[1] + 1);
