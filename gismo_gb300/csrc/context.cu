@@ -560,8 +560,17 @@ void Context::assemble(int precision) {
                     launch::stage31Tile(P, dPatches, tabTile31[P].d, (long long)tabTile31[P].h.size(), cDf, sDf, pfDf,
                                         nseg, s);
                 }
-                launch::contractRowDF<31, 0, 4>(P, dPatches, tabRow[0][P].d, ni, tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
-                launch::contractRowDF<31, 4, 4>(P, dPatches, tabRow[0][P].d, ni, tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
+                if (tiled) {
+                    // only the boundary rows remain: two output fields per launch (half the
+                    // registers of four, twice the resident warps)
+                    launch::contractRowDF<31, 0, 2>(P, dPatches, tabRow[0][P].d, 0, tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
+                    launch::contractRowDF<31, 2, 2>(P, dPatches, tabRow[0][P].d, 0, tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
+                    launch::contractRowDF<31, 4, 2>(P, dPatches, tabRow[0][P].d, 0, tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
+                    launch::contractRowDF<31, 6, 2>(P, dPatches, tabRow[0][P].d, 0, tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
+                } else {
+                    launch::contractRowDF<31, 0, 4>(P, dPatches, tabRow[0][P].d, ni, tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
+                    launch::contractRowDF<31, 4, 4>(P, dPatches, tabRow[0][P].d, ni, tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
+                }
             } else {
                 launch::contractRowDF<21, 0, 4>(P, dPatches, tabRow[0][P].d, nb(0), tabRowB[0][P].d, nbB(0), cDf, sDf, dIbuf, pfDf, s);
             }

@@ -224,11 +224,20 @@ DF_HD void sincospiDf(df32 x, df32& s, df32& c) {
                             8.2206352466243295e-18};
     // sin(a) = a sum_{j=0..7} (-1)^j a^(2j) / (2j+1)!,  cos(a) = sum_{j=0..8} (-1)^j a^(2j) / (2j)!
     // |a| <= pi/4, so the first omitted terms are below (pi/4)^16/17!/0.90 < 7e-17 of sin(a) and
-    // (pi/4)^18/18! < 3e-18 of cos(a) >= 0.707, both under the df32 unit 2^-48 = 3.6e-15
-    df32 sp(-inv[15]);
-    for (int j = 6; j >= 0; --j) sp = df32((j % 2 ? -1.0 : 1.0) * inv[2 * j + 1]) + a2 * sp;
-    df32 cp(inv[16]);
-    for (int j = 7; j >= 0; --j) cp = df32((j % 2 ? -1.0 : 1.0) * inv[2 * j]) + a2 * cp;
+    // (pi/4)^18/18! < 3e-18 of cos(a) >= 0.707, both under the df32 unit 2^-48 = 3.6e-15.
+    // The tails j >= 6 of both sums (at most (pi/4)^12/13! = 9e-12 and (pi/4)^12/12! = 1.2e-10 of
+    // the sum) are summed in FP32 from the FP32 part of a^2: their rounding (a few 2^-24 of the
+    // tail) and the dropped low part of a^2 (relative 2^-24 raised to at most the 8th power) stay
+    // below 1e-16; the leading terms run in df32
+    const float a2f = a2.hi;
+    float st = float(-inv[15]);
+    st = ffma(a2f, st, float(inv[13]));
+    df32 sp(st, 0.f);
+    for (int j = 5; j >= 0; --j) sp = df32((j % 2 ? -1.0 : 1.0) * inv[2 * j + 1]) + a2 * sp;
+    float ct = float(inv[16]);
+    for (int j = 7; j >= 6; --j) ct = ffma(a2f, ct, float((j % 2 ? -1.0 : 1.0) * inv[2 * j]));
+    df32 cp(ct, 0.f);
+    for (int j = 5; j >= 0; --j) cp = df32((j % 2 ? -1.0 : 1.0) * inv[2 * j]) + a2 * cp;
     const df32 sa = a * sp, ca = cp;
     const int q = ((int)n) & 3;
     if (q == 0) { s = sa; c = ca; }
@@ -243,11 +252,14 @@ DF_HD df32 expDf(df32 y) {
     df32 r = y - dfLn2() * k;
     r = df32(fmul(r.hi, 0.0625f), fmul(r.lo, 0.0625f));
     // degree 7: |r/16| <= ln2/32, so the first omitted term (ln2/32)^8/8! < 1.3e-18, and below
-    // 2.1e-17 after the 4 squarings
+    // 2.1e-17 after the 4 squarings. The tail j >= 5 (at most (ln2/32)^5/5! = 4e-11) is summed in
+    // FP32 from the FP32 part of r: its error, 16 times that after the squarings, stays below 1e-16
     const double inv[8] = {1.0, 1.0, 0.5, 1.6666666666666666e-01, 4.1666666666666664e-02, 8.3333333333333332e-03,
                            1.3888888888888889e-03, 1.9841269841269841e-04};
-    df32 e(inv[7]);
-    for (int j = 6; j >= 0; --j) e = df32(inv[j]) + r * e;
+    float et = float(inv[7]);
+    for (int j = 6; j >= 5; --j) et = ffma(r.hi, et, float(inv[j]));
+    df32 e(et, 0.f);
+    for (int j = 4; j >= 0; --j) e = df32(inv[j]) + r * e;
     for (int j = 0; j < 4; ++j) e = e * e;
     return ldexpDf(e, int(k));
 }
