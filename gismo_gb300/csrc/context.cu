@@ -1021,6 +1021,10 @@ void Context::solveMixed(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
     if (const char* e = std::getenv("GSGPU_MIXED_DELTA")) B.delta = std::atof(e);  // tuning override
     B.r32 = dR32; B.z32 = dZ32; B.p32 = dP32; B.t32 = dT32; B.dx32 = dDx32; B.xhi = dXhi; B.xlo = dXlo;
     if (sdiaOk) B.sdia = sdiaOp;
+    {
+        auto a16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
+        B.vec4 = a16(dDx32) && a16(dR32) && a16(dZ32) && a16(dP32) && a16(dT32) && a16(dDinv32);
+    }
     const double tol = o.tol > 0 ? o.tol : 1e-10;
     const int maxit = o.max_iters > 0 ? o.max_iters : 1000;
     launch::mixedInit(B, tol, maxit, s);

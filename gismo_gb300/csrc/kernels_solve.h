@@ -74,6 +74,7 @@ struct CgBuffers {
           *xlo = nullptr;
     // if sdia.d is set, the inner FP32 products use the half-diagonal form instead of the CSR hi values
     SdiaOp sdia;
+    bool vec4 = false;  // the FP32 vectors are 16-byte aligned: the half-diagonal path's vector kernels take four entries a thread
 };
 
 struct df32;
