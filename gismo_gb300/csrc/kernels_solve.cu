@@ -497,24 +497,32 @@ __global__ void __launch_bounds__(kB) k_xupd(int n, double* __restrict__ x, floa
 }
 
 // r = b - (A_hi + A_lo) x with df32 products and compensated accumulation; partial sums of r.r
-template <int LPR, bool REL>
+// (box rows take their column offsets from the shared table, as in the FP32 SpMV: the same slots in
+// the same order, 8 instead of 10 bytes per non-zero)
+template <int LPR, bool REL, bool BOX>
 __global__ void __launch_bounds__(kB) k_resid_df(int n, const int* __restrict__ ptr, const int* __restrict__ col,
-                                                 const int16_t* __restrict__ coff,
+                                                 const int16_t* __restrict__ coff, const uint8_t* __restrict__ box,
+                                                 const int* __restrict__ boxOff, int nbox,
                                                  const float* __restrict__ hi, const float* __restrict__ lo,
                                                  const float* __restrict__ xhi, const float* __restrict__ xlo,
                                                  const double* __restrict__ b, double* __restrict__ r,
                                                  double* __restrict__ part, const CgState* __restrict__ st) {
     if (st->done || !st->pause) return;
+    __shared__ int sbox[BOX ? launch::kMaxBox : 1];
+    stageBox<BOX>(sbox, boxOff, nbox);
     const int rowsPerBlock = kB / LPR;
     const int lane = threadIdx.x % LPR;
     double contrib = 0.0;
     for (int base = blockIdx.x * rowsPerBlock; base < n; base += gridDim.x * rowsPerBlock) {
         const int row = base + threadIdx.x / LPR;
         Dot2 acc;
-        if (row < n)
-            dev::rowMac<LPR, kUnroll, REL>(
-                row, ptr[row], ptr[row + 1], lane, col, coff, [&](int k) { return df32(hi[k], lo[k]); },
-                [&](int c) { return df32(xhi[c], xlo[c]); }, [&](df32 v, df32 x) { acc.mac(v, x); });
+        if (row < n) {
+            auto fv = [&](int k) { return df32(hi[k], lo[k]); };
+            auto fx = [&](int c) { return df32(xhi[c], xlo[c]); };
+            auto fm = [&](df32 v, df32 x) { acc.mac(v, x); };
+            if (BOX && box[row]) dev::rowMacBox<LPR, kUnroll>(row, ptr[row], ptr[row + 1], lane, sbox, fv, fx, fm);
+            else dev::rowMac<LPR, kUnroll, REL>(row, ptr[row], ptr[row + 1], lane, col, coff, fv, fx, fm);
+        }
         df32 y = acc.result();
         for (int o = LPR / 2; o > 0; o >>= 1) {
             df32 oth(__shfl_xor_sync(0xffffffffu, y.hi, o), __shfl_xor_sync(0xffffffffu, y.lo, o));
@@ -649,17 +657,6 @@ void cgInit(const CgBuffers& B, double tol, int maxit, cudaStream_t s) {
 }
 
 // launch a row kernel template for the lanes-per-row and column-format choice of B
-#define GSGPU_ROW_DISPATCH(KERNEL, NB, ...)                                                                    \
-    do {                                                                                                       \
-        const bool rel = B.coff != nullptr;                                                                    \
-        switch (B.lanes_per_row) {                                                                             \
-            case 4: rel ? KERNEL<4, true><<<NB, kB, 0, s>>>(__VA_ARGS__) : KERNEL<4, false><<<NB, kB, 0, s>>>(__VA_ARGS__); break; \
-            case 8: rel ? KERNEL<8, true><<<NB, kB, 0, s>>>(__VA_ARGS__) : KERNEL<8, false><<<NB, kB, 0, s>>>(__VA_ARGS__); break; \
-            case 16: rel ? KERNEL<16, true><<<NB, kB, 0, s>>>(__VA_ARGS__) : KERNEL<16, false><<<NB, kB, 0, s>>>(__VA_ARGS__); break; \
-            default: rel ? KERNEL<32, true><<<NB, kB, 0, s>>>(__VA_ARGS__) : KERNEL<32, false><<<NB, kB, 0, s>>>(__VA_ARGS__); break; \
-        }                                                                                                      \
-    } while (0)
-
 // kernels with the box-row template flag: <LPR, REL, BOX>
 #define GSGPU_BOX_ROW(KERNEL, L, NB, ...)                                                               \
     do {                                                                                                \
@@ -774,8 +771,8 @@ void mixedReplace(const CgBuffers& B, cudaStream_t s) {
     const int np = cgPartials(B.n);
     const int nb = spmvPartials(B.n, B.lanes_per_row);
     k_xupd<<<np, kB, 0, s>>>(B.n, B.x, B.dx32, B.xhi, B.xlo, B.st);
-    GSGPU_ROW_DISPATCH(k_resid_df, nb, B.n, B.ptr, B.col, B.coff, B.val_hi, B.val_lo, B.xhi, B.xlo, B.b, B.r, B.part2,
-                       B.st);
+    GSGPU_BOX_DISPATCH(k_resid_df, nb, B.n, B.ptr, B.col, B.coff, B.box, B.box_off, B.nbox, B.val_hi, B.val_lo, B.xhi,
+                       B.xlo, B.b, B.r, B.part2, B.st);
     k_rel_check<<<1, kB, 0, s>>>(nb, B.part2, B.st);
     k_r32<<<np, kB, 0, s>>>(B.n, B.r, B.r32, B.z32, B.p32, B.dinv32, B.part1, B.st);
     k_rho<<<1, kB, 0, s>>>(np, B.part1, B.st);
