@@ -406,9 +406,11 @@ void Context::refreshUploads() {
     {
         std::vector<dev::FieldConst<double>> fc64;
         std::vector<dev::FieldConst<df32>> fcdf;
+        fieldKmax = 0;
         for (const FieldParams& F : pd.fieldTable()) {
             fc64.push_back(dev::fieldConst<double>(F));
             fcdf.push_back(dev::fieldConst<df32>(F));
+            fieldKmax = std::max(fieldKmax, F.kmax);
         }
         upload(arena, dFields, fc64, stream);
         upload(arena, dFieldsDf, fcdf, stream);
@@ -522,13 +524,13 @@ void Context::assemble(int precision) {
         if (pd.dim == 3)
             launch::geoStage2<df32>(dPatches, tabGeo2.d, (long long)tabGeo2.h.size(), y1Df, gtabDf, dIbuf, y2Df, s);
         launch::pointStep<df32>(dPatches, tabPoint.d, (long long)tabPoint.h.size(), dFieldsDf, y1Df, y2Df, gtabDf,
-                                dIbuf, dWqDf, cDf, lDf, dDetKey, s);
+                                dIbuf, dWqDf, cDf, lDf, dDetKey, fieldKmax, s);
     } else {
         launch::geoStage1<double>(dPatches, tabGeo1.d, (long long)tabGeo1.h.size(), dCoefs, dGtab, dIbuf, dY1, s);
         if (pd.dim == 3)
             launch::geoStage2<double>(dPatches, tabGeo2.d, (long long)tabGeo2.h.size(), dY1, dGtab, dIbuf, dY2, s);
         launch::pointStep<double>(dPatches, tabPoint.d, (long long)tabPoint.h.size(), dFields, dY1, dY2, dGtab, dIbuf,
-                                  dWq, dFieldC, dFieldL, dDetKey, s);
+                                  dWq, dFieldC, dFieldL, dDetKey, fieldKmax, s);
     }
     GSGPU_CUDA_TRY(cudaEventRecord(ev[3], s));
     // K3: sum-factorised stiffness contraction into the band
@@ -1298,9 +1300,11 @@ int gsgpu::updateBatchData(gsgpu_context* ctx, std::vector<gsgpu::ProblemDesc>& 
         }
         std::vector<gsgpu::dev::FieldConst<double>> fc64;
         std::vector<gsgpu::dev::FieldConst<gsgpu::df32>> fcdf;
+        c.fieldKmax = 0;
         for (const gsgpu::FieldParams& F : c.pd.fieldTable()) {
             fc64.push_back(gsgpu::dev::fieldConst<double>(F));
             fcdf.push_back(gsgpu::dev::fieldConst<gsgpu::df32>(F));
+            c.fieldKmax = std::max(c.fieldKmax, F.kmax);
         }
         cudaStream_t s = c.stream;
         GSGPU_CUDA_TRY(cudaMemcpyAsync(c.dFields, fc64.data(), fc64.size() * sizeof(fc64[0]), cudaMemcpyHostToDevice, s));

@@ -135,6 +135,7 @@ struct Context {
     dev::FieldConst<df32>* dFieldsDf = nullptr;
     double *dKnots = nullptr, *dGknots = nullptr, *dTab = nullptr, *dGtab = nullptr, *dPf = nullptr, *dWq = nullptr;
     df32* dTabDf = nullptr;  // the basis table as double-float values (the mixed path's load contraction)
+    int fieldKmax = 8;       // the largest Fourier wave number of the uploaded fields
     TabJob *dTabJobs = nullptr, *dGtabJobs = nullptr;
     PfJob* dPfJobs = nullptr;
     int* dIbuf = nullptr;

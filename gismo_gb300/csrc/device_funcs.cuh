@@ -232,8 +232,8 @@ GS_HD Cplx<R> cmulFused(const Cplx<R>& a, const Cplx<R>& b) {
 
 // sum over the Fourier modes of g = sum_m amp_m cos(pi k_m.x + phase_m) and of
 // gg_i = -sum_m amp_m k_mi sin(pi k_m.x + phase_m), from the powers zp[i][k] = exp(i pi k x_i)
-template <typename R>
-GS_HD void modeSums(const FieldConst<R>& F, const Cplx<R> (*zp)[kMaxKappaWave + 1], int d, R& g, R* gg) {
+template <typename R, int NW>
+GS_HD void modeSums(const FieldConst<R>& F, const Cplx<R> (*zp)[NW], int d, R& g, R* gg) {
     g = Real<R>::zero();
     for (int i = 0; i < 3; ++i) gg[i] = Real<R>::zero();
     for (int m = 0; m < F.nmodes; ++m) {
@@ -247,9 +247,8 @@ GS_HD void modeSums(const FieldConst<R>& F, const Cplx<R> (*zp)[kMaxKappaWave + 
 // df32: the amplitude enters with the phase, each complex product rounds once per component
 // (dot2Terms) and the mode sums accumulate compensated (Dot2), about half the FP32 operations of
 // the generic form at an error of a few 2^-48 of sum_m amp_m
-template <>
-GS_HD void modeSums<df32>(const FieldConst<df32>& F, const Cplx<df32> (*zp)[kMaxKappaWave + 1], int d, df32& g,
-                          df32* gg) {
+template <int NW>
+GS_HD void modeSums(const FieldConst<df32>& F, const Cplx<df32> (*zp)[NW], int d, df32& g, df32* gg) {
     Dot2 ag, ag0, ag1, ag2;
     for (int m = 0; m < F.nmodes; ++m) {
         Cplx<df32> e{F.ace[m], F.ase[m]};
@@ -268,7 +267,9 @@ GS_HD void modeSums<df32>(const FieldConst<df32>& F, const Cplx<df32> (*zp)[kMax
     gg[2] = -ag2.result();
 }
 
-template <typename R>
+// KW: the largest wave number the powers table holds (>= F.kmax); the table is a local array indexed
+// by the modes' wave numbers at run time, so its size is what the point kernel's local memory holds
+template <typename R, int KW = kMaxKappaWave>
 GS_HD void fields(const FieldConst<R>& F, const R* x, R& kappa, R& f) {
     const int d = F.dim;
     R sn[3], cs[3];
@@ -288,7 +289,7 @@ GS_HD void fields(const FieldConst<R>& F, const R* x, R& kappa, R& f) {
         f = kappa * lap;
         return;
     }
-    Cplx<R> zp[3][kMaxKappaWave + 1];
+    Cplx<R> zp[3][KW + 1];
     for (int i = 0; i < d; ++i) {
         R s, c;
         if (F.ufreq == 1) { s = sn[i]; c = cs[i]; }
@@ -300,7 +301,7 @@ GS_HD void fields(const FieldConst<R>& F, const R* x, R& kappa, R& f) {
         for (int k = 1; k <= F.kmax; ++k) zp[i][k] = cmulFused(zp[i][k - 1], z);
     }
     R g, gg[3];
-    modeSums<R>(F, zp, d, g, gg);
+    modeSums(F, zp, d, g, gg);
     g = g * F.scale;
     R dot = Real<R>::zero();
     for (int i = 0; i < d; ++i) dot += gg[i] * gu[i];
@@ -369,7 +370,7 @@ GS_HD void pointMap(const DevPatch& D, long long item, const R* __restrict__ Y1,
 // C^{ab} = w kappa |det J| (J^-1 J^-T)_{ab} = w kappa / |det J| sum_m cof_{ma} cof_{mb},
 // L = w |det J| f.  Component order 3D: 00 01 02 11 12 22 ; 2D: 00 01 11.
 // Returns det J.
-template <typename R>
+template <typename R, int KW = kMaxKappaWave>
 GS_HD double pointStep(const DevPatch& D, const FieldConst<R>& F, long long item, const R* __restrict__ Y1,
                        const R* __restrict__ Y2, const R* __restrict__ gtab, const int* __restrict__ ibuf,
                        const R* __restrict__ wq, R* __restrict__ C, R* __restrict__ Lf) {
@@ -384,7 +385,7 @@ GS_HD double pointStep(const DevPatch& D, const FieldConst<R>& F, long long item
     R w = wq[D.qoff[0] + g0] * wq[D.qoff[1] + g1];
     if (d == 3) w = w * wq[D.qoff[2] + g2];
     R kappa, f;
-    fields(F, x, kappa, f);
+    fields<R, KW>(F, x, kappa, f);
     const long long nq = D.nq;
     R det;
     if constexpr (std::is_same<R, df32>::value) {

@@ -26,10 +26,11 @@ void geoStage2(const DevPatch* P, const BlkEnt* tab, long long nblk, const R* Y1
 // M = w |det J| per quadrature point into the load field's slot (the mass matrix's field)
 void massField(const DevPatch* P, const BlkEnt* tab, long long nblk, const double* Y1, const double* Y2,
                const double* gtab, const int* ibuf, const double* wq, double* M, cudaStream_t s);
+// kmax: the largest Fourier wave number of the fields (sizes the point kernel's powers table)
 template <typename R>
 void pointStep(const DevPatch* P, const BlkEnt* tab, long long nblk, const dev::FieldConst<R>* F, const R* Y1,
                const R* Y2, const R* gtab, const int* ibuf, const R* wq, R* C, R* Lf, unsigned long long* detkey,
-               cudaStream_t s);
+               int kmax, cudaStream_t s);
 template <typename T, int KIND>
 void contract(const DevPatch* P, const BlkEnt* tab, long long nblk, const T* in, T* out, const int* ibuf, const T* pf,
               cudaStream_t s);

@@ -90,8 +90,13 @@ __global__ void __launch_bounds__(kBlock) k_mass_field(const DevPatch* __restric
     M[D.lfield_off + item] = w * fabs(det);
 }
 
+// the double-float instance is held to 64 registers (4 blocks per SM; measured faster than the 78
+// it takes unbounded), the FP64 one is left to the compiler; KW sizes the powers table of the
+// Fourier coefficient (the problem's largest wave number, 4 or 8)
 template <typename R>
-__global__ void __launch_bounds__(kBlock) k_point(const DevPatch* __restrict__ P, const BlkEnt* __restrict__ tab,
+constexpr int kPointBlocks = std::is_same<R, df32>::value ? 4 : 1;
+template <typename R, int KW>
+__global__ void __launch_bounds__(kBlock, kPointBlocks<R>) k_point(const DevPatch* __restrict__ P, const BlkEnt* __restrict__ tab,
                                                   const dev::FieldConst<R>* __restrict__ F, const R* __restrict__ Y1,
                                                   const R* __restrict__ Y2, const R* __restrict__ gtab,
                                                   const int* __restrict__ ibuf, const R* __restrict__ wq,
@@ -110,7 +115,7 @@ __global__ void __launch_bounds__(kBlock) k_point(const DevPatch* __restrict__ P
     __syncthreads();
     const long long item = be.base + threadIdx.x;
     unsigned long long key = ~0ULL;
-    if (item < D.nq) key = detKey(dev::pointStep<R>(D, sF, item, Y1, Y2, gtab, ibuf, wq, C, Lf));
+    if (item < D.nq) key = detKey(dev::pointStep<R, KW>(D, sF, item, Y1, Y2, gtab, ibuf, wq, C, Lf));
     for (int o = 16; o > 0; o >>= 1) {
         const unsigned long long other = __shfl_xor_sync(0xffffffffu, key, o);
         key = other < key ? other : key;
@@ -524,8 +529,10 @@ void geoStage2(const DevPatch* P, const BlkEnt* tab, long long nblk, const R* Y1
 template <typename R>
 void pointStep(const DevPatch* P, const BlkEnt* tab, long long nblk, const dev::FieldConst<R>* F, const R* Y1,
                const R* Y2, const R* gtab, const int* ibuf, const R* wq, R* C, R* Lf, unsigned long long* detkey,
-               cudaStream_t s) {
-    if (nblk > 0) k_point<R><<<unsigned(nblk), kBlock, 0, s>>>(P, tab, F, Y1, Y2, gtab, ibuf, wq, C, Lf, detkey);
+               int kmax, cudaStream_t s) {
+    if (nblk <= 0) return;
+    if (kmax <= 4) k_point<R, 4><<<unsigned(nblk), kBlock, 0, s>>>(P, tab, F, Y1, Y2, gtab, ibuf, wq, C, Lf, detkey);
+    else k_point<R, dev::kMaxKappaWave><<<unsigned(nblk), kBlock, 0, s>>>(P, tab, F, Y1, Y2, gtab, ibuf, wq, C, Lf, detkey);
 }
 #define INST_GEO(R)                                                                                                \
     template void geoStage1<R>(const DevPatch*, const BlkEnt*, long long, const R*, const R*, const int*, R*,       \
@@ -533,7 +540,8 @@ void pointStep(const DevPatch* P, const BlkEnt* tab, long long nblk, const dev::
     template void geoStage2<R>(const DevPatch*, const BlkEnt*, long long, const R*, const R*, const int*, R*,       \
                                cudaStream_t);                                                                      \
     template void pointStep<R>(const DevPatch*, const BlkEnt*, long long, const dev::FieldConst<R>*, const R*,      \
-                               const R*, const R*, const int*, const R*, R*, R*, unsigned long long*, cudaStream_t);
+                               const R*, const R*, const int*, const R*, R*, R*, unsigned long long*, int,          \
+                               cudaStream_t);
 INST_GEO(double)
 INST_GEO(df32)
 
