@@ -63,6 +63,38 @@ def test_mixed_solution_matches_fp64(case):
     A.close()
 
 
+def _high_waves():
+    """A displaced 3D degree-2 patch whose kappa modes reach wave number 8 (the point kernel's
+    larger powers table; the other cases stay at 4)."""
+    import numpy as np
+    prob = P.displaced_single_patch(3, (6, 7, 5), (2, 2, 2), 11, 0.04)
+    P.set_kappa_fourier(prob, np.random.default_rng(5), 12, kmax=8)
+    assert int(np.max(prob.kappa_k)) > 4
+    return prob
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_high_wave_numbers_match_the_oracle(precision):
+    """Fourier modes with wave numbers above 4 take the point kernel with the 9-entry powers
+    table: operator and rhs against the FP64 oracle (FP64 1e-12, df32 1e-11)."""
+    from gismo_gb300.assembler import GpuPoissonAssembler
+    from oracle import oracle as O
+    prob = _high_waves()
+    o = O.OracleProblem(prob)
+    o.assemble()
+    optr, ocol, oval = o.csr()
+    A = GpuPoissonAssembler(prob)
+    A.assemble(precision)
+    ptr, col, val = A.csr()
+    tol = 1e-12 if precision == "fp64" else 1e-11
+    assert np.array_equal(ptr, optr) and np.array_equal(col, ocol)
+    rowmax = np.maximum.reduceat(np.abs(oval), optr[:-1])
+    floor = np.repeat(rowmax, np.diff(optr)) * (1e-14 if precision == "fp64" else 1e-13)
+    assert np.all(np.abs(val - oval) <= tol * np.abs(oval) + floor)
+    assert np.abs(A.rhs() - o.rhs()).max() <= tol * np.abs(o.rhs()).max()
+    A.close()
+
+
 def test_mixed_needs_mixed_assembly():
     from gismo_gb300.assembler import GpuPoissonAssembler
     from gismo_gb300._lib import GsGpuError, ERR_STATE
