@@ -208,13 +208,15 @@ def _serve(reqs, precision, tol, slots=4, budget_gb=120.0, max_batch=64):
 
 
 def run_serving(args, sampler):
-    """Both servers solve every request to 1e-9 relative residual, so that each mixed result stays
-    within the metric's 1e-8 (relative 2-norm) of the FP64 solution; the error is measured per
-    request against a tightly converged (1e-12) FP64 solve of the same request, untimed."""
+    """Both servers solve every request to 1e-11 relative residual: the worst request of the mix has a
+    solution error about 150 times its relative residual (1.5e-7 at 1e-9), so 1e-11 keeps each mixed
+    result within the metric's 1e-8 (relative 2-norm) of the FP64 solution. The error is measured per
+    request against a tightly converged (1e-13) FP64 solve of the same request, untimed, and the
+    difference from the plain FP64 server's result is reported beside it."""
     from gismo_gb300 import problems as P
     rates = [50.0, 200.0, 1000.0, 2000.0]
     count = args.requests
-    tol = 1e-9
+    tol = 1e-11
     per_rate = []
     clk = sampler()
     clk.start()
@@ -222,13 +224,14 @@ def run_serving(args, sampler):
         reqs = P.serving_requests(count, rate=rate, seed=11)
         m, res_m = _serve(reqs, "mixed", tol)
         f, res_f = _serve(reqs, "fp64", tol)
-        _, res_t = _serve([(0.0, pr) for _, pr in reqs], "fp64", 1e-12)  # reference solutions, untimed
+        _, res_t = _serve([(0.0, pr) for _, pr in reqs], "fp64", 1e-13)  # reference solutions, untimed
 
-        def worst(res):
+        def worst(res, ref):
             return max(float(np.linalg.norm(a[0] - b[0]) / max(np.linalg.norm(b[0]), 1e-300))
-                       for a, b in zip(res, res_t))
+                       for a, b in zip(res, ref))
         per_rate.append({"rate_req_s": rate, "requests": count, "mixed": m, "plain_fp64": f,
-                         "max_rel_err_mixed_vs_fp64": worst(res_m), "max_rel_err_fp64_at_tol": worst(res_f),
+                         "max_rel_err_mixed_vs_fp64": worst(res_m, res_t), "max_rel_err_fp64_at_tol": worst(res_f, res_t),
+                         "max_rel_diff_mixed_vs_fp64": worst(res_m, res_f),
                          "speedup_mixed_over_fp64": m["dofs_per_s"] / f["dofs_per_s"]})
     # a stream on fixed meshes (8 recurring discretisations, every request its own geometry and
     # kappa field): batches of a recurring structure run on resident contexts without refresh()
@@ -244,11 +247,12 @@ def run_serving(args, sampler):
     clocks = clk.stop()
     top = per_rate[-1]
     cfg = {"workload": "serving_stream", "requests_per_rate": count, "slots": 4, "budget_gb": 120.0,
-           "max_batch": 64, "tol": tol, "error_reference": "each request solved in FP64 to 1e-12",
+           "max_batch": 64, "tol": tol, "error_reference": "each request solved in FP64 to 1e-13",
            "mix": "60% 2D 16..256/dir, 40% 3D 8..48/dir, degree 2..4"}
     line = _line("serving", top["mixed"]["dofs_per_s"], "DoF/s", args, cfg, {
         "p50_ms": top["mixed"]["p50_ms"], "p99_ms": top["mixed"]["p99_ms"],
         "max_rel_err_mixed_vs_fp64": max(r["max_rel_err_mixed_vs_fp64"] for r in per_rate),
+        "max_rel_diff_mixed_vs_fp64": max(r["max_rel_diff_mixed_vs_fp64"] for r in per_rate),
         "rates": per_rate, "fixed_meshes_200_req_s": fm, "clocks": clocks})
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = _cpu_batch([pr for _, pr in P.serving_requests(count, rate=rates[-1], seed=11)])

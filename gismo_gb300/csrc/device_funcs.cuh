@@ -159,43 +159,47 @@ inline FieldConst<R> fieldConst(const FieldParams& F) {
 // -------------------------------------------------------------------------------------------
 // geometry map, sum-factorised over the control net: stage 1 (direction 0)
 // 3D: Y1[m][tau][i2][i1][g0] ; 2D: Y1[m][tau][i1][g0]  (tau: 0 value, 1 derivative)
-template <typename R>
-GS_HD R geoStage1(const DevPatch& D, long long item, const R* __restrict__ coefs, const R* __restrict__ gtab,
+// I: the type of the item's index arithmetic (unsigned where the stage's work fits in 31 bits:
+// its divisions are then a fraction of the 64-bit ones, which dominate these short dot products)
+template <typename R, typename I = long long>
+GS_HD R geoStage1(const DevPatch& D, long long itemL, const R* __restrict__ coefs, const R* __restrict__ gtab,
                   const int* __restrict__ ibuf) {
+    const I item = I(itemL);
     const int Q0 = D.Q[0];
-    const int g0 = int(item % Q0);
-    long long r = item / Q0;
-    long long rest;  // (i2*gn1 + i1) or i1
+    const int g0 = int(item % I(Q0));
+    I r = item / I(Q0);
+    I rest;  // (i2*gn1 + i1) or i1
     if (D.dim == 3) {
-        const long long plane = (long long)D.gn[2] * D.gn[1];
+        const I plane = I(D.gn[2]) * I(D.gn[1]);
         rest = r % plane;
         r /= plane;
     } else {
-        rest = r % D.gn[1];
-        r /= D.gn[1];
+        rest = r % I(D.gn[1]);
+        r /= I(D.gn[1]);
     }
     const int tau = int(r % 2);
     const int m = int(r / 2);
     const int gp = D.gp[0];
     const int f0 = ibuf[D.gqoff[0] + g0];
     const R* tb = gtab + D.gtoff[0] + (long long)g0 * 2 * (gp + 1) + tau * (gp + 1);
-    const R* c = coefs + D.coef_off + m * D.ngeo + rest * D.gn[0] + f0;
+    const R* c = coefs + D.coef_off + m * D.ngeo + (long long)rest * D.gn[0] + f0;
     Acc<R> acc;
     for (int s = 0; s <= gp; ++s) acc.mac(tb[s], c[s]);
     return acc.result();
 }
 
 // 3D stage 2 (direction 1): Y2[m][tau][i2][g1][g0], tau: 0 vv, 1 dv (d/dxi0), 2 vd (d/dxi1)
-template <typename R>
-GS_HD R geoStage2(const DevPatch& D, long long item, const R* __restrict__ Y1, const R* __restrict__ gtab,
+template <typename R, typename I = long long>
+GS_HD R geoStage2(const DevPatch& D, long long itemL, const R* __restrict__ Y1, const R* __restrict__ gtab,
                   const int* __restrict__ ibuf) {
+    const I item = I(itemL);
     const int Q0 = D.Q[0], Q1 = D.Q[1];
-    const int g0 = int(item % Q0);
-    long long r = item / Q0;
-    const int g1 = int(r % Q1);
-    r /= Q1;
-    const int i2 = int(r % D.gn[2]);
-    r /= D.gn[2];
+    const int g0 = int(item % I(Q0));
+    I r = item / I(Q0);
+    const int g1 = int(r % I(Q1));
+    r /= I(Q1);
+    const int i2 = int(r % I(D.gn[2]));
+    r /= I(D.gn[2]);
     const int tau = int(r % 3);
     const int m = int(r / 3);
     const int t1 = (tau == 1) ? 1 : 0;  // derivative in direction 0 (from stage 1)
@@ -312,15 +316,29 @@ GS_HD void fields(const FieldConst<R>& F, const R* x, R& kappa, R& f) {
 
 // last geometry stage at quadrature point `item` of patch D: physical point x and Jacobian J
 // (J[m][k] = d x_m / d xi_k) from the stage-1/2 partial contractions
+// the Gauss-point indices of quadrature point `item` of patch D (32-bit divisions where the patch's
+// point count allows: 64-bit ones cost several times more)
+GS_HD void pointIndex(const DevPatch& D, long long item, int& g0, int& g1, int& g2) {
+    const int Q0 = D.Q[0], Q1 = D.Q[1];
+    if (D.nq < (1LL << 31)) {
+        const unsigned it = unsigned(item), r = it / unsigned(Q0);
+        g0 = int(it - r * unsigned(Q0));
+        g1 = int(r % unsigned(Q1));
+        g2 = int(r / unsigned(Q1));
+    } else {
+        const long long r = item / Q0;
+        g0 = int(item - r * Q0);
+        g1 = int(r % Q1);
+        g2 = int(r / Q1);
+    }
+}
 template <typename R>
 GS_HD void pointMap(const DevPatch& D, long long item, const R* __restrict__ Y1, const R* __restrict__ Y2,
                     const R* __restrict__ gtab, const int* __restrict__ ibuf, R x[3], R J[3][3]) {
     const int d = D.dim;
     const int Q0 = D.Q[0], Q1 = D.Q[1];
-    const int g0 = int(item % Q0);
-    long long r = item / Q0;
-    const int g1 = int(r % Q1);
-    const int g2 = int(r / Q1);
+    int g0, g1, g2;
+    pointIndex(D, item, g0, g1, g2);
     if (d == 3) {
         const int gp = D.gp[2];
         const int f2 = ibuf[D.gqoff[2] + g2];
@@ -375,11 +393,8 @@ GS_HD double pointStep(const DevPatch& D, const FieldConst<R>& F, long long item
                        const R* __restrict__ Y2, const R* __restrict__ gtab, const int* __restrict__ ibuf,
                        const R* __restrict__ wq, R* __restrict__ C, R* __restrict__ Lf) {
     const int d = D.dim;
-    const int Q0 = D.Q[0], Q1 = D.Q[1];
-    const int g0 = int(item % Q0);
-    long long r = item / Q0;
-    const int g1 = int(r % Q1);
-    const int g2 = int(r / Q1);
+    int g0, g1, g2;
+    pointIndex(D, item, g0, g1, g2);
     R x[3], J[3][3];
     pointMap<R>(D, item, Y1, Y2, gtab, ibuf, x, J);
     R w = wq[D.qoff[0] + g0] * wq[D.qoff[1] + g1];

@@ -43,7 +43,8 @@ __global__ void __launch_bounds__(kBlock) k_geo1(const DevPatch* __restrict__ P,
     const long long work = D.dim == 3 ? (long long)D.dim * 2 * D.gn[2] * D.gn[1] * D.Q[0]
                                       : (long long)D.dim * 2 * D.gn[1] * D.Q[0];
     if (item >= work) return;
-    Y1[D.y1_off + item] = dev::geoStage1<R>(D, item, coefs, gtab, ibuf);
+    Y1[D.y1_off + item] = work < (1LL << 31) ? dev::geoStage1<R, unsigned>(D, item, coefs, gtab, ibuf)
+                                             : dev::geoStage1<R>(D, item, coefs, gtab, ibuf);
 }
 
 template <typename R>
@@ -55,7 +56,8 @@ __global__ void __launch_bounds__(kBlock) k_geo2(const DevPatch* __restrict__ P,
     const long long item = be.base + threadIdx.x;
     const long long work = (long long)D.dim * 3 * D.gn[2] * D.Q[1] * D.Q[0];
     if (item >= work) return;
-    Y2[D.y2_off + item] = dev::geoStage2<R>(D, item, Y1, gtab, ibuf);
+    Y2[D.y2_off + item] = work < (1LL << 31) ? dev::geoStage2<R, unsigned>(D, item, Y1, gtab, ibuf)
+                                             : dev::geoStage2<R>(D, item, Y1, gtab, ibuf);
 }
 
 __device__ __forceinline__ unsigned long long detKey(double v) {
