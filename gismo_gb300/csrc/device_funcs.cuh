@@ -24,6 +24,16 @@ constexpr int kMaxKappaWave = 8;  // largest |k_m,i| of a Fourier mode supported
 // -------------------------------------------------------------------------------------------
 // K1: values and first derivatives of the p+1 B-splines of span s at u (Cox-de Boor triangle;
 // derivatives from the degree p-1 values). out[0..p] values, out[p+1..2p+1] derivatives.
+// The triangle's roundings are fixed (a product that feeds a later sum is rounded on its own, the
+// other one fused: bMul / fma), so that the one-lane form here and the warp-cooperative kernel,
+// which computes the same expressions in another order of statements, give the same bits.
+GS_HD double bMul(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __dmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
 GS_HD void basis1d(const double* __restrict__ t, int p, int s, double u, double* __restrict__ out) {
     double N[16], Nm1[16];
     N[0] = 1.0;
@@ -35,8 +45,8 @@ GS_HD void basis1d(const double* __restrict__ t, int p, int s, double u, double*
         for (int r = 0; r < k; ++r) {
             const double tr = t[s + 1 + r], tl = t[s + 1 + r - k];
             const double tmp = N[r] / (tr - tl);
-            N[r] = saved + (tr - u) * tmp;
-            saved = (u - tl) * tmp;
+            N[r] = fma(tr - u, tmp, saved);
+            saved = bMul(u - tl, tmp);
         }
         N[k] = saved;
     }
@@ -44,8 +54,8 @@ GS_HD void basis1d(const double* __restrict__ t, int p, int s, double u, double*
     for (int r = 0; r <= p; ++r) {
         out[r] = N[r];
         double d = 0.0;
-        if (r >= 1) d += p * Nm1[r - 1] / (t[a + r + p] - t[a + r]);
-        if (r <= p - 1) d -= p * Nm1[r] / (t[a + r + p + 1] - t[a + r + 1]);
+        if (r >= 1) d += bMul(double(p), Nm1[r - 1]) / (t[a + r + p] - t[a + r]);
+        if (r <= p - 1) d -= bMul(double(p), Nm1[r]) / (t[a + r + p + 1] - t[a + r + 1]);
         out[p + 1 + r] = d;
     }
 }

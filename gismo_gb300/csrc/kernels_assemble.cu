@@ -23,6 +23,65 @@ __global__ void __launch_bounds__(kBlock) k_basis(const TabJob* __restrict__ job
     for (int r = 0; r < 2 * (j.p + 1); ++r) out[j.out + r] = buf[r];
 }
 
+// K1, warp-cooperative: the Cox-de Boor triangle of each abscissa by a group of kBasisGroup
+// lanes, lane r holding N_r; level k forms N_0..N_k from the lane's own N_r and its neighbour's
+// quotient N_{r-1} / (t_{r-1+s+1} - t_{..}) (a shuffle), so the triangle takes p steps of one
+// division each instead of p(p+1)/2 on one lane, in registers (one lane per abscissa keeps the
+// triangle in a local array). Every value is the same expression, with the same roundings fixed
+// (dev::bMul, fma), as in basis1d: the same bits.
+// Degrees above kBasisGroup - 1 (wider than the group) take basis1d on the group's first lane.
+constexpr int kBasisGroup = 8;
+__global__ void __launch_bounds__(kBlock) k_basis_warp(const TabJob* __restrict__ jobs, long long njobs,
+                                                       const double* __restrict__ knots, double* __restrict__ out) {
+    const long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / kBasisGroup;
+    const int r = int(threadIdx.x % kBasisGroup);
+    const bool valid = g < njobs;
+    TabJob j{};
+    if (valid) j = jobs[g];
+    const int p = j.p;
+    const int pw = p < kBasisGroup ? p : 0;  // the degree the group's shuffle triangle handles
+    const double* t = knots + j.koff;
+    const int s = j.span;
+    const double u = j.u;
+    double N = r == 0 ? 1.0 : 0.0, Nm1 = 0.0;
+    for (int k = 1; k < kBasisGroup; ++k) {  // uniform trip count: every lane takes part in the shuffles
+        const bool act = valid && k <= pw;
+        if (act && k == pw) Nm1 = N;  // the degree p-1 values, for the derivatives
+        double tmp = 0.0, tr = 0.0;
+        if (act && r < k) {
+            tr = t[s + 1 + r];
+            tmp = N / (tr - t[s + 1 + r - k]);
+        }
+        const double prev = __shfl_up_sync(0xffffffffu, tmp, 1, kBasisGroup);
+        if (act && r <= k) {
+            const double saved = r >= 1 ? dev::bMul(u - t[s + r - k], prev) : 0.0;
+            N = r < k ? fma(tr - u, tmp, saved) : saved;
+        }
+    }
+    const double prevNm1 = __shfl_up_sync(0xffffffffu, Nm1, 1, kBasisGroup);
+    if (!valid) return;
+    if (p >= kBasisGroup) {
+        if (r == 0) {
+            double buf[32];
+            dev::basis1d(knots + j.koff, j.p, j.span, j.u, buf);
+            for (int q = 0; q < 2 * (j.p + 1); ++q) out[j.out + q] = buf[q];
+        }
+        return;
+    }
+    if (r > p) return;
+    if (p == 0) {
+        out[j.out] = 1.0;
+        out[j.out + 1] = 0.0;
+        return;
+    }
+    const int a = s - p;
+    double d = 0.0;
+    if (r >= 1) d += dev::bMul(double(p), prevNm1) / (t[a + r + p] - t[a + r]);
+    if (r <= p - 1) d -= dev::bMul(double(p), Nm1) / (t[a + r + p + 1] - t[a + r + 1]);
+    out[j.out + r] = N;
+    out[j.out + p + 1 + r] = d;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kBlock) k_pair(const PfJob* __restrict__ jobs, const BlkEnt* __restrict__ tab,
                                                  const double* __restrict__ basis, T* __restrict__ pf) {
@@ -508,7 +567,12 @@ inline unsigned grid1(long long n) { return unsigned((n + kBlock - 1) / kBlock);
 namespace launch {
 
 void basisTables(const TabJob* jobs, long long njobs, const double* knots, double* out, cudaStream_t s) {
-    if (njobs > 0) k_basis<<<grid1(njobs), kBlock, 0, s>>>(jobs, njobs, knots, out);
+    if (njobs <= 0) return;
+    if (std::getenv("GSGPU_BASIS_LANE")) {  // one lane per abscissa (the same values)
+        k_basis<<<grid1(njobs), kBlock, 0, s>>>(jobs, njobs, knots, out);
+        return;
+    }
+    k_basis_warp<<<grid1(njobs * kBasisGroup), kBlock, 0, s>>>(jobs, njobs, knots, out);
 }
 template <typename T>
 void pairFactors(const PfJob* jobs, const BlkEnt* tab, long long nblk, const double* basis, T* pf, cudaStream_t s) {

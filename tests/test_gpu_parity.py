@@ -257,3 +257,26 @@ def test_mass_matrix_matches_oracle_at_size():
         mo = o.mass()
         assert np.abs(m - mo).max() <= REL * np.abs(mo).max()
         A.close()
+
+
+@pytest.mark.parametrize("case", ["square_p2_64", "disp2d_p4_40x33", "volume_p3_12", "disp3d_p232_5x6x7"])
+def test_warp_basis_tables_are_bitwise_neutral(case, monkeypatch):
+    """The warp-cooperative basis kernel (a lane group per abscissa, shuffles between the lanes of
+    the Cox-de Boor triangle) gives the FP64 operator and rhs of the one-lane-per-abscissa kernel
+    (GSGPU_BASIS_LANE=1) bit for bit: degrees 2 to 4, 2D and 3D, mixed degrees per direction."""
+    make = {"square_p2_64": lambda: P.square_poisson(64, 2),
+            "disp2d_p4_40x33": lambda: P.displaced_single_patch(2, (40, 33), (4, 4), 9, 0.05, ufreq=3),
+            "volume_p3_12": lambda: P.volume_poisson(12, 3, seed=4),
+            "disp3d_p232_5x6x7": lambda: P.displaced_single_patch(3, (5, 6, 7), (2, 3, 2), 8, 0.04)}[case]
+    prob = make()
+    out = []
+    for lane in (False, True):
+        if lane:
+            monkeypatch.setenv("GSGPU_BASIS_LANE", "1")
+        else:
+            monkeypatch.delenv("GSGPU_BASIS_LANE", raising=False)
+        A = _assembler(prob)
+        A.assemble("fp64")
+        out.append((A.csr()[2], A.rhs()))
+        A.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
