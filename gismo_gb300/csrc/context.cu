@@ -1026,6 +1026,9 @@ void Context::solveMixed(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
     {
         auto a16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
         B.vec4 = a16(dDx32) && a16(dR32) && a16(dZ32) && a16(dP32) && a16(dT32) && a16(dDinv32);
+        // programmatic dependent launch of the half-diagonal iteration kernels (GSGPU_NO_PDL=1 off)
+        B.pdl = B.vec4 && B.sdia.d && B.sdia.group == 4 && !std::getenv("GSGPU_NO_PDL");
+        B.sdia.pdl = B.pdl;
     }
     const double tol = o.tol > 0 ? o.tol : 1e-10;
     const int maxit = o.max_iters > 0 ? o.max_iters : 1000;

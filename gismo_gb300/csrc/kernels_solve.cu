@@ -10,6 +10,7 @@
 
 #include "df32.cuh"
 #include "kernels_solve.h"
+#include "pdl.cuh"
 #include "spmv_row.cuh"
 
 namespace gsgpu {
@@ -315,6 +316,8 @@ __global__ void __launch_bounds__(kB, kSpmv32BlocksPerSm) k_spmv32_dot(int n, co
 }
 
 __global__ void __launch_bounds__(kB) k_alpha_m(int nparts, const double* __restrict__ part, CgState* __restrict__ st) {
+    pdlWait();
+    pdlTrigger();
     if (st->done || st->pause) return;
     const double pAp = reducePartials(part, nparts);
     if (threadIdx.x == 0) st->alpha = st->rho / pAp;
@@ -387,6 +390,7 @@ __global__ void __launch_bounds__(kB) k_update32b4(int n, float* __restrict__ dx
                                                    const float* __restrict__ t, const float* __restrict__ dinv,
                                                    double* __restrict__ prr, double* __restrict__ prz,
                                                    CgState* __restrict__ st) {
+    pdlWait();
     if (st->done || st->pause) {
         if (blockIdx.x == 0 && threadIdx.x == 0) st->pupd_skip = 1;
         return;
@@ -419,6 +423,7 @@ __global__ void __launch_bounds__(kB) k_update32b4(int n, float* __restrict__ dx
             one(dx[i], r[i], zi, p[i], t[i], dinv[i]);
             z[i] = zi;
         }
+    pdlTrigger();
     blockSumStoreF2(rr, rz, prr, prz);
     if (!lastBlock(&st->arrive)) return;
     const double rrs = reducePartialsLast(prr, gridDim.x);
@@ -437,6 +442,8 @@ __global__ void __launch_bounds__(kB) k_update32b4(int n, float* __restrict__ dx
 // p = z + beta p over four entries per thread (the tail by thread 0), as k_pupd32
 __global__ void __launch_bounds__(kB) k_pupd32_4(int n, float* __restrict__ p, const float* __restrict__ z,
                                                  const CgState* __restrict__ st) {
+    pdlWait();
+    pdlTrigger();
     if (st->done || st->pupd_skip) return;
     const float beta = float(st->beta);
     const int n4 = n >> 2;
@@ -744,12 +751,12 @@ void mixedRest(const CgBuffers& B, cudaStream_t s) {
     const int nb = mixedSpmvPartials(B);
     if (B.sdia.d) {  // beta from the update's last block (measured: -3 us per iteration on the C2 volume;
                      // alpha from the product's last block measured +15 us and stays a kernel)
-        k_alpha_m<<<1, kB, 0, s>>>(nb, B.part2, B.st);
+        launchMaybePdl(k_alpha_m, dim3(1), dim3(kB), s, B.pdl && B.vec4, nb, B.part2, B.st);
         if (B.vec4) {  // 16-byte aligned vectors: four entries per thread
             const int np4 = std::max(1, (B.n / 4 + kB - 1) / kB);
-            k_update32b4<<<np4, kB, 0, s>>>(B.n, B.dx32, B.r32, B.z32, B.p32, B.t32, B.dinv32, B.part0, B.part1,
-                                            B.st);
-            k_pupd32_4<<<np4, kB, 0, s>>>(B.n, B.p32, B.z32, B.st);
+            launchMaybePdl(k_update32b4, dim3(np4), dim3(kB), s, B.pdl, B.n, B.dx32, B.r32, B.z32, B.p32, B.t32,
+                           B.dinv32, B.part0, B.part1, B.st);
+            launchMaybePdl(k_pupd32_4, dim3(np4), dim3(kB), s, B.pdl, B.n, B.p32, B.z32, B.st);
             return;
         }
         k_update32b<<<np, kB, 0, s>>>(B.n, B.dx32, B.r32, B.z32, B.p32, B.t32, B.dinv32, B.part0, B.part1, B.st);

@@ -34,6 +34,7 @@ struct SdiaOp {
     int p[3] = {0, 0, 0};
     int xpad = 0;  // zeros the vector x of the product carries before and after its n entries
     int group = 1;  // rows per thread of the load-based product: 1 (scalar loads) or 4 (16-byte loads)
+    bool pdl = false;  // launch the four-row product with programmatic dependent launch (pdl.cuh)
     // if set: host copies of the two tensor maps (the diagonals, the vector x) of the TMA-fed product,
     // and the device word its bounded waits set when they expire
     const void* tmaps = nullptr;
@@ -75,6 +76,7 @@ struct CgBuffers {
     // if sdia.d is set, the inner FP32 products use the half-diagonal form instead of the CSR hi values
     SdiaOp sdia;
     bool vec4 = false;  // the FP32 vectors are 16-byte aligned: the half-diagonal path's vector kernels take four entries a thread
+    bool pdl = false;   // the half-diagonal path's iteration kernels use programmatic dependent launch
 };
 
 struct df32;

@@ -25,6 +25,7 @@
 #include "context.h"
 #include "df32.cuh"
 #include "kernels_solve.h"
+#include "pdl.cuh"
 
 namespace gsgpu {
 namespace {
@@ -229,6 +230,7 @@ template <int P0>
 __global__ void __launch_bounds__(kBG, kG4BlocksPerSm) k_sdia32_g4(SdiaOp A, const float* __restrict__ x,
                                                                    float* __restrict__ t, double* __restrict__ part,
                                                                    const CgState* __restrict__ st) {
+    pdlWait();
     if (st->done || st->pause) return;
     constexpr int W0 = 2 * P0 + 1;
     constexpr int kAhead = kG4Ahead;
@@ -296,6 +298,7 @@ __global__ void __launch_bounds__(kBG, kG4BlocksPerSm) k_sdia32_g4(SdiaOp A, con
             }
         }
     }
+    pdlTrigger();
     __shared__ double ws[kBG / 32];
     contrib = warpSumD(contrib);
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = contrib;
@@ -602,10 +605,10 @@ void sdiaSpmv(const SdiaOp& A, const float* x, float* t, double* part, const CgS
     const int nb = sdiaPartials(A);
     if (A.group == kG) {
         switch (A.p[0]) {
-            case 1: k_sdia32_g4<1><<<nb, kBG, 0, s>>>(A, x, t, part, st); break;
-            case 2: k_sdia32_g4<2><<<nb, kBG, 0, s>>>(A, x, t, part, st); break;
-            case 3: k_sdia32_g4<3><<<nb, kBG, 0, s>>>(A, x, t, part, st); break;
-            default: k_sdia32_g4<4><<<nb, kBG, 0, s>>>(A, x, t, part, st); break;
+            case 1: launchMaybePdl(k_sdia32_g4<1>, dim3(nb), dim3(kBG), s, A.pdl, A, x, t, part, st); break;
+            case 2: launchMaybePdl(k_sdia32_g4<2>, dim3(nb), dim3(kBG), s, A.pdl, A, x, t, part, st); break;
+            case 3: launchMaybePdl(k_sdia32_g4<3>, dim3(nb), dim3(kBG), s, A.pdl, A, x, t, part, st); break;
+            default: launchMaybePdl(k_sdia32_g4<4>, dim3(nb), dim3(kBG), s, A.pdl, A, x, t, part, st); break;
         }
         return;
     }

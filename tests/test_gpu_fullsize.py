@@ -133,7 +133,10 @@ def test_batch_full_range_matches_oracle():
     its = info["per_problem"]["iterations"]
     for j, pr in enumerate(batch):
         o = O.OracleProblem(pr)
-        o.assemble()
+        # one thread: the oracle's scatter order, and so the last digits of its matrix and its CG
+        # iteration count, do not depend on the host's thread count and scheduling (on 16 threads
+        # a 172-iteration problem took 172-174 iterations from run to run)
+        o.assemble(1)
         optr, ocol, oval = o.csr()
         a, b = off[j], off[j + 1]
         k0, k1 = ptr[a], ptr[b]
