@@ -75,16 +75,21 @@ def run_batch(args, sampler):
         return time.perf_counter() - t0, xs, info
 
     out = {}
+    split = {}
     for prec, mtol in (("fp64", tol), ("mixed", tol)):
         for _ in range(args.warmup):
             step(prec, mtol)
         clk = sampler()
         clk.start()
         ts = []
+        asm, sol = [], []
         for _ in range(args.steps):
             t, xs, info = step(prec, mtol)
             ts.append(t)
+            asm.append(float(B.assemble_times()[6]))
+            sol.append(float(info["t_solve_ms"]))
         clocks = clk.stop()
+        split[prec] = {"assemble_ms": float(np.median(asm)), "solve_ms": float(np.median(sol))}
         x = np.concatenate(xs)
         out[prec] = dict(ms=float(np.median(ts)) * 1e3, info=info, clocks=clocks,
                          err=float(np.linalg.norm(x - xref) / np.linalg.norm(xref)))
@@ -101,7 +106,7 @@ def run_batch(args, sampler):
         "rel_err_vs_fp64": {"mixed": out["mixed"]["err"], "fp64_at_tol": out["fp64"]["err"],
                             "reference": "FP64 GPU batch solved to 1e-12"},
         "iterations_mixed_inner": {"max": int(its.max()), "mean": float(its.mean())},
-        "clocks": out["mixed"]["clocks"]})
+        "device_ms": split, "clocks": out["mixed"]["clocks"]})
     B.close()
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = _cpu_batch(probs)

@@ -223,6 +223,7 @@ struct Context {
     int *dSegRow = nullptr, *dRowSeg = nullptr, *dSegDone = nullptr;
     double *dSegRc0 = nullptr, *dSegRc1 = nullptr;
     SegState *dSegSt = nullptr, *dSegOuter = nullptr;
+    df32* dSegXdf = nullptr;  // the double-float split of the batch solution (mixed residuals)
     cudaGraphExec_t gexecSeg[2] = {nullptr, nullptr};
     std::vector<SegState> segLast;
     void batchSetup();

@@ -6,6 +6,7 @@
 // dot products are per-row contributions summed per segment by one warp in a fixed order, so
 // the results do not depend on the launch shape.
 #include "context.h"
+#include "df32.cuh"
 #include "kernels_batch.h"
 #include "spmv_row.cuh"
 
@@ -189,15 +190,22 @@ __global__ void __launch_bounds__(kB) k_ref_resid(SegCg<float> B, SegRefine R, i
         // the first residual on every running segment, later ones on the segments whose FP32
         // recursion is waiting for its replacement
         const bool act = row < B.n && rowActive(B.rowSeg, R.st, row) && (first || B.st[B.rowSeg[row]].pause);
-        double acc = 0.0;
+        // (hi + lo) x in double-float arithmetic on the FP32 pipe (x as its df32 split, compensated
+        // accumulation per lane, the lanes' sums added in df32), as the single-system residual
+        // replacement does: FP64 products here ran on GB300's FP64 pipe at a fraction of the rate
+        Dot2 acc;
         if (act)
             dev::rowMac<kLanes, kUnroll, REL>(
                 row, B.ptr[row], B.ptr[row + 1], lane, B.col, B.coff,
-                [&](int k) { return double(R.hi[k]) + double(R.lo[k]); }, [&](int c) { return R.x[c]; },
-                [&](double v, double x) { acc += v * x; });
-        for (int o = kLanes / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                [&](int k) { return df32(R.hi[k], R.lo[k]); }, [&](int c) { return R.xdf[c]; },
+                [&](df32 v, df32 x) { acc.mac(v, x); });
+        df32 y = acc.result();
+        for (int o = kLanes / 2; o > 0; o >>= 1) {
+            const df32 oth(__shfl_xor_sync(0xffffffffu, y.hi, o), __shfl_xor_sync(0xffffffffu, y.lo, o));
+            y = y + oth;
+        }
         if (act && lane == 0) {
-            const double ri = R.b[row] - acc;
+            const double ri = R.b[row] - y.toDouble();
             R.r[row] = ri;
             B.rc0[row] = ri * ri;
         }
@@ -236,7 +244,9 @@ __global__ void __launch_bounds__(kB) k_ref_rhs(SegCg<float> B, SegRefine R) {
 __global__ void __launch_bounds__(kB) k_ref_absorb(SegCg<float> B, SegRefine R) {
     for (int i = blockIdx.x * kB + threadIdx.x; i < B.n; i += gridDim.x * kB)
         if (rowActive(B.rowSeg, R.st, i)) {
-            R.x[i] += double(B.x[i]);
+            const double xi = R.x[i] + double(B.x[i]);
+            R.x[i] = xi;
+            R.xdf[i] = df32(xi);
             B.x[i] = 0.f;
         }
 }
@@ -322,6 +332,7 @@ void segIteration(const SegCg<T>& B, cudaStream_t s) {
 void refineResidual(const SegCg<float>& B, const SegRefine& R, double tol, int maxref, int first, cudaStream_t s) {
     if (first) {
         GSGPU_CUDA_TRY(cudaMemsetAsync(R.x, 0, sizeof(double) * size_t(B.n), s));
+        GSGPU_CUDA_TRY(cudaMemsetAsync(R.xdf, 0, sizeof(df32) * size_t(B.n), s));
         GSGPU_CUDA_TRY(cudaMemsetAsync(R.st, 0, sizeof(SegState) * size_t(B.nseg), s));
         GSGPU_CUDA_TRY(cudaMemsetAsync(R.ndone, 0, sizeof(int), s));
     }

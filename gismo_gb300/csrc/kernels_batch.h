@@ -41,11 +41,14 @@ struct SegCg {
 };
 
 // iterative refinement: FP64 residual with the split operator hi + lo and FP64 x
+struct df32;
+
 struct SegRefine {
     const float* hi = nullptr;
     const float* lo = nullptr;
     const double* b = nullptr;
     double* x = nullptr;         // FP64 solution
+    df32* xdf = nullptr;         // its double-float split, kept with x (the residual's right factor)
     double* r = nullptr;         // FP64 residual
     float* r32 = nullptr;        // FP32 copy of the first residual (the recursion's right-hand side)
     SegState* st = nullptr;      // outer state: relres of b - A x, residual replacements in iters

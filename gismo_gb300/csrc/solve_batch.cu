@@ -46,6 +46,7 @@ void Context::batchSetup() {
     allocN(arena, dSegSt, nseg);
     allocN(arena, dSegOuter, nseg);
     allocN(arena, dSegDone, 2);  // [inner done, outer done]
+    allocN(arena, dSegXdf, std::max(1, pat.n));
 }
 
 // one chunk of 16 iterations as a captured graph (per precision, once per context)
@@ -146,6 +147,7 @@ void Context::solveBatch(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
         R.lo = dValLo;
         R.b = dRhs;
         R.x = dX;
+        R.xdf = dSegXdf;
         R.r = dR;
         R.r32 = dXhi;
         R.st = dSegOuter;
