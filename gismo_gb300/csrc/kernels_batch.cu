@@ -36,6 +36,23 @@ __device__ __forceinline__ double warpRange(const double* __restrict__ part, int
     return warpSum(v);
 }
 
+// the same sum by the kSegB threads of one block (fixed order: thread-strided partials, then the
+// warps' sums in warp order); every thread returns it. One block per segment: the largest segments
+// of a batch (tens of thousands of rows) no longer serialise hundreds of dependent loads on one warp
+constexpr int kSegB = 128;
+__device__ __forceinline__ double blockRange(const double* __restrict__ part, int a, int b) {
+    __shared__ double ws[kSegB / 32];
+    double v = 0.0;
+    for (int i = a + int(threadIdx.x); i < b; i += kSegB) v += part[i];
+    v = warpSum(v);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double sum = 0.0;
+    for (int w = 0; w < kSegB / 32; ++w) sum += ws[w];
+    __syncthreads();
+    return sum;
+}
+
 __device__ __forceinline__ bool rowActive(const int* __restrict__ rowSeg, const SegState* __restrict__ st, int row) {
     const SegState& S = st[rowSeg[row]];
     return !S.done && !S.pause;
@@ -114,17 +131,19 @@ __global__ void __launch_bounds__(kB) k_seg_spmv(SegCg<T> B) {
     }
 }
 
+// one block per segment
 template <typename T>
-__global__ void __launch_bounds__(kB) k_seg_alpha(SegCg<T> B) {
-    const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (s >= B.nseg || B.st[s].done) return;
-    if (B.st[s].pause) {  // idle until the replacement; the pausing iteration's p update has run
-        if (lane == 0) B.st[s].pause = 2;
+__global__ void __launch_bounds__(kSegB) k_seg_alpha(SegCg<T> B) {
+    const int s = blockIdx.x;
+    const int done = B.st[s].done, pause = B.st[s].pause;
+    __syncthreads();  // every thread has read the flags before thread 0 may change them
+    if (done) return;
+    if (pause) {  // idle until the replacement; the pausing iteration's p update has run
+        if (threadIdx.x == 0) B.st[s].pause = 2;
         return;
     }
-    const double pAp = warpRange(B.rc0, B.segRow[s], B.segRow[s + 1], lane);
-    if (lane == 0) B.st[s].alpha = B.st[s].rho / pAp;
+    const double pAp = blockRange(B.rc0, B.segRow[s], B.segRow[s + 1]);
+    if (threadIdx.x == 0) B.st[s].alpha = B.st[s].rho / pAp;
 }
 
 // x += alpha p; r -= alpha t; z = D^-1 r; rc0 = r .* r, rc1 = r .* z
@@ -144,14 +163,14 @@ __global__ void __launch_bounds__(kB) k_seg_update(SegCg<T> B) {
     }
 }
 
+// one block per segment
 template <typename T>
-__global__ void __launch_bounds__(kB) k_seg_scalars(SegCg<T> B) {
-    const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (s >= B.nseg || B.st[s].done || B.st[s].pause) return;
-    const double rr = warpRange(B.rc0, B.segRow[s], B.segRow[s + 1], lane);
-    const double rz = warpRange(B.rc1, B.segRow[s], B.segRow[s + 1], lane);
-    if (lane == 0) {
+__global__ void __launch_bounds__(kSegB) k_seg_scalars(SegCg<T> B) {
+    const int s = blockIdx.x;
+    if (B.st[s].done || B.st[s].pause) return;  // thread 0 changes them only after both sums
+    const double rr = blockRange(B.rc0, B.segRow[s], B.segRow[s + 1]);
+    const double rz = blockRange(B.rc1, B.segRow[s], B.segRow[s + 1]);
+    if (threadIdx.x == 0) {
         SegState& S = B.st[s];
         S.iters += 1;
         S.relres = sqrt(rr) / S.bnorm;
@@ -323,9 +342,9 @@ void segIteration(const SegCg<T>& B, cudaStream_t s) {
     const int gs = gridFor(B.n, kB / kLanes);
     if (B.coff) k_seg_spmv<T, true><<<gs, kB, 0, s>>>(B);
     else k_seg_spmv<T, false><<<gs, kB, 0, s>>>(B);
-    k_seg_alpha<T><<<segGrid(B.nseg), kB, 0, s>>>(B);
+    k_seg_alpha<T><<<unsigned(B.nseg > 0 ? B.nseg : 1), kSegB, 0, s>>>(B);
     k_seg_update<T><<<gridFor(B.n, kB), kB, 0, s>>>(B);
-    k_seg_scalars<T><<<segGrid(B.nseg), kB, 0, s>>>(B);
+    k_seg_scalars<T><<<unsigned(B.nseg > 0 ? B.nseg : 1), kSegB, 0, s>>>(B);
     k_seg_pupd<T><<<gridFor(B.n, kB), kB, 0, s>>>(B);
 }
 
