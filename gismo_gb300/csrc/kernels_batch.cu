@@ -231,12 +231,12 @@ __global__ void __launch_bounds__(kB) k_ref_resid(SegCg<float> B, SegRefine R, i
     }
 }
 
-__global__ void __launch_bounds__(kB) k_ref_seg(SegCg<float> B, SegRefine R, double tol, int maxref, int first) {
-    const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (s >= B.nseg || R.st[s].done || (!first && !B.st[s].pause)) return;
-    const double rr = warpRange(B.rc0, B.segRow[s], B.segRow[s + 1], lane);
-    if (lane == 0) {
+// one block per segment
+__global__ void __launch_bounds__(kSegB) k_ref_seg(SegCg<float> B, SegRefine R, double tol, int maxref, int first) {
+    const int s = blockIdx.x;
+    if (R.st[s].done || (!first && !B.st[s].pause)) return;  // changed by thread 0 only after the sum
+    const double rr = blockRange(B.rc0, B.segRow[s], B.segRow[s + 1]);
+    if (threadIdx.x == 0) {
         SegState& S = R.st[s];
         if (first) {
             S.bnorm = sqrt(rr);
@@ -288,20 +288,22 @@ __global__ void __launch_bounds__(kB) k_ref_replace(SegCg<float> B, SegRefine R)
 
 // per segment: a segment the true residual has finished leaves the recursion; a paused one
 // resumes with rho of the replaced residual (or ends at its iteration limit)
-__global__ void __launch_bounds__(kB) k_ref_replace_seg(SegCg<float> B, SegRefine R) {
-    const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (s >= B.nseg || B.st[s].done) return;
-    if (R.st[s].done) {
-        if (lane == 0) {
-            B.st[s].done = R.st[s].done;
+// one block per segment
+__global__ void __launch_bounds__(kSegB) k_ref_replace_seg(SegCg<float> B, SegRefine R) {
+    const int s = blockIdx.x;
+    const int innerDone = B.st[s].done, outerDone = R.st[s].done, pause = B.st[s].pause;
+    __syncthreads();  // every thread has read the flags before thread 0 may change them
+    if (innerDone) return;
+    if (outerDone) {
+        if (threadIdx.x == 0) {
+            B.st[s].done = outerDone;
             atomicAdd(B.ndone, 1);
         }
         return;
     }
-    if (!B.st[s].pause) return;
-    const double rz = warpRange(B.rc1, B.segRow[s], B.segRow[s + 1], lane);
-    if (lane == 0) {
+    if (!pause) return;
+    const double rz = blockRange(B.rc1, B.segRow[s], B.segRow[s + 1]);
+    if (threadIdx.x == 0) {
         SegState& S = B.st[s];
         if (S.iters >= S.maxit) {
             S.done = 2;
@@ -358,7 +360,7 @@ void refineResidual(const SegCg<float>& B, const SegRefine& R, double tol, int m
     const int gs = gridFor(B.n, kB / kLanes);
     if (B.coff) k_ref_resid<true><<<gs, kB, 0, s>>>(B, R, first);
     else k_ref_resid<false><<<gs, kB, 0, s>>>(B, R, first);
-    k_ref_seg<<<segGrid(B.nseg), kB, 0, s>>>(B, R, tol, maxref, first);
+    k_ref_seg<<<unsigned(B.nseg > 0 ? B.nseg : 1), kSegB, 0, s>>>(B, R, tol, maxref, first);
 }
 
 void refineRhs(const SegCg<float>& B, const SegRefine& R, cudaStream_t s) {
@@ -369,7 +371,7 @@ void refineReplace(const SegCg<float>& B, const SegRefine& R, double tol, int ma
     k_ref_absorb<<<gridFor(B.n, kB), kB, 0, s>>>(B, R);
     refineResidual(B, R, tol, maxref, 0, s);
     k_ref_replace<<<gridFor(B.n, kB), kB, 0, s>>>(B, R);
-    k_ref_replace_seg<<<segGrid(B.nseg), kB, 0, s>>>(B, R);
+    k_ref_replace_seg<<<unsigned(B.nseg > 0 ? B.nseg : 1), kSegB, 0, s>>>(B, R);
 }
 
 void refineCount(const SegCg<float>& B, const SegRefine& R, cudaStream_t s) {
