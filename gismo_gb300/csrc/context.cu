@@ -710,32 +710,82 @@ void Context::applyMatrix(const double* x, double* y) {
 
 // gsField::distanceL2 of the last solution: the geometry stages are re-run in FP64 (after a
 // mixed-precision assembly their buffers hold double-float values), then one quadrature kernel
+// gsField::distanceL2 / distanceH1 integrate with their evaluator's default rule, p + 1 Gauss points
+// per direction, whatever rule the assembler uses (gsNorm.h, the visitor's default quadrature).
+// With the default assembly rule (quA = 1, quB = 1) that is the assembly grid, whose tables and
+// geometry buffers are reused; otherwise the norm grid gets its own layout and temporary buffers.
 std::vector<double> Context::l2PerPatch(bool h1) {
     if (!solved) throw StateError("l2_error() before solve()");
     cudaStream_t s = stream;
-    // after a mixed assembly the geometry table holds double-float values: rebuild it in FP64
-    launch::basisTables(dGtabJobs, (long long)L.gtabjobs.size(), dGknots, dGtab, s);
-    launch::basisTables(dTabJobs, (long long)L.tabjobs.size(), dKnots, dTab, s);
-    launch::geoStage1<double>(dPatches, tabGeo1.d, (long long)tabGeo1.h.size(), dCoefs, dGtab, dIbuf, dY1, s);
-    if (pd.dim == 3)
-        launch::geoStage2<double>(dPatches, tabGeo2.d, (long long)tabGeo2.h.size(), dY1, dGtab, dIbuf, dY2, s);
+    const bool own = !(pd.quA == 1.0 && pd.quB == 1);
+    Layout Ln;
+    if (own) {
+        ProblemDesc pn = pd;
+        pn.quA = 1.0;
+        pn.quB = 1;
+        buildLayout(pn, Ln);
+    }
+    const Layout& N = own ? Ln : L;
+    // the norm grid's device data: the assembly's when the rules agree, else temporaries
+    DevPatch* dP = dPatches;
+    TabJob *dTJ = dTabJobs, *dGJ = dGtabJobs;
+    int* dIb = dIbuf;
+    double *dW = dWq, *dT = dTab, *dG = dGtab, *dYa = dY1, *dYb = dY2, *dKn = dKnots, *dGk = dGknots;
+    Tab tG1, tG2, tP;
+    const Tab *pG1 = &tabGeo1, *pG2 = &tabGeo2, *pP = &tabPoint;
+    if (own) {
+        dP = nullptr, dTJ = dGJ = nullptr, dIb = nullptr, dW = dT = dG = dYa = dYb = dKn = dGk = nullptr;
+        upload(arena, dP, N.dev, s);
+        upload(arena, dTJ, N.tabjobs, s);
+        upload(arena, dGJ, N.gtabjobs, s);
+        upload(arena, dIb, N.ibuf, s);
+        upload(arena, dW, N.wq, s);
+        upload(arena, dKn, N.knots, s);
+        upload(arena, dGk, N.gknots, s);
+        allocN(arena, dT, N.ntab);
+        allocN(arena, dG, N.ngtab);
+        allocN(arena, dYa, N.y1);
+        allocN(arena, dYb, std::max(1LL, N.y2));
+        auto mk = [&](Tab& T, auto workfn) {
+            std::vector<long long> w;
+            for (const DevPatch& D : N.dev) w.push_back(workfn(D));
+            blockTable(w, launch::kBlock, T.h);
+            upload(arena, T.d, T.h, s);
+        };
+        mk(tG1, [](const DevPatch& D) {
+            return D.dim == 3 ? (long long)D.dim * 2 * D.gn[2] * D.gn[1] * D.Q[0] : (long long)D.dim * 2 * D.gn[1] * D.Q[0];
+        });
+        mk(tG2, [](const DevPatch& D) { return D.dim == 3 ? (long long)D.dim * 3 * D.gn[2] * D.Q[1] * D.Q[0] : 0LL; });
+        mk(tP, [](const DevPatch& D) { return D.nq; });
+        pG1 = &tG1, pG2 = &tG2, pP = &tP;
+    }
+    // (after a mixed assembly the assembly's geometry table holds double-float values: rebuilt in FP64)
+    launch::basisTables(dGJ, (long long)N.gtabjobs.size(), dGk, dG, s);
+    launch::basisTables(dTJ, (long long)N.tabjobs.size(), dKn, dT, s);
+    launch::geoStage1<double>(dP, pG1->d, (long long)pG1->h.size(), dCoefs, dG, dIb, dYa, s);
+    if (pd.dim == 3) launch::geoStage2<double>(dP, pG2->d, (long long)pG2->h.size(), dYa, dG, dIb, dYb, s);
     const long long nlocal = (long long)map.index.size();
-    const long long nblk = (long long)tabPoint.h.size();
+    const long long nblk = (long long)pP->h.size();
     double* coef = nullptr;
     double* part = nullptr;
     allocN(arena, coef, nlocal);
     allocN(arena, part, nblk);
     launch::solutionCoefs(nlocal, dIndex, map.freeSize, dX, dDdof, coef, s);
-    launch::l2Partials(dPatches, tabPoint.d, nblk, dFields, dY1, dY2, dGtab, dIbuf, dWq, dTab, coef, part, h1, s);
+    launch::l2Partials(dP, pP->d, nblk, dFields, dYa, dYb, dG, dIb, dW, dT, coef, part, h1, s);
     std::vector<double> h(nblk);
     GSGPU_CUDA_TRY(cudaGetLastError());
     GSGPU_CUDA_TRY(cudaMemcpyAsync(h.data(), part, nblk * sizeof(double), cudaMemcpyDeviceToHost, s));
     GSGPU_CUDA_TRY(cudaStreamSynchronize(s));
     arena.release(coef);
     arena.release(part);
+    if (own) {
+        for (void* p : {(void*)dP, (void*)dTJ, (void*)dGJ, (void*)dIb, (void*)dW, (void*)dKn, (void*)dGk, (void*)dT,
+                        (void*)dG, (void*)dYa, (void*)dYb, (void*)tG1.d, (void*)tG2.d, (void*)tP.d})
+            arena.release(p);
+    }
     // per patch, in block order (the blocks of a patch are contiguous in the table)
     std::vector<double> acc(pd.patches.size(), 0.0);
-    for (long long b = 0; b < nblk; ++b) acc[size_t(tabPoint.h[size_t(b)].patch)] += h[size_t(b)];
+    for (long long b = 0; b < nblk; ++b) acc[size_t(pP->h[size_t(b)].patch)] += h[size_t(b)];
     return acc;
 }
 

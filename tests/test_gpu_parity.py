@@ -280,3 +280,33 @@ def test_warp_basis_tables_are_bitwise_neutral(case, monkeypatch):
         out.append((A.csr()[2], A.rhs()))
         A.close()
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("case", ["disp2d_quad_1.5_2", "disp3d_quad_2_0", "cubegrid_quad_1_2"])
+def test_error_norms_use_the_reference_rule(case):
+    """gsField::distanceL2 / distanceH1 integrate with p + 1 Gauss points per direction whatever the
+    assembler's quA, quB: with a non-default assembly rule the device norms take their own grid and
+    match the oracle's restatement of the reference's rule (reference_norms, pinned against the
+    reference itself) to 1e-9, not the assembly-rule norms."""
+    from oracle import oracle as O
+    if case == "disp2d_quad_1.5_2":
+        prob = P.displaced_single_patch(2, (9, 7), (3, 4), 31, 0.05, ufreq=2)
+        prob.quA, prob.quB = 1.5, 2
+    elif case == "disp3d_quad_2_0":
+        prob = P.displaced_single_patch(3, (5, 4, 6), (2, 2, 3), 33, 0.04)
+        prob.quA, prob.quB = 2.0, 0
+    else:
+        prob = P.cube_grid(n=2, n_elem=4, p=2, seed=35, kappa_modes=8)
+        prob.quA, prob.quB = 1.0, 2
+    A = _assembler(prob)
+    A.assemble("fp64")
+    x, info = A.solve(tol=1e-12, max_iters=5000)
+    assert info["converged"]
+    o = O.OracleProblem(prob)
+    o.assemble()
+    l2r, h1r = o.reference_norms(x)
+    assert abs(A.l2_error() - l2r) <= 1e-9 * l2r, (A.l2_error(), l2r, o.l2_error(x))
+    assert abs(A.h1_error() - h1r) <= 1e-9 * h1r, (A.h1_error(), h1r, o.h1_error(x))
+    # the assembly-rule norms differ (so the test checks the rule, not a coincidence)
+    assert abs(o.l2_error(x) - l2r) > 1e-9 * l2r
+    A.close()
