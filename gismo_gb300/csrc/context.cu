@@ -143,6 +143,7 @@ void Context::refresh() {
     }
     if (batch) segRow = segmentRows(pd, map);
     setupSdia();
+    setupSegSdia();
     applyTuning();
     if (device < 0) {  // host-only context: the plan, no device buffers
         refreshed = true;
@@ -343,38 +344,34 @@ void Context::findBoxRows() {
     nBoxRows = (long long)cnt;
 }
 
-// The half-diagonal FP32 inner operator applies when the problem is one patch (not a batch) with
-// simple knots along every axis and degrees 1..4, and its free dofs are one box of patch-local
-// functions numbered lexicographically, at least 2p + 1 wide along every axis. Checked on the dof
-// map itself; GSGPU_NO_SDIA=1 keeps the CSR form (the tests compare the two).
-void Context::setupSdia() {
-    sdiaOk = false;
-    sdiaOp = SdiaOp();
-    sdiaBand = SdiaBand();
-    if (batch || pd.patches.size() != 1 || std::getenv("GSGPU_NO_SDIA")) return;
-    const DevPatch& D = L.dev[0];
+// The half-diagonal FP32 inner operator applies to a patch with simple knots along every axis and
+// degrees 1..4 whose free dofs (global indices idx[0..ndofs) of its functions, free below freeSize)
+// are one box of m0 x m1 x m2 patch-local functions numbered lexicographically from row0, at least
+// 2p + 1 wide along every axis; lo is the box's lower corner. Checked on the dof map itself.
+static bool patchBox(const DevPatch& D, const int* idx, int freeSize, int row0, int m[3], int lo[3]) {
     const int dim = D.dim;
     for (int k = 0; k < dim; ++k)
-        if (!D.simple[k] || D.p[k] < 1 || D.p[k] > 4) return;
-    int lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1}, nd[3] = {1, 1, 1};
+        if (!D.simple[k] || D.p[k] < 1 || D.p[k] > 4) return false;
+    int hi[3] = {1, 1, 1}, nd[3] = {1, 1, 1};
+    for (int k = 0; k < 3; ++k) lo[k] = 0, m[k] = 1;
     for (int k = 0; k < dim; ++k) nd[k] = D.n[k], lo[k] = nd[k], hi[k] = -1;
-    const int* idx = map.index.data();
-    const int nfree = map.freeSize;
+    long long cnt = 0;
     for (int i2 = 0; i2 < nd[2]; ++i2)
         for (int i1 = 0; i1 < nd[1]; ++i1)
             for (int i0 = 0; i0 < nd[0]; ++i0)
-                if (idx[(size_t(i2) * nd[1] + i1) * nd[0] + i0] < nfree) {
+                if (idx[(size_t(i2) * nd[1] + i1) * nd[0] + i0] < freeSize) {
                     const int c[3] = {i0, i1, i2};
+                    ++cnt;
                     for (int k = 0; k < dim; ++k) lo[k] = std::min(lo[k], c[k]), hi[k] = std::max(hi[k], c[k] + 1);
                 }
-    int m[3] = {1, 1, 1};
+    if (cnt == 0) return false;
     long long nbox = 1;
     for (int k = 0; k < dim; ++k) {
         m[k] = hi[k] - lo[k];
-        if (m[k] < 2 * D.p[k] + 1) return;
+        if (m[k] < 2 * D.p[k] + 1) return false;
         nbox *= m[k];
     }
-    if (nbox != nfree) return;
+    if (nbox != cnt) return false;
     for (int i2 = 0; i2 < nd[2]; ++i2)
         for (int i1 = 0; i1 < nd[1]; ++i1)
             for (int i0 = 0; i0 < nd[0]; ++i0) {
@@ -382,11 +379,27 @@ void Context::setupSdia() {
                 bool in = true;
                 for (int k = 0; k < dim; ++k) in = in && c[k] >= lo[k] && c[k] < hi[k];
                 const int J = idx[(size_t(i2) * nd[1] + i1) * nd[0] + i0];
-                const long long want =
-                    in ? (long long)(c[0] - lo[0]) + (long long)m[0] * ((c[1] - lo[1]) + (long long)m[1] * (c[2] - lo[2]))
-                       : -1;
-                if (in ? J != want : J < nfree) return;
+                const long long want = in ? row0 + (long long)(c[0] - lo[0]) +
+                                                (long long)m[0] * ((c[1] - lo[1]) + (long long)m[1] * (c[2] - lo[2]))
+                                          : -1;
+                if (in ? J != want : J < freeSize) return false;
             }
+    return true;
+}
+
+// The single-patch form (sdia.cu) for a problem of one patch (not a batch); GSGPU_NO_SDIA=1 keeps
+// the CSR form (the tests compare the two).
+void Context::setupSdia() {
+    sdiaOk = false;
+    sdiaOp = SdiaOp();
+    sdiaBand = SdiaBand();
+    if (batch || pd.patches.size() != 1 || std::getenv("GSGPU_NO_SDIA")) return;
+    const DevPatch& D = L.dev[0];
+    const int dim = D.dim;
+    int m[3], lo[3];
+    if (!patchBox(D, map.index.data(), map.freeSize, 0, m, lo)) return;
+    const int nfree = map.freeSize;
+    if ((long long)m[0] * m[1] * m[2] != nfree) return;
     sdiaOp.n = nfree;
     for (int k = 0; k < 3; ++k) {
         sdiaOp.m[k] = m[k];
@@ -398,6 +411,52 @@ void Context::setupSdia() {
     sdiaOp.nh = launch::sdiaHalf(sdiaOp.p);
     sdiaOp.ns = (nfree + 255) / 256 * 256;
     sdiaOk = true;
+}
+
+// The batched form (kernels_batch.cu) for the problems of a batch that are such patches: per problem
+// its half diagonals, unpadded, one after the other (the other problems keep their CSR rows).
+// GSGPU_NO_SDIA=1 keeps the CSR form for all.
+void Context::setupSegSdia() {
+    segSdiaOk = false;
+    segSdiaHost.clear();
+    segSdiaSize = 0;
+    if (!batch || std::getenv("GSGPU_NO_SDIA")) return;
+    long long doff = 0;
+    int count = 0;
+    std::vector<SegSdiaDesc> descs;
+    for (size_t q = 0; q < pd.patches.size(); ++q) {
+        const HostPatch& P = pd.patches[q];
+        const DevPatch& D = L.dev[q];
+        SegSdiaDesc S;
+        S.row0 = segRow[q];
+        S.n = segRow[q + 1] - segRow[q];
+        int m[3], lo[3];
+        if (S.n == 0 || !patchBox(D, map.index.data() + P.offset, map.freeSize, S.row0, m, lo)) {
+            S.doff = doff;  // nh = 0: CSR rows
+            descs.push_back(S);
+            continue;
+        }
+        ++count;
+        for (int k = 0; k < 3; ++k) {
+            S.m[k] = m[k];
+            S.p[k] = k < D.dim ? D.p[k] : 0;
+            S.bn[k] = k < D.dim ? D.n[k] : 1;
+            S.W[k] = k < D.dim ? D.W[k] : 1;
+            S.lo[k] = k < D.dim ? lo[k] : 0;
+        }
+        S.band_off = D.band_off;
+        S.nh = launch::sdiaHalf(S.p);
+        S.doff = doff;
+        doff += (long long)S.nh * S.n;
+        descs.push_back(S);
+    }
+    if (std::getenv("GSGPU_BATCH_DEBUG"))
+        fprintf(stderr, "[batch] half-diagonal inner operator: %d of %zu problems, %lld values\n", count,
+                pd.patches.size(), doff);
+    if (count == 0) return;
+    segSdiaHost.swap(descs);
+    segSdiaSize = doff;
+    segSdiaOk = true;
 }
 
 // patch data, tables and the assembly buffers (everything but the pattern)
@@ -632,6 +691,10 @@ void Context::assemble(int precision) {
     if (mixed) {
         launch::gatherCsrDF(nnz, dSrc, bandDf, dOvfPtr, dOvfIdx, dValHi, dValLo, s);
         if (sdiaOk) launch::sdiaBuild(sdiaOp, sdiaBand, bandDf, dSdia, s);
+        if (segSdiaOk) {
+            if (!dSegSdia) allocN(arena, dSegSdia, segSdiaSize);
+            launch::segSdiaBuild(pat.n, dRowSeg, dSegSdiaDesc, bandDf, dSegSdia, s);
+        }
         launch::rhsRows<df32>(pat.n, dLvec, dLptr, dLidx, bandDf, dFptr, dFband, dFbidx, dDdof, dRhs, s);
     } else {
         launch::gatherCsr<double>(nnz, dSrc, dBand, dOvfPtr, dOvfIdx, dVal, s);

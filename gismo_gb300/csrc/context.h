@@ -174,10 +174,17 @@ struct Context {
     // of each stiffness combination (6) and each inner-product variant (2)
     void autotune(double* ms);
     float* dSdia = nullptr;
+    // batches: the half-diagonal inner operator of every problem (kernels_batch.cu), if all qualify
+    bool segSdiaOk = false;
+    std::vector<SegSdiaDesc> segSdiaHost;
+    long long segSdiaSize = 0;  // stored values
+    SegSdiaDesc* dSegSdiaDesc = nullptr;
+    float* dSegSdia = nullptr;
     float* dP32pad = nullptr;         // allocation of the inner CG direction with its zero padding
     int* dSdiaErr = nullptr;          // set by the TMA-fed product's bounded waits when they expire
     alignas(64) unsigned char sdiaMaps[256] = {};  // two CUtensorMap (diagonals, x) when TMA is used
     void setupSdia();
+    void setupSegSdia();
     Tab tabPf, tabCoef, tabGeo1, tabGeo2, tabPoint, tabSt[3], tabLd[3];
     Tab tabRow[3][5];  // [stage][degree along the stage axis]: interior rows of simple axes
     Tab tabRowB[3][5]; // the remaining rows

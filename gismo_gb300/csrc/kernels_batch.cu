@@ -5,6 +5,9 @@
 // grid-stride kernels (rows of converged segments are skipped after one rowSeg / done lookup);
 // dot products are per-row contributions summed per segment by one warp in a fixed order, so
 // the results do not depend on the launch shape.
+#include <algorithm>
+#include <type_traits>
+
 #include "context.h"
 #include "df32.cuh"
 #include "kernels_batch.h"
@@ -323,6 +326,113 @@ __global__ void __launch_bounds__(kB) k_ref_count(SegCg<float> B, SegRefine R) {
     if (s < B.nseg) R.st[s].total += B.st[s].iters;
 }
 
+// ---- half-diagonal FP32 inner operator of the problems (mixed solve) ----
+
+// d of every problem from the df32 band: one thread per batch row. The band entry of the problem's
+// row with box coordinates b and offset o is band_off + (c0 W0 + o0 + p0) + (c1 W1 + o1 + p1) n0 W0
+// + (c2 W2 + o2 + p2) n0 W0 n1 W1 with c = b + lo; offsets in the storage order of sdia.cu (the
+// centre line o0 = 0..p0 first, then the lines (o2, o1) >= (0, 1) lexicographically, o0 ascending).
+__global__ void __launch_bounds__(kB) k_seg_sdia_build(int n, const int* __restrict__ rowSeg,
+                                                      const SegSdiaDesc* __restrict__ desc,
+                                                      const df32* __restrict__ band, float* __restrict__ d) {
+    const int row = blockIdx.x * kB + threadIdx.x;
+    if (row >= n) return;
+    const SegSdiaDesc D = desc[rowSeg[row]];
+    if (D.nh == 0) return;
+    const int r = row - D.row0;
+    int b[3];
+    b[0] = r % D.m[0];
+    b[1] = (r / D.m[0]) % D.m[1];
+    b[2] = r / (D.m[0] * D.m[1]);
+    const long long n0W = (long long)D.bn[0] * D.W[0], n1W = (long long)D.bn[1] * D.W[1];
+    const long long rowBase = D.band_off + (long long)(b[0] + D.lo[0]) * D.W[0] +
+                              (long long)(b[1] + D.lo[1]) * D.W[1] * n0W +
+                              (long long)(b[2] + D.lo[2]) * D.W[2] * n0W * n1W;
+    auto value = [&](int o0, int o1, int o2) -> float {
+        const int c0 = b[0] + o0, c1 = b[1] + o1, c2 = b[2] + o2;
+        if (c0 < 0 || c0 >= D.m[0] || c1 < 0 || c1 >= D.m[1] || c2 < 0 || c2 >= D.m[2]) return 0.f;
+        return band[rowBase + (o0 + D.p[0]) + (long long)(o1 + D.p[1]) * n0W + (long long)(o2 + D.p[2]) * n0W * n1W].hi;
+    };
+    float* dr = d + D.doff + r;
+    const long long ns = D.n;
+    long long h = 0;
+    for (int o0 = 0; o0 <= D.p[0]; ++o0, ++h) dr[h * ns] = value(o0, 0, 0);
+    for (int o2 = 0; o2 <= D.p[2]; ++o2)
+        for (int o1 = o2 ? -D.p[1] : 1; o1 <= D.p[1]; ++o1)
+            for (int o0 = -D.p[0]; o0 <= D.p[0]; ++o0, ++h) dr[h * ns] = value(o0, o1, o2);
+}
+
+// row r (problem-local) of A x from the half diagonals dq = d + doff, x = xq[0..n): the row's own
+// values d[h n + r] times x[r + L_h] and the mirrored ones d[h n + r - L_h] times x[r - L_h]
+// (A(r, r - o) = A(r - o, r)). Every non-centre offset of the half box has L_h > 0 (the box is at
+// least 2p + 1 wide), so a term is taken when r + L_h < n (upper) or r - L_h >= 0 (mirrored); the
+// terms left out have a tensor point outside the box, whose stored value is 0. Terms in the order of
+// k_sdia32_dot (sdia.cu): the centre line, then per line its 2 (2 P0 + 1) products summed first.
+template <int P0>
+__device__ __forceinline__ float segSdiaRow(const SegSdiaDesc& D, int r, const float* __restrict__ dq,
+                                            const float* __restrict__ xq) {
+    constexpr int W0 = 2 * P0 + 1;
+    const int n = D.n;
+    const float* dh = dq + r;
+    float acc = 0.f;
+#pragma unroll
+    for (int o0 = 0; o0 <= P0; ++o0) {
+        if (r + o0 < n) acc = fmaf(__ldcg(dh), __ldg(xq + r + o0), acc);
+        if (o0 > 0 && r - o0 >= 0) acc = fmaf(__ldcg(dh - o0), __ldg(xq + r - o0), acc);
+        dh += n;
+    }
+    const int p1 = D.p[1], p2 = D.p[2], m0 = D.m[0], m1 = D.m[1];
+    for (int o2 = 0; o2 <= p2; ++o2)
+        for (int o1 = o2 ? -p1 : 1; o1 <= p1; ++o1) {
+            const int L21 = (o2 * m1 + o1) * m0;
+            float vu[W0], xu[W0], vd[W0], xd[W0];
+#pragma unroll
+            for (int k = 0; k < W0; ++k) {
+                const int L = L21 + k - P0;
+                const bool up = r + L < n, down = r - L >= 0;
+                vu[k] = up ? __ldcg(dh + (long long)k * n) : 0.f;
+                xu[k] = up ? __ldg(xq + r + L) : 0.f;
+                vd[k] = down ? __ldcg(dh + (long long)k * n - L) : 0.f;
+                xd[k] = down ? __ldg(xq + r - L) : 0.f;
+            }
+            float lsum = 0.f;
+#pragma unroll
+            for (int k = 0; k < W0; ++k) {
+                lsum = fmaf(vu[k], xu[k], lsum);
+                lsum = fmaf(vd[k], xd[k], lsum);
+            }
+            acc += lsum;
+            dh += (long long)W0 * n;
+        }
+    return acc;
+}
+
+// t = A p on the rows of running segments from the half diagonals (a problem without them: its CSR
+// row, one thread); rc0 = t .* p
+__global__ void __launch_bounds__(kB) k_seg_sdia(SegCg<float> B) {
+    for (int row = blockIdx.x * kB + threadIdx.x; row < B.n; row += gridDim.x * kB) {
+        const int s = B.rowSeg[row];
+        const SegState& S = B.st[s];
+        if (S.done || S.pause) continue;
+        const SegSdiaDesc& D = B.sdia[s];
+        const int r = row - D.row0;
+        const float* dq = B.sd + D.doff;
+        const float* xq = B.p + D.row0;
+        float acc = 0.f;
+        if (D.nh == 0) {
+            for (int k = B.ptr[row]; k < B.ptr[row + 1]; ++k)
+                acc = fmaf(B.val[k], B.p[B.coff ? row + int(B.coff[k]) : B.col[k]], acc);
+        } else switch (D.p[0]) {
+            case 1: acc = segSdiaRow<1>(D, r, dq, xq); break;
+            case 2: acc = segSdiaRow<2>(D, r, dq, xq); break;
+            case 3: acc = segSdiaRow<3>(D, r, dq, xq); break;
+            default: acc = segSdiaRow<4>(D, r, dq, xq); break;
+        }
+        B.t[row] = acc;
+        B.rc0[row] = double(acc) * double(B.p[row]);
+    }
+}
+
 }  // namespace
 
 namespace launch {
@@ -342,8 +452,27 @@ void segInit(const SegCg<T>& B, double tol, int maxit, cudaStream_t s) {
 template <typename T>
 void segIteration(const SegCg<T>& B, cudaStream_t s) {
     const int gs = gridFor(B.n, kB / kLanes);
-    if (B.coff) k_seg_spmv<T, true><<<gs, kB, 0, s>>>(B);
-    else k_seg_spmv<T, false><<<gs, kB, 0, s>>>(B);
+    bool halfDiag = false;
+    if constexpr (std::is_same<T, float>::value) {
+        if (B.sdia) {
+            // grid-stride over the rows with every block resident (48 registers: 5 blocks of 256 per
+            // SM), so no SM runs a second wave that others do not
+            static const int resident = [] {
+                int dev = 0, sms = 0, per = 0;
+                cudaGetDevice(&dev);
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_seg_sdia, kB, 0);
+                return std::max(1, sms * per);
+            }();
+            const long long need = (B.n + kB - 1) / kB;
+            k_seg_sdia<<<unsigned(std::max(1LL, std::min<long long>(need, resident))), kB, 0, s>>>(B);
+            halfDiag = true;
+        }
+    }
+    if (!halfDiag) {
+        if (B.coff) k_seg_spmv<T, true><<<gs, kB, 0, s>>>(B);
+        else k_seg_spmv<T, false><<<gs, kB, 0, s>>>(B);
+    }
     k_seg_alpha<T><<<unsigned(B.nseg > 0 ? B.nseg : 1), kSegB, 0, s>>>(B);
     k_seg_update<T><<<gridFor(B.n, kB), kB, 0, s>>>(B);
     k_seg_scalars<T><<<unsigned(B.nseg > 0 ? B.nseg : 1), kSegB, 0, s>>>(B);
@@ -376,6 +505,10 @@ void refineReplace(const SegCg<float>& B, const SegRefine& R, double tol, int ma
 
 void refineCount(const SegCg<float>& B, const SegRefine& R, cudaStream_t s) {
     k_ref_count<<<(B.nseg + kB - 1) / kB, kB, 0, s>>>(B, R);
+}
+
+void segSdiaBuild(int n, const int* rowSeg, const SegSdiaDesc* desc, const df32* band, float* d, cudaStream_t s) {
+    if (n > 0) k_seg_sdia_build<<<unsigned((n + kB - 1) / kB), kB, 0, s>>>(n, rowSeg, desc, band, d);
 }
 
 template void segDinv<double>(const SegCg<double>&, const int*, cudaStream_t);

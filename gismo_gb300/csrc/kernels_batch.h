@@ -19,6 +19,19 @@ struct SegState {
     double last_true;
 };
 
+// Half-diagonal storage of the FP32 inner operator of one batch problem whose free dofs are one box
+// of m0 x m1 x m2 patch-local functions numbered lexicographically (the single-patch form of
+// SdiaOp, sdia.cu, without padding): d[doff + h n + r] = A(r, r + o_h) for the nh offsets o_h of the
+// half neighbour box, 0 where r + o_h leaves the box; r = row - row0 is the problem-local row.
+// nh = 0: the problem does not have that shape, its rows use the CSR values
+struct SegSdiaDesc {
+    long long doff = 0;      // the problem's first stored value
+    long long band_off = 0;  // the patch's band offset
+    int row0 = 0, n = 0, nh = 0;
+    int m[3] = {1, 1, 1}, p[3] = {0, 0, 0};
+    int bn[3] = {1, 1, 1}, W[3] = {1, 1, 1}, lo[3] = {0, 0, 0};  // patch dof counts, band widths, box corner
+};
+
 // The batch matrix is one CSR matrix (block diagonal, rows of segment s in [segRow[s], segRow[s+1]))
 // swept by row-parallel kernels; rowSeg maps a row to its segment. Dot products go through
 // per-row contributions (rc0, rc1) that one warp per segment sums in a fixed order.
@@ -31,6 +44,10 @@ struct SegCg {
     const int* col = nullptr;
     const int16_t* coff = nullptr;
     const T* val = nullptr;
+    // FP32 recursion of the mixed solve: if set, the products use the problems' half diagonals sd
+    // (described by sdia[segment]) instead of the CSR values
+    const SegSdiaDesc* sdia = nullptr;
+    const float* sd = nullptr;
     const T* dinv = nullptr;
     const T* b = nullptr;
     T *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *t = nullptr;
@@ -74,5 +91,7 @@ void refineRhs(const SegCg<float>& B, const SegRefine& R, cudaStream_t s);
 void refineReplace(const SegCg<float>& B, const SegRefine& R, double tol, int maxref, cudaStream_t s);
 // per segment: the recursion's iteration count into the outer state's total
 void refineCount(const SegCg<float>& B, const SegRefine& R, cudaStream_t s);
+// the half diagonals of every problem of an n-row batch from the df32 band (hi parts)
+void segSdiaBuild(int n, const int* rowSeg, const SegSdiaDesc* desc, const df32* band, float* d, cudaStream_t s);
 }  // namespace launch
 }  // namespace gsgpu

@@ -49,7 +49,8 @@ struct Request {
 
 // device bytes a single-patch request needs in the batch path: the contraction intermediates and
 // fields of its layout, the CSR system (upper bound prod_k n_k (2p_k + 1) on its non-zeros) with
-// its FP64 values, gather sources, columns, FP32 halves, and the solver vectors
+// its FP64 values, gather sources, columns, FP32 halves, the half diagonals of the FP32 inner
+// operator (at most nnz / 2 + n values), and the solver vectors
 double estimateBytes(const ProblemDesc& pd) {
     Layout L;
     buildLayout(pd, L);
@@ -61,7 +62,7 @@ double estimateBytes(const ProblemDesc& pd) {
         }
     const double layout = 8.0 * double(L.s + L.u + L.band + L.fields + L.lfield + L.y1 + L.y2 + L.lv1 + L.lv2 +
                                        L.lvec + L.ntab + L.ngtab + L.npf + 2 * L.coefs);
-    return layout + nnz * (8 + 4 + 4 + 2 + 8) + n * (8 * 12 + 4 * 8 + 4) + (1 << 20);
+    return layout + nnz * (8 + 4 + 4 + 2 + 8 + 2) + n * (8 * 12 + 4 * 8 + 4 + 4) + (1 << 20);
 }
 
 }  // namespace

@@ -47,6 +47,7 @@ void Context::batchSetup() {
     allocN(arena, dSegOuter, nseg);
     allocN(arena, dSegDone, 2);  // [inner done, outer done]
     allocN(arena, dSegXdf, std::max(1, pat.n));
+    if (segSdiaOk) upload(arena, dSegSdiaDesc, segSdiaHost, stream);
 }
 
 // one chunk of 16 iterations as a captured graph (per precision, once per context)
@@ -142,6 +143,10 @@ void Context::solveBatch(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
         B.p = dP32;
         B.t = dT32;
         B.outer = dSegOuter;
+        if (segSdiaOk) {
+            B.sdia = dSegSdiaDesc;
+            B.sd = dSegSdia;
+        }
         SegRefine R;
         R.hi = dValHi;
         R.lo = dValLo;
