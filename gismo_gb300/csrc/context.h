@@ -179,6 +179,9 @@ struct Context {
     std::vector<SegSdiaDesc> segSdiaHost;
     long long segSdiaSize = 0;  // stored values
     SegSdiaDesc* dSegSdiaDesc = nullptr;
+    int nPiece = 0;  // pieces of the batch's segments (SegCg::pieceRow)
+    int *dPieceRow = nullptr, *dPieceSeg = nullptr, *dSegPiece = nullptr;
+    double* dPiecePart = nullptr;
     float* dSegSdia = nullptr;
     float* dP32pad = nullptr;         // allocation of the inner CG direction with its zero padding
     int* dSdiaErr = nullptr;          // set by the TMA-fed product's bounded waits when they expire

@@ -113,67 +113,114 @@ __global__ void __launch_bounds__(kB) k_seg_init_seg(SegCg<T> B, double tol, int
     }
 }
 
-// t = A p on the rows of running segments; rc0 = t .* p
+// a piece's segment is running (the test is uniform over the warp that owns the piece)
+template <typename T>
+__device__ __forceinline__ bool pieceRunning(const SegCg<T>& B, int j) {
+    const SegState& S = B.st[B.pieceSeg[j]];
+    return !S.done && !S.pause;
+}
+
+// the piece kernels: one warp per piece of kSegPiece = 32 rows, grid-stride over the pieces; the
+// piece's partial sums are the warp's shuffle trees (fixed order, no block barrier)
+__device__ __forceinline__ int warpId() { return int((blockIdx.x * blockDim.x + threadIdx.x) >> 5); }
+__device__ __forceinline__ int warpCount() { return int((gridDim.x * blockDim.x) >> 5); }
+
+// t = A p on the pieces of running segments (kLanes lanes per CSR row); pp0[piece] = its part of p.t
 template <typename T, bool REL>
 __global__ void __launch_bounds__(kB) k_seg_spmv(SegCg<T> B) {
-    constexpr int rpb = kB / kLanes;
+    constexpr int rpw = 32 / kLanes;  // rows per warp pass
     const int lane = threadIdx.x % kLanes;
-    for (int base = blockIdx.x * rpb; base < B.n; base += gridDim.x * rpb) {
-        const int row = base + threadIdx.x / kLanes;
-        const bool act = row < B.n && rowActive(B.rowSeg, B.st, row);
-        T acc = T(0);
-        if (act)
-            dev::rowMac<kLanes, kUnroll, REL>(
-                row, B.ptr[row], B.ptr[row + 1], lane, B.col, B.coff, [&](int k) { return B.val[k]; },
-                [&](int c) { return B.p[c]; }, [&](T v, T x) { acc += v * x; });
-        for (int o = kLanes / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (act && lane == 0) {
-            B.t[row] = acc;
-            B.rc0[row] = double(acc) * double(B.p[row]);
+    for (int j = warpId(); j < B.npiece; j += warpCount()) {
+        if (!pieceRunning(B, j)) continue;
+        const int r1 = B.pieceRow[j + 1];
+        double c = 0.0;
+        for (int base = B.pieceRow[j]; base < r1; base += rpw) {
+            const int row = base + int(threadIdx.x & 31) / kLanes;
+            const bool act = row < r1;
+            T acc = T(0);
+            if (act)
+                dev::rowMac<kLanes, kUnroll, REL>(
+                    row, B.ptr[row], B.ptr[row + 1], lane, B.col, B.coff, [&](int k) { return B.val[k]; },
+                    [&](int c) { return B.p[c]; }, [&](T v, T x) { acc += v * x; });
+            for (int o = kLanes / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (act && lane == 0) {
+                B.t[row] = acc;
+                c += double(acc) * double(B.p[row]);
+            }
+        }
+        c = warpSum(c);  // one tree per piece (the rows' terms were summed per lane first)
+        if ((threadIdx.x & 31) == 0) B.pp0[j] = c;
+    }
+}
+
+// one warp per segment: alpha = rho / p.Ap from the segment's piece partials
+template <typename T>
+__global__ void __launch_bounds__(kB) k_seg_alpha(SegCg<T> B) {
+    const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (s >= B.nseg) return;
+    const int done = B.st[s].done, pause = B.st[s].pause;
+    __syncwarp();  // every lane has read the flags before lane 0 may change them
+    if (done) return;
+    if (pause) {  // idle until the replacement; the pausing iteration's p update has run
+        if (lane == 0) B.st[s].pause = 2;
+        return;
+    }
+    const double pAp = warpRange(B.pp0, B.segPiece[s], B.segPiece[s + 1], lane);
+    if (lane == 0) B.st[s].alpha = B.st[s].rho / pAp;
+}
+
+// the warp's sum of the lanes' products a b as a double on lane 0. FP32 factors: each product is
+// exact as a double-float (TwoProd) and the shuffle tree adds double-floats on the FP32 pipe; a tree
+// of doubles (10 FP64 additions per warp and 32 rows for two sums) made the piece kernels FP64 bound
+// (GB300's FP64 pipe does 2 FMAs per clock per SM: 133-150 us per update of 8M rows against 56 us
+// for the row-parallel form). FP64 factors: the product and the tree in FP64.
+__device__ __forceinline__ double warpDot(float a, float b) {
+    float p, e;
+    twoProd(a, b, p, e);
+    df32 v(p, e);
+    for (int o = 16; o > 0; o >>= 1)
+        v = v + df32(__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o));
+    return double(v.hi) + double(v.lo);
+}
+__device__ __forceinline__ double warpDot(double a, double b) { return warpSum(a * b); }
+
+// x += alpha p; r -= alpha t; z = D^-1 r on the pieces of running segments; pp0, pp1[piece] = its
+// parts of r.r and r.z
+template <typename T>
+__global__ void __launch_bounds__(kB) k_seg_update(SegCg<T> B) {
+    for (int j = warpId(); j < B.npiece; j += warpCount()) {
+        if (!pieceRunning(B, j)) continue;
+        const int i = B.pieceRow[j] + int(threadIdx.x & 31);
+        T ri = T(0), zi = T(0);
+        if (i < B.pieceRow[j + 1]) {
+            const T alpha = T(B.st[B.pieceSeg[j]].alpha);
+            B.x[i] += alpha * B.p[i];
+            ri = B.r[i] - alpha * B.t[i];
+            B.r[i] = ri;
+            zi = B.dinv[i] * ri;
+            B.z[i] = zi;
+        }
+        const double rr = warpDot(ri, ri), rz = warpDot(ri, zi);
+        if ((threadIdx.x & 31) == 0) {
+            B.pp0[j] = rr;
+            B.pp1[j] = rz;
         }
     }
 }
 
-// one block per segment
+// one warp per segment: r.r and r.z from the piece partials, the stopping test, beta
 template <typename T>
-__global__ void __launch_bounds__(kSegB) k_seg_alpha(SegCg<T> B) {
-    const int s = blockIdx.x;
-    const int done = B.st[s].done, pause = B.st[s].pause;
-    __syncthreads();  // every thread has read the flags before thread 0 may change them
-    if (done) return;
-    if (pause) {  // idle until the replacement; the pausing iteration's p update has run
-        if (threadIdx.x == 0) B.st[s].pause = 2;
-        return;
-    }
-    const double pAp = blockRange(B.rc0, B.segRow[s], B.segRow[s + 1]);
-    if (threadIdx.x == 0) B.st[s].alpha = B.st[s].rho / pAp;
-}
-
-// x += alpha p; r -= alpha t; z = D^-1 r; rc0 = r .* r, rc1 = r .* z
-template <typename T>
-__global__ void __launch_bounds__(kB) k_seg_update(SegCg<T> B) {
-    for (int i = blockIdx.x * kB + threadIdx.x; i < B.n; i += gridDim.x * kB) {
-        const SegState& S = B.st[B.rowSeg[i]];
-        if (S.done || S.pause) continue;
-        const T alpha = T(S.alpha);
-        B.x[i] += alpha * B.p[i];
-        const T ri = B.r[i] - alpha * B.t[i];
-        B.r[i] = ri;
-        const T zi = B.dinv[i] * ri;
-        B.z[i] = zi;
-        B.rc0[i] = double(ri) * double(ri);
-        B.rc1[i] = double(ri) * double(zi);
-    }
-}
-
-// one block per segment
-template <typename T>
-__global__ void __launch_bounds__(kSegB) k_seg_scalars(SegCg<T> B) {
-    const int s = blockIdx.x;
-    if (B.st[s].done || B.st[s].pause) return;  // thread 0 changes them only after both sums
-    const double rr = blockRange(B.rc0, B.segRow[s], B.segRow[s + 1]);
-    const double rz = blockRange(B.rc1, B.segRow[s], B.segRow[s + 1]);
-    if (threadIdx.x == 0) {
+__global__ void __launch_bounds__(kB) k_seg_scalars(SegCg<T> B) {
+    const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (s >= B.nseg) return;
+    const bool skip = B.st[s].done || B.st[s].pause;
+    __syncwarp();  // lane 0 changes them only after every lane has read them
+    if (skip) return;
+    const double rr = warpRange(B.pp0, B.segPiece[s], B.segPiece[s + 1], lane);
+    const double rz = warpRange(B.pp1, B.segPiece[s], B.segPiece[s + 1], lane);
+    if (lane == 0) {
         SegState& S = B.st[s];
         S.iters += 1;
         S.relres = sqrt(rr) / S.bnorm;
@@ -407,29 +454,34 @@ __device__ __forceinline__ float segSdiaRow(const SegSdiaDesc& D, int r, const f
     return acc;
 }
 
-// t = A p on the rows of running segments from the half diagonals (a problem without them: its CSR
-// row, one thread); rc0 = t .* p
-__global__ void __launch_bounds__(kB) k_seg_sdia(SegCg<float> B) {
-    for (int row = blockIdx.x * kB + threadIdx.x; row < B.n; row += gridDim.x * kB) {
-        const int s = B.rowSeg[row];
-        const SegState& S = B.st[s];
-        if (S.done || S.pause) continue;
-        const SegSdiaDesc& D = B.sdia[s];
-        const int r = row - D.row0;
-        const float* dq = B.sd + D.doff;
-        const float* xq = B.p + D.row0;
-        float acc = 0.f;
-        if (D.nh == 0) {
-            for (int k = B.ptr[row]; k < B.ptr[row + 1]; ++k)
-                acc = fmaf(B.val[k], B.p[B.coff ? row + int(B.coff[k]) : B.col[k]], acc);
-        } else switch (D.p[0]) {
-            case 1: acc = segSdiaRow<1>(D, r, dq, xq); break;
-            case 2: acc = segSdiaRow<2>(D, r, dq, xq); break;
-            case 3: acc = segSdiaRow<3>(D, r, dq, xq); break;
-            default: acc = segSdiaRow<4>(D, r, dq, xq); break;
+// t = A p on the pieces of running segments from the half diagonals, one row per lane (a problem
+// without them: its CSR row, one lane); pp0[piece] = its part of p.t. Blocks of kBS threads: at
+// its 54 registers an SM holds 36 warps in blocks of 4 warps, 32 in blocks of 8
+constexpr int kBS = 128;
+__global__ void __launch_bounds__(kBS) k_seg_sdia(SegCg<float> B) {
+    for (int j = warpId(); j < B.npiece; j += warpCount()) {
+        if (!pieceRunning(B, j)) continue;
+        const int row = B.pieceRow[j] + int(threadIdx.x & 31);
+        float acc = 0.f, pr = 0.f;
+        if (row < B.pieceRow[j + 1]) {
+            const SegSdiaDesc& D = B.sdia[B.pieceSeg[j]];
+            const int r = row - D.row0;
+            const float* dq = B.sd + D.doff;
+            const float* xq = B.p + D.row0;
+            if (D.nh == 0) {
+                for (int k = B.ptr[row]; k < B.ptr[row + 1]; ++k)
+                    acc = fmaf(B.val[k], B.p[B.coff ? row + int(B.coff[k]) : B.col[k]], acc);
+            } else switch (D.p[0]) {
+                case 1: acc = segSdiaRow<1>(D, r, dq, xq); break;
+                case 2: acc = segSdiaRow<2>(D, r, dq, xq); break;
+                case 3: acc = segSdiaRow<3>(D, r, dq, xq); break;
+                default: acc = segSdiaRow<4>(D, r, dq, xq); break;
+            }
+            B.t[row] = acc;
+            pr = B.p[row];
         }
-        B.t[row] = acc;
-        B.rc0[row] = double(acc) * double(B.p[row]);
+        const double c = warpDot(acc, pr);
+        if ((threadIdx.x & 31) == 0) B.pp0[j] = c;
     }
 }
 
@@ -449,33 +501,43 @@ void segInit(const SegCg<T>& B, double tol, int maxit, cudaStream_t s) {
     k_seg_init_seg<T><<<segGrid(B.nseg), kB, 0, s>>>(B, tol, maxit);
 }
 
+// blocks of kB threads that are resident together for kernel k (grid-stride over the pieces with
+// every block resident: no SM runs a second wave that others do not)
+template <typename K>
+int residentBlocks(K k, int threads = kB) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, threads, 0);
+    return std::max(1, sms * per);
+}
+
 template <typename T>
 void segIteration(const SegCg<T>& B, cudaStream_t s) {
-    const int gs = gridFor(B.n, kB / kLanes);
+    const unsigned np = unsigned(std::max(1, (B.npiece + kB / 32 - 1) / (kB / 32)));  // blocks of kB / 32 pieces
     bool halfDiag = false;
     if constexpr (std::is_same<T, float>::value) {
         if (B.sdia) {
-            // grid-stride over the rows with every block resident (48 registers: 5 blocks of 256 per
-            // SM), so no SM runs a second wave that others do not
-            static const int resident = [] {
-                int dev = 0, sms = 0, per = 0;
-                cudaGetDevice(&dev);
-                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_seg_sdia, kB, 0);
-                return std::max(1, sms * per);
-            }();
-            const long long need = (B.n + kB - 1) / kB;
-            k_seg_sdia<<<unsigned(std::max(1LL, std::min<long long>(need, resident))), kB, 0, s>>>(B);
+            static const int resident = residentBlocks(k_seg_sdia, kBS);
+            const unsigned nps = unsigned(std::max(1, (B.npiece + kBS / 32 - 1) / (kBS / 32)));
+            k_seg_sdia<<<std::min<unsigned>(nps, resident), kBS, 0, s>>>(B);
             halfDiag = true;
         }
     }
     if (!halfDiag) {
-        if (B.coff) k_seg_spmv<T, true><<<gs, kB, 0, s>>>(B);
-        else k_seg_spmv<T, false><<<gs, kB, 0, s>>>(B);
+        if (B.coff) {
+            static const int resident = residentBlocks(k_seg_spmv<T, true>);
+            k_seg_spmv<T, true><<<std::min<unsigned>(np, resident), kB, 0, s>>>(B);
+        } else {
+            static const int resident = residentBlocks(k_seg_spmv<T, false>);
+            k_seg_spmv<T, false><<<std::min<unsigned>(np, resident), kB, 0, s>>>(B);
+        }
     }
-    k_seg_alpha<T><<<unsigned(B.nseg > 0 ? B.nseg : 1), kSegB, 0, s>>>(B);
-    k_seg_update<T><<<gridFor(B.n, kB), kB, 0, s>>>(B);
-    k_seg_scalars<T><<<unsigned(B.nseg > 0 ? B.nseg : 1), kSegB, 0, s>>>(B);
+    const unsigned ns = unsigned(segGrid(B.nseg));
+    k_seg_alpha<T><<<ns, kB, 0, s>>>(B);
+    static const int resident = residentBlocks(k_seg_update<T>);
+    k_seg_update<T><<<std::min<unsigned>(np, resident), kB, 0, s>>>(B);
+    k_seg_scalars<T><<<ns, kB, 0, s>>>(B);
     k_seg_pupd<T><<<gridFor(B.n, kB), kB, 0, s>>>(B);
 }
 

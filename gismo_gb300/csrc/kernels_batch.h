@@ -51,11 +51,22 @@ struct SegCg {
     const T* dinv = nullptr;
     const T* b = nullptr;
     T *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *t = nullptr;
-    double *rc0 = nullptr, *rc1 = nullptr;  // n each
+    double *rc0 = nullptr, *rc1 = nullptr;  // n each (start and residual replacements)
+    // pieces: every segment split into runs of at most kSegPiece rows (piece j: rows pieceRow[j] ..
+    // pieceRow[j + 1] - 1 of segment pieceSeg[j]; segment s owns pieces segPiece[s] .. segPiece[s + 1]
+    // - 1). The iterations' dot products go through one fixed-order partial per piece (pp0, pp1)
+    int npiece = 0;
+    const int* pieceRow = nullptr;  // npiece + 1
+    const int* pieceSeg = nullptr;  // npiece
+    const int* segPiece = nullptr;  // nseg + 1
+    double *pp0 = nullptr, *pp1 = nullptr;  // npiece each
     SegState* st = nullptr;
     const SegState* outer = nullptr;  // segments whose outer state is done take no part (refinement)
     int* ndone = nullptr;
 };
+
+// rows per piece: the lanes of one warp of the piece kernels
+constexpr int kSegPiece = 32;
 
 // iterative refinement: FP64 residual with the split operator hi + lo and FP64 x
 struct df32;

@@ -48,6 +48,23 @@ void Context::batchSetup() {
     allocN(arena, dSegDone, 2);  // [inner done, outer done]
     allocN(arena, dSegXdf, std::max(1, pat.n));
     if (segSdiaOk) upload(arena, dSegSdiaDesc, segSdiaHost, stream);
+    // pieces of at most kSegPiece rows, aligned to the start of their segment (so a problem's sums
+    // do not depend on the other problems of the batch)
+    std::vector<int> pieceRow, pieceSeg, segPiece(nseg + 1, 0);
+    for (int j = 0; j < nseg; ++j) {
+        segPiece[j] = int(pieceSeg.size());
+        for (int r = segRow[j]; r < segRow[j + 1]; r += kSegPiece) {
+            pieceRow.push_back(r);
+            pieceSeg.push_back(j);
+        }
+    }
+    segPiece[nseg] = int(pieceSeg.size());
+    pieceRow.push_back(pat.n);
+    nPiece = int(pieceSeg.size());
+    upload(arena, dPieceRow, pieceRow, stream);
+    upload(arena, dPieceSeg, pieceSeg.empty() ? std::vector<int>(1, 0) : pieceSeg, stream);
+    upload(arena, dSegPiece, segPiece, stream);
+    allocN(arena, dPiecePart, 2LL * std::max(1, nPiece));
 }
 
 // one chunk of 16 iterations as a captured graph (per precision, once per context)
@@ -105,6 +122,12 @@ void Context::solveBatch(const gsgpu_solver_opts& o, gsgpu_solve_info& info) {
         B.coff = dColOff;
         B.rc0 = dSegRc0;
         B.rc1 = dSegRc1;
+        B.npiece = nPiece;
+        B.pieceRow = dPieceRow;
+        B.pieceSeg = dPieceSeg;
+        B.segPiece = dSegPiece;
+        B.pp0 = dPiecePart;
+        B.pp1 = dPiecePart + std::max(1, nPiece);
         B.st = dSegSt;
         B.ndone = dSegDone;
     };
